@@ -1,0 +1,330 @@
+"""Benchmark: LULESH Sedov FOM (zones*cycles/s, FP64) on the 150^3 problem.
+
+A step is one LagrangeLeapFrog cycle (timeIncrement! + lagrangeLeapFrog) of
+the 150^3 Sedov problem (3,375,000 elements, 11 regions, balance 1, cost 1,
+the reference's own arithmetic). Inputs are generated by the problem setup;
+the state (~2.6 GB) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+The reference arm times the CPU restatement of the reference (the oracle,
+OpenMP over all host cores): Julia, the reference's language, is not
+available on these machines.
+"""
+import argparse
+import ctypes
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "lulesh.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "FOM zones*cycles/s FP64 s=150"
+UNIT = "zones*cycles/s"
+NX = 150
+# Algorithmic bytes (minimal HBM traffic of the method, FP64 fields, int32
+# connectivity): 364 B per element + 152 B per node per cycle for the whole
+# step; the force kernel's share is 80 B per element (nodelist, p, q, ss, v,
+# volo, elemMass) + 48 B per node (x, y, z, xd, yd, zd).
+STEP_BYTES_PER_ELEM, STEP_BYTES_PER_NODE = 364, 152
+FORCE_BYTES_PER_ELEM, FORCE_BYTES_PER_NODE = 80, 48
+STATE_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"]
+
+
+def _measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f), "measured"
+    return {"hbm_gbs": 6800.0}, "fallback"
+
+
+def _profile_numbers():
+    """Per-launch ncu figures of k_force at 150^3, if a profile summary was committed."""
+    path = os.path.join(ROOT, "profiles", "k_force_s150_ncu.json")
+    if os.path.exists(path):
+        with open(path) as f:
+            return json.load(f)
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.QUERY,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sms.append(float(parts[1]))
+                maxs.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        if not sms:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+        sms.sort()
+        return {"sm_mhz": sms[len(sms) // 2], "sm_max_mhz": max(maxs), "reasons": sorted(reasons),
+                "samples": len(sms)}
+
+
+def _dist():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def max_over_ranks(value, world):
+    """Max of a float over the torch.distributed ranks (identity at one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([value], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_oracle_rate(nx, seconds, threads=0, min_cycles=2, warm=1):
+    """Oracle (reference restatement) zones*cycles/s over a time-bounded sample."""
+    import oracle
+    L = oracle.load(openmp=True)
+    if threads:
+        L.ora_set_threads(threads)
+    used = L.ora_max_threads()
+    d = oracle.OracleDomain(nx, nr=11)
+    for _ in range(warm):
+        d.time_increment()
+        d.lagrange_leapfrog()
+    n, t0 = 0, time.perf_counter()
+    while n < min_cycles or time.perf_counter() - t0 < seconds:
+        d.time_increment()
+        d.lagrange_leapfrog()
+        n += 1
+    dt = time.perf_counter() - t0
+    d.close()
+    return nx ** 3 * n / dt, used, n, dt
+
+
+def run_reference(args):
+    world, rank, _ = _dist()
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    L = oracle.load(openmp=True)
+    threads = L.ora_max_threads()
+    d = oracle.OracleDomain(args.nx, nr=11)
+    for _ in range(args.warmup):
+        d.time_increment()
+        d.lagrange_leapfrog()
+    budget = 180.0  # seconds of timed CPU work at most
+    n, t0 = 0, time.perf_counter()
+    while n < args.steps and (n < 1 or time.perf_counter() - t0 < budget):
+        d.time_increment()
+        d.lagrange_leapfrog()
+        n += 1
+    dt = time.perf_counter() - t0
+    value = args.nx ** 3 * n / dt
+    sample = (f"{n} of {args.steps} cycles of the {args.nx}^3 problem after {args.warmup} warm-up cycles"
+              + ("" if n == args.steps else f" (stopped at the {budget:.0f} s budget)"))
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"Sedov blast {args.nx}^3, 11 regions, balance 1, cost 1, FP64",
+                       "nx": args.nx, "parallelism": "none (CPU)", "l2": "state larger than L2"},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "Julia (the reference's language) is not installed; the reference arm is the "
+                    "oracle, a C++ restatement of src/domain.jl + src/utils.jl, OpenMP over all cores"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    world, rank, local = _dist()
+    import torch
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", init_method="env://")
+    torch.cuda.set_device(local)
+    import lulesh_gb300 as L
+
+    dev = local
+    prob = L.LuleshProblem(nx=args.nx, nr=11, balance=1, cost=1, mode=args.mode, device=dev)
+    g = L.Domain(prob)
+    E, N = g.numElem, g.numNode
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+
+    fma_s, add_s = ctypes.c_double(), ctypes.c_double()
+    L.load_library().lulesh_measure_fp64_peak(dev, ctypes.byref(fma_s), ctypes.byref(add_s))
+
+    # warm-up, then the timed region: exactly K cycles, device-resident, with
+    # per-kernel CUDA events on the library's stream
+    g.enable_timing(True)
+    L.run(g, g.cycle + args.warmup)
+    g.kernel_times()
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0 = g.cycle
+    with ClockSampler(dev) as clocks:
+        torch.cuda.synchronize(dev)
+        start.record(stream)
+        s = L.run(g, c0 + args.steps)
+        end.record(stream)
+        torch.cuda.synchronize(dev)
+    cycles = s["cycle"] - c0
+    ms = start.elapsed_time(end)
+    ms_max = max_over_ranks(ms, world)
+    barrier(world)
+    ktimes = g.kernel_times()
+    value = world * E * cycles / (ms_max * 1e-3)
+
+    # end to end through the reference-facing calls: the Domain state comes
+    # from pinned host buffers, then K x (timeIncrement!, lagrangeLeapFrog),
+    # each moving the step scalars, then the state goes back to the host
+    g.enable_timing(False)
+    host = {f: torch.empty(g.numElem if f in ("e", "p", "q", "v", "ss") else N, dtype=torch.float64,
+                           pin_memory=True).numpy() for f in STATE_FIELDS}
+    for f in STATE_FIELDS:
+        host[f][:] = g.field(f)
+    state_bytes = sum(a.nbytes for a in host.values())
+    scalar_bytes = 72  # the device step state struct, each way, per step
+    torch.cuda.synchronize(dev)
+    barrier(world)
+    t0 = time.perf_counter()
+    for f in STATE_FIELDS:
+        g.set_field(f, host[f])
+    for _ in range(cycles):
+        L.timeIncrement(g)
+        L.lagrangeLeapFrog(g)
+    for f in STATE_FIELDS:
+        host[f][:] = g.field(f)
+    e2e_s = max_over_ranks(time.perf_counter() - t0, world)
+    e2e = {"value": world * E * cycles / e2e_s, "unit": UNIT,
+           "h2d_bytes_per_step": scalar_bytes + state_bytes / cycles,
+           "d2h_bytes_per_step": scalar_bytes + state_bytes / cycles}
+
+    if rank != 0:
+        g.close()
+        return 0
+
+    peaks, peak_kind = _measured_peaks()
+    hbm = float(peaks.get("hbm_gbs", 6800.0))
+    force_ms = ktimes.get("k_force", 0.0) / cycles
+    dominant = max(ktimes, key=ktimes.get)
+    force_bytes = FORCE_BYTES_PER_ELEM * E + FORCE_BYTES_PER_NODE * N
+    achieved = force_bytes / (force_ms * 1e-3) / 1e9
+    prof = _profile_numbers()
+    traffic = prof.get("dram_bytes_per_launch") if prof else None
+    roofline = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                "frac": achieved / hbm, "traffic": traffic,
+                "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
+                "algorithmic_bytes_per_launch": force_bytes}
+    step_bytes = STEP_BYTES_PER_ELEM * E + STEP_BYTES_PER_NODE * N
+    step_gbs = step_bytes * cycles / (ms * 1e-3) / 1e9
+    fp64 = {"bound": "fp64", "peak_fma_per_s": fma_s.value, "peak_add_per_s": add_s.value,
+            "peak_source": "lulesh_measure_fp64_peak (this run, this GPU)"}
+    if prof and prof.get("fp64_inst_per_launch"):
+        rate = prof["fp64_inst_per_launch"] / (force_ms * 1e-3)
+        fp64.update({"kernel": "k_force", "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
+                     "fp64_inst_per_launch": prof["fp64_inst_per_launch"]})
+
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        rate, used, n, dt = cpu_oracle_rate(args.nx, args.cpu_seconds)
+        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"{n} cycles of the {args.nx}^3 problem in {dt:.1f} s (oracle, OpenMP)"}
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": cycles,
+            "warmup": args.warmup, "ms_per_step": ms_max / cycles, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"Sedov blast {args.nx}^3, 11 regions, balance 1, cost 1, FP64",
+                       "nx": args.nx, "elements": E, "nodes": N, "mode": args.mode,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "state larger than L2 (no flush)"},
+            "roofline": roofline,
+            "step_roofline": {"achieved": step_gbs, "peak": hbm, "unit": "GB/s", "frac": step_gbs / hbm,
+                              "algorithmic_bytes_per_cycle": step_bytes},
+            "fp64_roofline": fp64,
+            "kernel_ms_per_cycle": {k: v / cycles for k, v in ktimes.items()},
+            "dominant_kernel": dominant,
+            "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    g.close()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--nx", type=int, default=NX)
+    ap.add_argument("--mode", type=int, default=0)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be at least 3")
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

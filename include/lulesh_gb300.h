@@ -1,0 +1,191 @@
+/*
+ * lulesh_gb300.h - C ABI of the GB300 (sm_103a) LagrangeLeapFrog library.
+ *
+ * Drop-in for the single-rank timestep of JuliaLabs/LULESH.jl. A handle owns
+ * one Sedov problem whose nodal and element fields live on the GPU as FP64
+ * structure-of-arrays buffers; the host only sees the step's scalars unless it
+ * asks for a field. Every entry point returns a lulesh_status code (0 = OK).
+ *
+ * Plain C types only: a Julia `ccall`, a Python ctypes stub or C/C++ code can
+ * bind it directly. One handle is driven by one host thread at a time.
+ */
+#ifndef LULESH_GB300_H
+#define LULESH_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. The reference raises Julia exceptions at the same points. */
+typedef enum {
+  LULESH_OK = 0,
+  LULESH_ERR_VOLUME = 1,     /* any "Volume Error" (src/domain.jl:1104,1727,1758,2118,2169,2905,2926) */
+  LULESH_ERR_QSTOP = 2,      /* "QStopError" (src/domain.jl:2580) */
+  LULESH_ERR_BAD_BC = 3,     /* error("Error") on an invalid elemBC mask (src/domain.jl:2343) */
+  LULESH_ERR_CUDA = 4,       /* a CUDA runtime call failed */
+  LULESH_ERR_TIMEOUT = 5,    /* a bounded device wait ran out */
+  LULESH_ERR_ARGUMENT = 6,   /* bad argument (null pointer, unknown id, size mismatch) */
+  LULESH_ERR_MEMORY = 7      /* device allocation failed */
+} lulesh_status;
+
+/* Which reference check raised a LULESH_ERR_VOLUME (finer than the code). */
+typedef enum {
+  LULESH_SITE_NONE = 0,
+  LULESH_SITE_EARLY = 1,       /* integrateStressForElems, src/domain.jl:1104 */
+  LULESH_SITE_HOURGLASS = 2,   /* calcHourglassControlForElems, src/domain.jl:1727 */
+  LULESH_SITE_MID = 3,         /* calcVolumeForceForElems, src/domain.jl:1758 */
+  LULESH_SITE_KINEMATICS = 4,  /* calcKinematicsForElems, src/domain.jl:2118 */
+  LULESH_SITE_LAGRANGE = 5,    /* calcLagrangeElements, src/domain.jl:2169 */
+  LULESH_SITE_MATERIAL = 6,    /* applyMaterialPropertiesForElems, src/domain.jl:2905 */
+  LULESH_SITE_UPDATE = 7       /* updateVolumesForElems, src/domain.jl:2926 */
+} lulesh_site;
+
+/* Mode bits: 0 reproduces the reference exactly (including three defects of
+ * its restatement); each bit corrects one of them. 7 = LULESH 2.0 method. */
+enum {
+  LULESH_MODE_FAITHFUL = 0,
+  LULESH_FIX_NORMALS = 1,   /* calcElemNodeNormals face 5, src/domain.jl:1046-1055 */
+  LULESH_FIX_VOLUDER = 2,   /* calcElemVolumeDerivative node slots, src/domain.jl:1253-1255 */
+  LULESH_FIX_LXIP = 4,      /* xi-plus neighbour index, src/domain.jl:2349 */
+  LULESH_MODE_LULESH2 = 7
+};
+
+/* Problem description: LuleshProblem (src/LULESH.jl:31-49) for one rank. */
+typedef struct {
+  int32_t nx;             /* elements per edge (>= 1) */
+  int32_t nr;             /* regions (>= 1); src/domain.jl:338 */
+  int32_t balance;        /* region balance exponent */
+  int32_t cost;           /* region cost factor */
+  int32_t mode;           /* LULESH_MODE_* bits */
+  int32_t region_reps;    /* 0: regions cost nothing (the reference); 1: evaluate the
+                             EOS regReps[r] times per region r (LULESH 2.0 cost model;
+                             results are unchanged) */
+  int32_t keep_aux;       /* 1: also store fx,fy,fz,xdd,ydd,zdd,dxx,dyy,dzz,ql,qq each
+                             step, which the reference keeps in its Domain */
+  int32_t device;         /* CUDA device ordinal */
+  uint64_t region_seed;   /* seed of the region generator (Random.seed!(myRank)) */
+} lulesh_params;
+
+/* The Domain scalars that change every step (src/types.jl:98-107). */
+typedef struct {
+  double time;            /* domain.time */
+  double deltatime;       /* domain.deltatime */
+  double dtcourant;       /* domain.dtcourant */
+  double dthydro;         /* domain.dthydro */
+  int64_t cycle;          /* domain.cycle */
+  int32_t status;         /* lulesh_status of the last step */
+  int32_t site;           /* lulesh_site of the last LULESH_ERR_VOLUME */
+} lulesh_scalars;
+
+/* Field identifiers: the Domain vectors of src/types.jl:1-87. Double fields
+ * are FP64; index fields are int64 holding the raw values the Julia Domain
+ * stores; LULESH_F_ELEMBC is uint32. */
+typedef enum {
+  /* element-centred FP64 (numElem) */
+  LULESH_F_E = 0, LULESH_F_P, LULESH_F_Q, LULESH_F_QL, LULESH_F_QQ, LULESH_F_V, LULESH_F_VOLO,
+  LULESH_F_DELV, LULESH_F_VDOV, LULESH_F_AREALG, LULESH_F_SS, LULESH_F_ELEMMASS, LULESH_F_VNEW,
+  LULESH_F_DELV_XI, LULESH_F_DELV_ETA, LULESH_F_DELV_ZETA, LULESH_F_DELX_XI, LULESH_F_DELX_ETA,
+  LULESH_F_DELX_ZETA, LULESH_F_DXX, LULESH_F_DYY, LULESH_F_DZZ,
+  /* node-centred FP64 (numNode) */
+  LULESH_F_X = 32, LULESH_F_Y, LULESH_F_Z, LULESH_F_XD, LULESH_F_YD, LULESH_F_ZD, LULESH_F_XDD,
+  LULESH_F_YDD, LULESH_F_ZDD, LULESH_F_FX, LULESH_F_FY, LULESH_F_FZ, LULESH_F_NODALMASS,
+  /* int64 index fields (raw Julia values) */
+  LULESH_F_NODELIST = 64,       /* 8*numElem, 0-based node ids, element-major */
+  LULESH_F_LXIM, LULESH_F_LXIP, LULESH_F_LETAM, LULESH_F_LETAP, LULESH_F_LZETAM, LULESH_F_LZETAP,
+  LULESH_F_SYMMX, LULESH_F_SYMMY, LULESH_F_SYMMZ,
+  LULESH_F_NODEELEMCOUNT, LULESH_F_NODEELEMSTART, LULESH_F_NODEELEMCORNERLIST,
+  LULESH_F_MATELEMLIST, LULESH_F_REGNUMLIST, LULESH_F_REGELEMLIST, LULESH_F_REGCSR,
+  LULESH_F_REGREPS, LULESH_F_REGSORTED, LULESH_F_REGELEMSIZE,
+  /* uint32 */
+  LULESH_F_ELEMBC = 96
+} lulesh_field;
+
+/* Scalar identifiers: the Domain parameters of src/types.jl:91-126. */
+typedef enum {
+  LULESH_S_DTFIXED = 0, LULESH_S_DELTATIMEMULTLB, LULESH_S_DELTATIMEMULTUB, LULESH_S_STOPTIME,
+  LULESH_S_DTMAX, LULESH_S_DTHYDRO, LULESH_S_DTCOURANT, LULESH_S_TIME, LULESH_S_DELTATIME,
+  LULESH_S_U_CUT, LULESH_S_HGCOEF, LULESH_S_QSTOP, LULESH_S_MONOQ_MAX_SLOPE,
+  LULESH_S_MONOQ_LIMITER_MULT, LULESH_S_E_CUT, LULESH_S_P_CUT, LULESH_S_SS4O3, LULESH_S_Q_CUT,
+  LULESH_S_V_CUT, LULESH_S_QLC_MONOQ, LULESH_S_QQC_MONOQ, LULESH_S_QQC, LULESH_S_EOSVMAX,
+  LULESH_S_EOSVMIN, LULESH_S_PMIN, LULESH_S_EMIN, LULESH_S_DVOVMAX, LULESH_S_REFDENS,
+  LULESH_S_CYCLE, LULESH_S_COUNT
+} lulesh_scalar;
+
+typedef struct lulesh_domain lulesh_domain;
+
+/* Fill *p with the reference defaults for an nx^3 problem (nr = 11 as the
+ * reference's TODO asks, balance = cost = 1, mode 0). */
+void lulesh_default_params(lulesh_params* p, int32_t nx);
+
+/* Domain(prob): builds the Sedov mesh, connectivity, boundary conditions,
+ * masses, energy deposit, initial dt and regions on the device.
+ * Replaces Domain(prob::LuleshProblem), src/domain.jl:467-771. */
+int lulesh_create(const lulesh_params* params, lulesh_domain** out);
+
+/* Releases every device and host resource of the handle. */
+int lulesh_destroy(lulesh_domain* dom);
+
+/* timeIncrement!(domain): host-side dt control, src/domain.jl:920-961. */
+int lulesh_time_increment(lulesh_domain* dom);
+
+/* lagrangeLeapFrog(domain): one step on the device, src/domain.jl:3067-3080.
+ * Copies the scalars in, runs the step kernels, copies dtcourant, dthydro and
+ * the status back. Returns the step status. */
+int lulesh_lagrange_leapfrog(lulesh_domain* dom);
+
+/* The examples/benchmark.jl:82-98 loop (timeIncrement! then lagrangeLeapFrog
+ * until time >= stoptime, stopping once cycle >= num_iters) run entirely on
+ * the device from a captured CUDA graph; dt is computed on the device.
+ * On return *out (if non-null) holds the final scalars. */
+int lulesh_run(lulesh_domain* dom, int64_t num_iters, lulesh_scalars* out);
+
+/* Current step scalars (time, deltatime, dtcourant, dthydro, cycle, status). */
+int lulesh_get_scalars(const lulesh_domain* dom, lulesh_scalars* out);
+
+/* Read / write one Domain scalar (getfield / setfield! on the Domain). */
+int lulesh_get_scalar(const lulesh_domain* dom, int32_t id, double* value);
+int lulesh_set_scalar(lulesh_domain* dom, int32_t id, double value);
+
+/* Number of entries of a field (numElem, numNode, 8*numElem, ...). */
+int lulesh_field_length(const lulesh_domain* dom, int32_t field, int64_t* count);
+
+/* Copy a field between the device and a caller-owned host buffer of exactly
+ * `count` entries (double, int64 or uint32 per the field). Synchronous. */
+int lulesh_download_field(lulesh_domain* dom, int32_t field, void* host, int64_t count);
+int lulesh_upload_field(lulesh_domain* dom, int32_t field, const void* host, int64_t count);
+
+/* verifyAndWriteFinalOutput's numbers (src/utils.jl:124-158): out[0] = e[1]
+ * (origin energy), out[1] = MaxAbsDiff, out[2] = TotalAbsDiff,
+ * out[3] = MaxRelDiff of the plane-0 symmetry check. */
+int lulesh_verify(lulesh_domain* dom, double out[4]);
+
+/* numElem and numNode of the handle. */
+int lulesh_sizes(const lulesh_domain* dom, int64_t* num_elem, int64_t* num_node);
+
+/* The CUDA stream (cudaStream_t) the handle launches on, for callers that
+ * order their own work or CUDA events against the step. */
+int lulesh_get_stream(lulesh_domain* dom, void** stream);
+
+/* Kernel timing: when enabled, each step records CUDA events around every
+ * kernel on the handle's stream; lulesh_kernel_times returns the summed
+ * milliseconds per kernel (names in the same order) and resets them. */
+int lulesh_enable_timing(lulesh_domain* dom, int32_t enable);
+int lulesh_kernel_times(lulesh_domain* dom, double* ms, int32_t max_kernels, int32_t* n_kernels);
+const char* lulesh_kernel_name(int32_t index);
+
+/* Diagnostic without a reference counterpart: measures the device's FP64
+ * FMA and add issue rates (instructions per second), the roof this FP64
+ * step is bound by. */
+int lulesh_measure_fp64_peak(int32_t device, double* fma_per_s, double* add_per_s);
+
+/* Human-readable text of a status code. */
+const char* lulesh_status_string(int32_t status);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LULESH_GB300_H */

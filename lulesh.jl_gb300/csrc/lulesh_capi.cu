@@ -1,0 +1,804 @@
+// C ABI of the plain (single problem) path: see include/lulesh_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "../../include/lulesh_gb300.h"
+#include "lulesh_internal.h"
+#include "lulesh_kernels.h"
+#include "lulesh_setup.h"
+#include "lulesh_device.cuh"
+
+using namespace lulesh;
+
+namespace {
+
+constexpr int kNumKernels = 5;
+const char* const kKernelNames[kNumKernels] = {"k_time_increment", "k_force", "k_node",
+                                               "k_kinematics", "k_material"};
+constexpr int kGraphCycles = 16;   // cycles per captured graph
+constexpr int kTimingCycles = 256; // cycles of kernel events held before a read-back
+constexpr int kPollLaunches = 4;   // graph launches between host polls
+constexpr int kPollCyclesTimed = 64;  // timed (graph-less) cycles between host polls
+
+struct HostScalars {
+  double s[LULESH_S_COUNT];
+};
+
+}  // namespace
+
+struct lulesh_domain {
+  lulesh_params params;
+  int64_t E = 0, N = 0;
+  double sc[LULESH_S_COUNT];  // Domain scalars (LULESH_S_*), cycle stored as double
+  int32_t status = 0, site = 0;
+  DevDomain dd{};
+  void* arena = nullptr;
+  cudaStream_t stream = nullptr;
+  DevState* hst = nullptr;  // pinned mirror of the device state
+  cudaGraphExec_t graph = nullptr;
+  int64_t graph_key = -1;
+  // host copies of what only the host uses
+  std::vector<int> symmX, symmY, symmZ;
+  std::vector<int64_t> regNumList, regElemlist, regCSR, regReps, regSorted, regElemSize;
+  // timing: a ring of kTimingCycles cycles x (kNumKernels+1) events, read
+  // back when full or when the caller asks, so timed runs never stall per cycle
+  bool timing = false;
+  std::vector<cudaEvent_t> ring;
+  int ring_used = 0;
+  double kernel_ms[kNumKernels] = {};
+  int64_t cycle_i() const { return (int64_t)sc[LULESH_S_CYCLE]; }
+};
+
+static int cuda_fail(cudaError_t e) {
+  if (e == cudaSuccess) return LULESH_OK;
+  std::fprintf(stderr, "liblulesh_gb300: CUDA error %s\n", cudaGetErrorString(e));
+  return LULESH_ERR_CUDA;
+}
+#define CK(call) do { int rc_ = cuda_fail(call); if (rc_) return rc_; } while (0)
+
+static Params make_params(const lulesh_domain* d) {
+  Params p;
+  p.u_cut = d->sc[LULESH_S_U_CUT];
+  p.hgcoef = d->sc[LULESH_S_HGCOEF];
+  p.qstop = d->sc[LULESH_S_QSTOP];
+  p.monoq_max_slope = d->sc[LULESH_S_MONOQ_MAX_SLOPE];
+  p.monoq_limiter_mult = d->sc[LULESH_S_MONOQ_LIMITER_MULT];
+  p.e_cut = d->sc[LULESH_S_E_CUT];
+  p.p_cut = d->sc[LULESH_S_P_CUT];
+  p.q_cut = d->sc[LULESH_S_Q_CUT];
+  p.v_cut = d->sc[LULESH_S_V_CUT];
+  p.qlc_monoq = d->sc[LULESH_S_QLC_MONOQ];
+  p.qqc_monoq = d->sc[LULESH_S_QQC_MONOQ];
+  p.qqc = d->sc[LULESH_S_QQC];
+  p.eosvmax = d->sc[LULESH_S_EOSVMAX];
+  p.eosvmin = d->sc[LULESH_S_EOSVMIN];
+  p.pmin = d->sc[LULESH_S_PMIN];
+  p.emin = d->sc[LULESH_S_EMIN];
+  p.dvovmax = d->sc[LULESH_S_DVOVMAX];
+  p.refdens = d->sc[LULESH_S_REFDENS];
+  p.dtfixed = d->sc[LULESH_S_DTFIXED];
+  p.deltatimemultlb = d->sc[LULESH_S_DELTATIMEMULTLB];
+  p.deltatimemultub = d->sc[LULESH_S_DELTATIMEMULTUB];
+  p.stoptime = d->sc[LULESH_S_STOPTIME];
+  p.dtmax = d->sc[LULESH_S_DTMAX];
+  return p;
+}
+
+// Maps kernel status bits to (status, site) in the reference's check order.
+static void decode_status(unsigned bits, int32_t* status, int32_t* site) {
+  *status = LULESH_OK;
+  *site = LULESH_SITE_NONE;
+  if (!bits) return;
+  if (bits & ST_EARLY) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_EARLY; return; }
+  if (bits & ST_HOURGLASS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_HOURGLASS; return; }
+  if (bits & ST_KINEMATICS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_KINEMATICS; return; }
+  if (bits & ST_BAD_BC) { *status = LULESH_ERR_BAD_BC; return; }
+  if (bits & ST_QSTOP) { *status = LULESH_ERR_QSTOP; return; }
+  if (bits & ST_MATERIAL) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_MATERIAL; return; }
+  if (bits & ST_UPDATE) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_UPDATE; return; }
+}
+
+static void state_to_device_mirror(lulesh_domain* d) {
+  DevState* s = d->hst;
+  s->time = d->sc[LULESH_S_TIME];
+  s->deltatime = d->sc[LULESH_S_DELTATIME];
+  s->dtcourant = d->sc[LULESH_S_DTCOURANT];
+  s->dthydro = d->sc[LULESH_S_DTHYDRO];
+  s->cycle = (long long)d->sc[LULESH_S_CYCLE];
+  s->acc_courant = kInfBits;
+  s->acc_hydro = kInfBits;
+  s->status = 0u;
+  s->done = 0;
+  s->iters_left = 0;
+  s->first = 1;
+}
+
+static void state_from_device_mirror(lulesh_domain* d) {
+  DevState* s = d->hst;
+  d->sc[LULESH_S_TIME] = s->time;
+  d->sc[LULESH_S_DELTATIME] = s->deltatime;
+  double dtc = s->dtcourant, dth = s->dthydro;
+  if (s->acc_courant != kInfBits) { unsigned long long b = s->acc_courant; std::memcpy(&dtc, &b, 8); }
+  if (s->acc_hydro != kInfBits) { unsigned long long b = s->acc_hydro; std::memcpy(&dth, &b, 8); }
+  d->sc[LULESH_S_DTCOURANT] = dtc;
+  d->sc[LULESH_S_DTHYDRO] = dth;
+  d->sc[LULESH_S_CYCLE] = (double)s->cycle;
+  decode_status(s->status, &d->status, &d->site);
+}
+
+// ---------------------------------------------------------------------------
+// device memory layout
+// ---------------------------------------------------------------------------
+namespace {
+struct Carver {
+  char* base;
+  size_t off = 0;
+  template <class T> T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
+    off += n * sizeof(T);
+    return p;
+  }
+};
+}  // namespace
+
+static size_t layout(DevDomain& dd, char* base, int64_t E, int64_t N, bool aux) {
+  Carver c{base};
+  dd.x = c.take<double>(N); dd.y = c.take<double>(N); dd.z = c.take<double>(N);
+  dd.xd = c.take<double>(N); dd.yd = c.take<double>(N); dd.zd = c.take<double>(N);
+  dd.nodalMass = c.take<double>(N); dd.inv_nodalMass = c.take<double>(N);
+  if (aux) {
+    dd.xdd = c.take<double>(N); dd.ydd = c.take<double>(N); dd.zdd = c.take<double>(N);
+    dd.fx = c.take<double>(N); dd.fy = c.take<double>(N); dd.fz = c.take<double>(N);
+  } else {
+    dd.xdd = dd.ydd = dd.zdd = dd.fx = dd.fy = dd.fz = nullptr;
+  }
+  dd.nodeBC = c.take<unsigned char>(N);
+  dd.nodeElemStart = c.take<int>(N + 1);
+  dd.cornerList = c.take<int>(8 * E);
+  dd.nodelist = c.take<int>(8 * E);
+  dd.e = c.take<double>(E); dd.p = c.take<double>(E); dd.q = c.take<double>(E); dd.v = c.take<double>(E);
+  dd.volo = c.take<double>(E); dd.inv_volo = c.take<double>(E); dd.elemMass = c.take<double>(E);
+  dd.ss = c.take<double>(E); dd.ql = c.take<double>(E); dd.qq = c.take<double>(E);
+  dd.vnew = c.take<double>(E); dd.delv = c.take<double>(E); dd.arealg = c.take<double>(E);
+  dd.vdov = c.take<double>(E);
+  dd.delv_xi = c.take<double>(E); dd.delv_eta = c.take<double>(E); dd.delv_zeta = c.take<double>(E);
+  dd.delx_xi = c.take<double>(E); dd.delx_eta = c.take<double>(E); dd.delx_zeta = c.take<double>(E);
+  if (aux) {
+    dd.dxx = c.take<double>(E); dd.dyy = c.take<double>(E); dd.dzz = c.take<double>(E);
+  } else {
+    dd.dxx = dd.dyy = dd.dzz = nullptr;
+  }
+  dd.elemBC = c.take<unsigned int>(E);
+  dd.lxim = c.take<int>(E); dd.lxip = c.take<int>(E); dd.letam = c.take<int>(E);
+  dd.letap = c.take<int>(E); dd.lzetam = c.take<int>(E); dd.lzetap = c.take<int>(E);
+  dd.regElemlist0 = nullptr;
+  dd.regOfSlot = nullptr;
+  dd.fcx = c.take<double>(8 * E); dd.fcy = c.take<double>(8 * E); dd.fcz = c.take<double>(8 * E);
+  dd.st = c.take<DevState>(1);
+  return c.off + 256;
+}
+
+template <class T>
+static int h2d(T* dst, const T* src, size_t n, cudaStream_t s) {
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return LULESH_OK;
+}
+template <class T>
+static int d2h(T* dst, const T* src, size_t n, cudaStream_t s) {
+  CK(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+  return LULESH_OK;
+}
+
+static void set_default_scalars(double* sc) {
+  // src/domain.jl:663-701
+  sc[LULESH_S_DTFIXED] = -1.0e-6;
+  sc[LULESH_S_DELTATIMEMULTLB] = 1.1;
+  sc[LULESH_S_DELTATIMEMULTUB] = 1.2;
+  sc[LULESH_S_STOPTIME] = 1.0e-2;
+  sc[LULESH_S_DTMAX] = 1.0e-2;
+  sc[LULESH_S_DTHYDRO] = 1e20;
+  sc[LULESH_S_DTCOURANT] = 1e20;
+  sc[LULESH_S_TIME] = 0.0;
+  sc[LULESH_S_DELTATIME] = 0.0;
+  sc[LULESH_S_U_CUT] = 1.0e-7;
+  sc[LULESH_S_HGCOEF] = 3.0;
+  sc[LULESH_S_QSTOP] = 1.0e+12;
+  sc[LULESH_S_MONOQ_MAX_SLOPE] = 1.0;
+  sc[LULESH_S_MONOQ_LIMITER_MULT] = 2.0;
+  sc[LULESH_S_E_CUT] = 1.0e-7;
+  sc[LULESH_S_P_CUT] = 1.0e-7;
+  sc[LULESH_S_SS4O3] = 4.0 / 3.0;
+  sc[LULESH_S_Q_CUT] = 1.0e-7;
+  sc[LULESH_S_V_CUT] = 1.0e-10;
+  sc[LULESH_S_QLC_MONOQ] = 0.5;
+  sc[LULESH_S_QQC_MONOQ] = 2.0 / 3.0;
+  sc[LULESH_S_QQC] = 2.0;
+  sc[LULESH_S_EOSVMAX] = 1.0e+9;
+  sc[LULESH_S_EOSVMIN] = 1.0e-9;
+  sc[LULESH_S_PMIN] = 0.0;
+  sc[LULESH_S_EMIN] = -1.0e+15;
+  sc[LULESH_S_DVOVMAX] = 0.1;
+  sc[LULESH_S_REFDENS] = 1.0;
+  sc[LULESH_S_CYCLE] = 0.0;
+}
+
+static int upload_node_bc(lulesh_domain* d) {
+  std::vector<unsigned char> bc(d->N, 0);
+  for (int v : d->symmX) if (v >= 0 && v < d->N) bc[v] |= 1u;
+  for (int v : d->symmY) if (v >= 0 && v < d->N) bc[v] |= 2u;
+  for (int v : d->symmZ) if (v >= 0 && v < d->N) bc[v] |= 4u;
+  int rc = h2d(d->dd.nodeBC, bc.data(), bc.size(), d->stream);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(d->stream));
+  return LULESH_OK;
+}
+
+static void drop_graph(lulesh_domain* d) {
+  if (d->graph) cudaGraphExecDestroy(d->graph);
+  d->graph = nullptr;
+  d->graph_key = -1;
+}
+
+// ---------------------------------------------------------------------------
+// step launch
+// ---------------------------------------------------------------------------
+static int collect_times(lulesh_domain* d) {
+  if (d->ring_used == 0) return LULESH_OK;
+  const int stride = kNumKernels + 1;
+  CK(cudaEventSynchronize(d->ring[(d->ring_used - 1) * stride + kNumKernels]));
+  for (int c = 0; c < d->ring_used; ++c)
+    for (int k = 0; k < kNumKernels; ++k) {
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, d->ring[c * stride + k], d->ring[c * stride + k + 1]));
+      d->kernel_ms[k] += ms;
+    }
+  d->ring_used = 0;
+  return LULESH_OK;
+}
+
+static int ensure_ring(lulesh_domain* d) {
+  if (!d->ring.empty()) return LULESH_OK;
+  d->ring.assign((size_t)kTimingCycles * (kNumKernels + 1), nullptr);
+  for (auto& ev : d->ring) CK(cudaEventCreate(&ev));
+  return LULESH_OK;
+}
+
+// Launches one cycle's kernels; with timing on, brackets each kernel with
+// events from the ring (reading the ring back first when it is full).
+static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_increment,
+                       long long num_iters, bool timed) {
+  const bool aux = d->params.keep_aux != 0;
+  cudaStream_t s = d->stream;
+  cudaEvent_t* ev = nullptr;
+  if (timed) {
+    int rc = ensure_ring(d);
+    if (rc) return rc;
+    if (d->ring_used == kTimingCycles && (rc = collect_times(d))) return rc;
+    ev = &d->ring[(size_t)d->ring_used * (kNumKernels + 1)];
+    d->ring_used += 1;
+  }
+  if (ev) cudaEventRecord(ev[0], s);
+  if (with_time_increment) launch_time_increment(d->dd.st, prm, num_iters, s);
+  if (ev) cudaEventRecord(ev[1], s);
+  launch_force(d->dd, prm, s);
+  if (ev) cudaEventRecord(ev[2], s);
+  launch_node(d->dd, prm, aux, s);
+  if (ev) cudaEventRecord(ev[3], s);
+  launch_kinematics(d->dd, prm, aux, s);
+  if (ev) cudaEventRecord(ev[4], s);
+  launch_material(d->dd, prm, aux, s);
+  if (ev) cudaEventRecord(ev[5], s);
+  CK(cudaGetLastError());
+  return LULESH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+void lulesh_default_params(lulesh_params* p, int32_t nx) {
+  if (!p) return;
+  std::memset(p, 0, sizeof(*p));
+  p->nx = nx;
+  p->nr = 11;
+  p->balance = 1;
+  p->cost = 1;
+  p->mode = LULESH_MODE_FAITHFUL;
+  p->region_reps = 0;
+  p->keep_aux = 0;
+  p->device = 0;
+  p->region_seed = 0;
+}
+
+const char* lulesh_status_string(int32_t status) {
+  switch (status) {
+    case LULESH_OK: return "ok";
+    case LULESH_ERR_VOLUME: return "Volume Error";
+    case LULESH_ERR_QSTOP: return "QStopError";
+    case LULESH_ERR_BAD_BC: return "Error (invalid elemBC mask)";
+    case LULESH_ERR_CUDA: return "CUDA error";
+    case LULESH_ERR_TIMEOUT: return "device wait timed out";
+    case LULESH_ERR_ARGUMENT: return "bad argument";
+    case LULESH_ERR_MEMORY: return "device allocation failed";
+    default: return "unknown status";
+  }
+}
+
+const char* lulesh_kernel_name(int32_t index) {
+  return (index >= 0 && index < kNumKernels) ? kKernelNames[index] : "";
+}
+
+int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
+  if (!params || !out) return LULESH_ERR_ARGUMENT;
+  *out = nullptr;
+  const int nx = params->nx;
+  // 8*numElem must fit a 32-bit index
+  if (nx < 1 || nx > 640 || params->nr < 1 || params->balance < 0 || params->cost < 0 ||
+      params->mode < 0 || params->mode > 7)
+    return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(params->device));
+  lulesh_domain* d = new (std::nothrow) lulesh_domain();
+  if (!d) return LULESH_ERR_MEMORY;
+  d->params = *params;
+  HostMesh m;
+  build_mesh(m, nx, params->nr, params->balance, params->cost, params->region_seed);
+  d->E = m.E;
+  d->N = m.N;
+  set_default_scalars(d->sc);
+  d->sc[LULESH_S_DELTATIME] = m.deltatime;
+
+  const bool aux = params->keep_aux != 0;
+  DevDomain& dd = d->dd;
+  const size_t bytes = layout(dd, nullptr, m.E, m.N, aux);
+  cudaError_t err = cudaMalloc(&d->arena, bytes);
+  if (err != cudaSuccess) { delete d; cudaGetLastError(); return LULESH_ERR_MEMORY; }
+  layout(dd, (char*)d->arena, m.E, m.N, aux);
+  dd.E = (int)m.E;
+  dd.N = (int)m.N;
+  dd.nx = nx;
+  dd.mode = params->mode;
+  int rc = LULESH_OK;
+  auto fail = [&](int code) { lulesh_destroy(d); return code; };
+  if ((err = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking)) != cudaSuccess) return fail(cuda_fail(err));
+  if ((err = cudaMallocHost(&d->hst, sizeof(DevState))) != cudaSuccess) return fail(cuda_fail(err));
+  if ((err = cudaMemsetAsync(d->arena, 0, bytes, d->stream)) != cudaSuccess) return fail(cuda_fail(err));
+
+  const int64_t E = m.E, N = m.N;
+  cudaStream_t s = d->stream;
+  // host staging that must outlive the async copies
+  std::vector<int> nodelist_cm(8 * E), start(m.nodeElemStart);
+  for (int64_t e = 0; e < E; ++e)
+    for (int c = 0; c < 8; ++c) nodelist_cm[c * E + e] = m.nodelist[8 * e + c];
+  std::vector<double> inv_volo(E), inv_mass(N), ones(E, 1.0), e0(E, 0.0);
+  for (int64_t i = 0; i < E; ++i) inv_volo[i] = 1.0 / m.volo[i];
+  for (int64_t i = 0; i < N; ++i) inv_mass[i] = 1.0 / m.nodalMass[i];
+  e0[0] = m.einit;
+  if ((rc = h2d(dd.x, m.x.data(), N, s)) || (rc = h2d(dd.y, m.y.data(), N, s)) ||
+      (rc = h2d(dd.z, m.z.data(), N, s)) || (rc = h2d(dd.nodalMass, m.nodalMass.data(), N, s)) ||
+      (rc = h2d(dd.inv_nodalMass, inv_mass.data(), N, s)) ||
+      (rc = h2d(dd.nodeElemStart, start.data(), N + 1, s)) ||
+      (rc = h2d(dd.cornerList, m.cornerList.data(), 8 * E, s)) ||
+      (rc = h2d(dd.nodelist, nodelist_cm.data(), 8 * E, s)) ||
+      (rc = h2d(dd.volo, m.volo.data(), E, s)) || (rc = h2d(dd.inv_volo, inv_volo.data(), E, s)) ||
+      (rc = h2d(dd.elemMass, m.elemMass.data(), E, s)) || (rc = h2d(dd.v, ones.data(), E, s)) ||
+      (rc = h2d(dd.e, e0.data(), E, s)) || (rc = h2d(dd.elemBC, m.elemBC.data(), E, s)) ||
+      (rc = h2d(dd.lxim, m.lxim.data(), E, s)) || (rc = h2d(dd.lxip, m.lxip.data(), E, s)) ||
+      (rc = h2d(dd.letam, m.letam.data(), E, s)) || (rc = h2d(dd.letap, m.letap.data(), E, s)) ||
+      (rc = h2d(dd.lzetam, m.lzetam.data(), E, s)) || (rc = h2d(dd.lzetap, m.lzetap.data(), E, s)))
+    return fail(rc);
+  d->symmX = m.symmX; d->symmY = m.symmY; d->symmZ = m.symmZ;
+  d->regNumList = m.regNumList; d->regElemlist = m.regElemlist; d->regCSR = m.regCSR;
+  d->regReps = m.regReps; d->regSorted = m.regSorted; d->regElemSize = m.regElemSize;
+  if ((rc = upload_node_bc(d))) return fail(rc);
+  state_to_device_mirror(d);
+  if ((rc = h2d(dd.st, d->hst, 1, s))) return fail(rc);
+  if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(cuda_fail(err));
+  *out = d;
+  return LULESH_OK;
+}
+
+int lulesh_destroy(lulesh_domain* d) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  cudaSetDevice(d->params.device);
+  if (d->stream) cudaStreamSynchronize(d->stream);
+  drop_graph(d);
+  for (auto& ev : d->ring) if (ev) cudaEventDestroy(ev);
+  if (d->hst) cudaFreeHost(d->hst);
+  if (d->arena) cudaFree(d->arena);
+  if (d->stream) cudaStreamDestroy(d->stream);
+  delete d;
+  return LULESH_OK;
+}
+
+int lulesh_sizes(const lulesh_domain* d, int64_t* ne, int64_t* nn) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  if (ne) *ne = d->E;
+  if (nn) *nn = d->N;
+  return LULESH_OK;
+}
+
+int lulesh_get_stream(lulesh_domain* d, void** stream) {
+  if (!d || !stream) return LULESH_ERR_ARGUMENT;
+  *stream = (void*)d->stream;
+  return LULESH_OK;
+}
+
+int lulesh_time_increment(lulesh_domain* d) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  const Params prm = make_params(d);
+  double time = d->sc[LULESH_S_TIME], dt = d->sc[LULESH_S_DELTATIME];
+  long long cycle = (long long)d->sc[LULESH_S_CYCLE];
+  time_increment(time, dt, cycle, d->sc[LULESH_S_DTCOURANT], d->sc[LULESH_S_DTHYDRO], prm);
+  d->sc[LULESH_S_TIME] = time;
+  d->sc[LULESH_S_DELTATIME] = dt;
+  d->sc[LULESH_S_CYCLE] = (double)cycle;
+  return LULESH_OK;
+}
+
+int lulesh_lagrange_leapfrog(lulesh_domain* d) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  const Params prm = make_params(d);
+  state_to_device_mirror(d);
+  int rc;
+  if ((rc = h2d(d->dd.st, d->hst, 1, d->stream))) return rc;
+  if ((rc = launch_step(d, prm, false, 0, d->timing))) return rc;
+  if ((rc = d2h(d->hst, d->dd.st, 1, d->stream))) return rc;
+  CK(cudaStreamSynchronize(d->stream));
+  if (d->timing && (rc = collect_times(d))) return rc;
+  state_from_device_mirror(d);
+  return d->status;
+}
+
+int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  const Params prm = make_params(d);
+  state_to_device_mirror(d);
+  int rc;
+  cudaStream_t s = d->stream;
+  if ((rc = h2d(d->dd.st, d->hst, 1, s))) return rc;
+  // cycles the loop can still take: the first always runs, later ones while cycle < num_iters
+  const int64_t cyc0 = d->cycle_i();
+  const int64_t budget = std::max<int64_t>(1, num_iters - cyc0);
+  if (d->timing) {
+    // per-kernel events and no graph; the host polls the done flag every
+    // kPollCyclesTimed cycles
+    for (int64_t k = 0; k < budget; ++k) {
+      if ((rc = launch_step(d, prm, true, num_iters, true))) return rc;
+      if ((k + 1) % kPollCyclesTimed == 0) {
+        if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
+        CK(cudaStreamSynchronize(s));
+        if (d->hst->done) break;
+      }
+    }
+    if ((rc = collect_times(d))) return rc;
+  } else {
+    // one graph = kGraphCycles cycles; rebuilt when the parameters change
+    const int64_t key = num_iters;
+    if (!d->graph || d->graph_key != key) {
+      drop_graph(d);
+      cudaGraph_t g;
+      CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      for (int c = 0; c < kGraphCycles; ++c) launch_step(d, prm, true, num_iters, false);
+      CK(cudaStreamEndCapture(s, &g));
+      cudaError_t e = cudaGraphInstantiate(&d->graph, g, 0);
+      cudaGraphDestroy(g);
+      CK(e);
+      d->graph_key = key;
+    }
+    int64_t launched = 0;
+    for (;;) {
+      for (int k = 0; k < kPollLaunches && launched < budget; ++k) {
+        CK(cudaGraphLaunch(d->graph, s));
+        launched += kGraphCycles;
+      }
+      if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      if (d->hst->done || launched >= budget) break;
+    }
+  }
+  if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
+  CK(cudaStreamSynchronize(s));
+  state_from_device_mirror(d);
+  if (out) lulesh_get_scalars(d, out);
+  return d->status;
+}
+
+int lulesh_get_scalars(const lulesh_domain* d, lulesh_scalars* out) {
+  if (!d || !out) return LULESH_ERR_ARGUMENT;
+  out->time = d->sc[LULESH_S_TIME];
+  out->deltatime = d->sc[LULESH_S_DELTATIME];
+  out->dtcourant = d->sc[LULESH_S_DTCOURANT];
+  out->dthydro = d->sc[LULESH_S_DTHYDRO];
+  out->cycle = (int64_t)d->sc[LULESH_S_CYCLE];
+  out->status = d->status;
+  out->site = d->site;
+  return LULESH_OK;
+}
+
+int lulesh_get_scalar(const lulesh_domain* d, int32_t id, double* v) {
+  if (!d || !v || id < 0 || id >= LULESH_S_COUNT) return LULESH_ERR_ARGUMENT;
+  *v = d->sc[id];
+  return LULESH_OK;
+}
+
+int lulesh_set_scalar(lulesh_domain* d, int32_t id, double v) {
+  if (!d || id < 0 || id >= LULESH_S_COUNT) return LULESH_ERR_ARGUMENT;
+  if (id == LULESH_S_CYCLE && (v < 0 || v != std::floor(v))) return LULESH_ERR_ARGUMENT;
+  d->sc[id] = v;
+  drop_graph(d);  // parameters are baked into the captured graph
+  return LULESH_OK;
+}
+
+int lulesh_enable_timing(lulesh_domain* d, int32_t enable) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  d->timing = enable != 0;
+  for (double& t : d->kernel_ms) t = 0.0;
+  return LULESH_OK;
+}
+
+int lulesh_kernel_times(lulesh_domain* d, double* ms, int32_t max_kernels, int32_t* n) {
+  if (!d || !ms) return LULESH_ERR_ARGUMENT;
+  const int k = std::min<int32_t>(max_kernels, kNumKernels);
+  for (int i = 0; i < k; ++i) { ms[i] = d->kernel_ms[i]; d->kernel_ms[i] = 0.0; }
+  if (n) *n = kNumKernels;
+  return LULESH_OK;
+}
+
+// ---- field I/O --------------------------------------------------------------
+
+namespace {
+enum Kind { F64_ELEM, F64_NODE, I64, U32 };
+}
+
+static double* f64_ptr(lulesh_domain* d, int32_t f, Kind* kind) {
+  DevDomain& dd = d->dd;
+  *kind = (f < LULESH_F_X) ? F64_ELEM : F64_NODE;
+  switch (f) {
+    case LULESH_F_E: return dd.e;
+    case LULESH_F_P: return dd.p;
+    case LULESH_F_Q: return dd.q;
+    case LULESH_F_QL: return dd.ql;
+    case LULESH_F_QQ: return dd.qq;
+    case LULESH_F_V: return dd.v;
+    case LULESH_F_VOLO: return dd.volo;
+    case LULESH_F_DELV: return dd.delv;
+    case LULESH_F_VDOV: return dd.vdov;
+    case LULESH_F_AREALG: return dd.arealg;
+    case LULESH_F_SS: return dd.ss;
+    case LULESH_F_ELEMMASS: return dd.elemMass;
+    case LULESH_F_VNEW: return dd.vnew;
+    case LULESH_F_DELV_XI: return dd.delv_xi;
+    case LULESH_F_DELV_ETA: return dd.delv_eta;
+    case LULESH_F_DELV_ZETA: return dd.delv_zeta;
+    case LULESH_F_DELX_XI: return dd.delx_xi;
+    case LULESH_F_DELX_ETA: return dd.delx_eta;
+    case LULESH_F_DELX_ZETA: return dd.delx_zeta;
+    case LULESH_F_DXX: return dd.dxx;
+    case LULESH_F_DYY: return dd.dyy;
+    case LULESH_F_DZZ: return dd.dzz;
+    case LULESH_F_X: return dd.x;
+    case LULESH_F_Y: return dd.y;
+    case LULESH_F_Z: return dd.z;
+    case LULESH_F_XD: return dd.xd;
+    case LULESH_F_YD: return dd.yd;
+    case LULESH_F_ZD: return dd.zd;
+    case LULESH_F_XDD: return dd.xdd;
+    case LULESH_F_YDD: return dd.ydd;
+    case LULESH_F_ZDD: return dd.zdd;
+    case LULESH_F_FX: return dd.fx;
+    case LULESH_F_FY: return dd.fy;
+    case LULESH_F_FZ: return dd.fz;
+    case LULESH_F_NODALMASS: return dd.nodalMass;
+    default: return nullptr;
+  }
+}
+
+static int64_t field_len(const lulesh_domain* d, int32_t f) {
+  const int64_t E = d->E, N = d->N;
+  if (f >= LULESH_F_E && f <= LULESH_F_DZZ) return E;
+  if (f >= LULESH_F_X && f <= LULESH_F_NODALMASS) return N;
+  switch (f) {
+    case LULESH_F_NODELIST: return 8 * E;
+    case LULESH_F_LXIM: case LULESH_F_LXIP: case LULESH_F_LETAM: case LULESH_F_LETAP:
+    case LULESH_F_LZETAM: case LULESH_F_LZETAP: return E;
+    case LULESH_F_SYMMX: return (int64_t)d->symmX.size();
+    case LULESH_F_SYMMY: return (int64_t)d->symmY.size();
+    case LULESH_F_SYMMZ: return (int64_t)d->symmZ.size();
+    case LULESH_F_NODEELEMCOUNT: case LULESH_F_NODEELEMSTART: return N;
+    case LULESH_F_NODEELEMCORNERLIST: return 8 * E;
+    case LULESH_F_MATELEMLIST: case LULESH_F_REGNUMLIST: case LULESH_F_REGELEMLIST: return E;
+    case LULESH_F_REGCSR: case LULESH_F_REGREPS: case LULESH_F_REGSORTED: case LULESH_F_REGELEMSIZE:
+      return d->params.nr;
+    case LULESH_F_ELEMBC: return E;
+    default: return -1;
+  }
+}
+
+int lulesh_field_length(const lulesh_domain* d, int32_t f, int64_t* count) {
+  if (!d || !count) return LULESH_ERR_ARGUMENT;
+  const int64_t n = field_len(d, f);
+  if (n < 0) return LULESH_ERR_ARGUMENT;
+  *count = n;
+  return LULESH_OK;
+}
+
+static int* neighbour_ptr(lulesh_domain* d, int32_t f) {
+  switch (f) {
+    case LULESH_F_LXIM: return d->dd.lxim;
+    case LULESH_F_LXIP: return d->dd.lxip;
+    case LULESH_F_LETAM: return d->dd.letam;
+    case LULESH_F_LETAP: return d->dd.letap;
+    case LULESH_F_LZETAM: return d->dd.lzetam;
+    case LULESH_F_LZETAP: return d->dd.lzetap;
+    default: return nullptr;
+  }
+}
+
+int lulesh_download_field(lulesh_domain* d, int32_t f, void* host, int64_t count) {
+  if (!d || !host) return LULESH_ERR_ARGUMENT;
+  const int64_t n = field_len(d, f);
+  if (n < 0 || count != n) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  cudaStream_t s = d->stream;
+  const int64_t E = d->E, N = d->N;
+  int rc;
+  if (f < LULESH_F_NODELIST) {
+    Kind k;
+    double* p = f64_ptr(d, f, &k);
+    if (!p) return LULESH_ERR_ARGUMENT;  // an aux field without keep_aux
+    if ((rc = d2h((double*)host, p, n, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+  }
+  int64_t* out = (int64_t*)host;
+  if (f == LULESH_F_ELEMBC) {
+    if ((rc = d2h((unsigned int*)host, d->dd.elemBC, n, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+  }
+  if (int* nb = neighbour_ptr(d, f)) {
+    std::vector<int> t(n);
+    if ((rc = d2h(t.data(), nb, n, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    for (int64_t i = 0; i < n; ++i) out[i] = t[i];
+    return LULESH_OK;
+  }
+  switch (f) {
+    case LULESH_F_NODELIST: {
+      std::vector<int> t(8 * E);
+      if ((rc = d2h(t.data(), d->dd.nodelist, 8 * E, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      for (int64_t e = 0; e < E; ++e)
+        for (int c = 0; c < 8; ++c) out[8 * e + c] = t[c * E + e];
+      return LULESH_OK;
+    }
+    case LULESH_F_NODEELEMCOUNT:
+    case LULESH_F_NODEELEMSTART: {
+      std::vector<int> t(N + 1);
+      if ((rc = d2h(t.data(), d->dd.nodeElemStart, N + 1, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      for (int64_t i = 0; i < N; ++i)
+        out[i] = (f == LULESH_F_NODEELEMSTART) ? t[i] : t[i + 1] - t[i];
+      return LULESH_OK;
+    }
+    case LULESH_F_NODEELEMCORNERLIST: {
+      std::vector<int> t(8 * E);
+      if ((rc = d2h(t.data(), d->dd.cornerList, 8 * E, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      // Julia value: 1-based element-major corner k = 8*e + c + 1
+      for (int64_t i = 0; i < 8 * E; ++i) {
+        const int64_t v = t[i], c = v / E, e = v % E;
+        out[i] = 8 * e + c + 1;
+      }
+      return LULESH_OK;
+    }
+    case LULESH_F_SYMMX: for (int64_t i = 0; i < n; ++i) out[i] = d->symmX[i]; return LULESH_OK;
+    case LULESH_F_SYMMY: for (int64_t i = 0; i < n; ++i) out[i] = d->symmY[i]; return LULESH_OK;
+    case LULESH_F_SYMMZ: for (int64_t i = 0; i < n; ++i) out[i] = d->symmZ[i]; return LULESH_OK;
+    case LULESH_F_MATELEMLIST: for (int64_t i = 0; i < n; ++i) out[i] = i + 1; return LULESH_OK;
+    case LULESH_F_REGNUMLIST: std::copy(d->regNumList.begin(), d->regNumList.end(), out); return LULESH_OK;
+    case LULESH_F_REGELEMLIST: std::copy(d->regElemlist.begin(), d->regElemlist.end(), out); return LULESH_OK;
+    case LULESH_F_REGCSR: std::copy(d->regCSR.begin(), d->regCSR.end(), out); return LULESH_OK;
+    case LULESH_F_REGREPS: std::copy(d->regReps.begin(), d->regReps.end(), out); return LULESH_OK;
+    case LULESH_F_REGSORTED: std::copy(d->regSorted.begin(), d->regSorted.end(), out); return LULESH_OK;
+    case LULESH_F_REGELEMSIZE: std::copy(d->regElemSize.begin(), d->regElemSize.end(), out); return LULESH_OK;
+    default: return LULESH_ERR_ARGUMENT;
+  }
+}
+
+int lulesh_upload_field(lulesh_domain* d, int32_t f, const void* host, int64_t count) {
+  if (!d || !host) return LULESH_ERR_ARGUMENT;
+  const int64_t n = field_len(d, f);
+  if (n < 0 || count != n) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  cudaStream_t s = d->stream;
+  const int64_t E = d->E, N = d->N;
+  int rc;
+  if (f < LULESH_F_NODELIST) {
+    Kind k;
+    double* p = f64_ptr(d, f, &k);
+    if (!p) return LULESH_ERR_ARGUMENT;
+    const double* h = (const double*)host;
+    if ((rc = h2d(p, h, n, s))) return rc;
+    // derived reciprocals follow the field
+    if (f == LULESH_F_VOLO || f == LULESH_F_NODALMASS) {
+      std::vector<double> inv(n);
+      for (int64_t i = 0; i < n; ++i) inv[i] = 1.0 / h[i];
+      if ((rc = h2d(f == LULESH_F_VOLO ? d->dd.inv_volo : d->dd.inv_nodalMass, inv.data(), n, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      return LULESH_OK;
+    }
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+  }
+  const int64_t* in = (const int64_t*)host;
+  if (f == LULESH_F_ELEMBC) {
+    if ((rc = h2d(d->dd.elemBC, (const unsigned int*)host, n, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+  }
+  if (int* nb = neighbour_ptr(d, f)) {
+    std::vector<int> t(n);
+    for (int64_t i = 0; i < n; ++i) t[i] = (int)in[i];
+    if ((rc = h2d(nb, t.data(), n, s))) return rc;
+    CK(cudaStreamSynchronize(s));
+    return LULESH_OK;
+  }
+  switch (f) {
+    case LULESH_F_NODELIST: {
+      std::vector<int> t(8 * E);
+      for (int64_t i = 0; i < 8 * E; ++i)
+        if (in[i] < 0 || in[i] >= N) return LULESH_ERR_ARGUMENT;
+      for (int64_t e = 0; e < E; ++e)
+        for (int c = 0; c < 8; ++c) t[c * E + e] = (int)in[8 * e + c];
+      if ((rc = h2d(d->dd.nodelist, t.data(), 8 * E, s))) return rc;
+      CK(cudaStreamSynchronize(s));
+      return LULESH_OK;
+    }
+    case LULESH_F_SYMMX: case LULESH_F_SYMMY: case LULESH_F_SYMMZ: {
+      std::vector<int>& dst = f == LULESH_F_SYMMX ? d->symmX : f == LULESH_F_SYMMY ? d->symmY : d->symmZ;
+      for (int64_t i = 0; i < n; ++i) dst[i] = (int)in[i];
+      return upload_node_bc(d);
+    }
+    default:
+      return LULESH_ERR_ARGUMENT;  // connectivity lists and regions are fixed at creation
+  }
+}
+
+int lulesh_verify(lulesh_domain* d, double out[4]) {
+  if (!d || !out) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  const int64_t nx = d->params.nx;
+  std::vector<double> e(nx * nx);
+  int rc;
+  if ((rc = d2h(e.data(), d->dd.e, nx * nx, d->stream))) return rc;
+  CK(cudaStreamSynchronize(d->stream));
+  // src/utils.jl:139-153
+  double maxAbs = 0.0, maxRel = 0.0, total = 0.0;
+  for (int64_t j = 1; j <= nx; ++j)
+    for (int64_t k = j + 1; k <= nx; ++k) {
+      const double a = e[(j - 1) * nx + k - 1], b = e[(k - 1) * nx + j - 1];
+      const double ad = std::fabs(a - b);
+      total += ad;
+      if (maxAbs < ad) maxAbs = ad;
+      const double rd = ad / b;
+      if (maxRel < rd) maxRel = rd;
+    }
+  out[0] = e[0];
+  out[1] = maxAbs;
+  out[2] = total;
+  out[3] = maxRel;
+  return LULESH_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// Device-side element and node arithmetic of the LagrangeLeapFrog step.
+//
+// Every function restates a reference expression in a form with fewer FP64
+// instructions (GB300 issues about two FP64 instructions per clock per SM,
+// so the FP64 instruction count, not HBM, bounds this step). The
+// reformulations are exact in real arithmetic and differ from the
+// reference's left-to-right evaluation only by rounding:
+//  * the shape-function Jacobian columns (src/domain.jl:1964-1974) and the
+//    monotonic-Q gradients (src/domain.jl:2244-2254) are the first-order
+//    Walsh coefficients of the 8 corner values, taken through the four body
+//    diagonals; power-of-two scale factors (0.125, 0.25, 8) are dropped where
+//    they cancel or only scale a sign test, which is exact;
+//  * the hourglass modes x8n*gamma (src/domain.jl:1510-1525) are the
+//    second/third-order Walsh coefficients, found by a 3-stage butterfly;
+//  * a face's area vector (sumElemFaceNormal, src/domain.jl:971-989) is
+//    -(d1 x d2)/8 for the face's two diagonals d1, d2;
+//  * voluDer (src/domain.jl:1178-1211) only ever sums the 12 hex edges, so
+//    the 36 edge sums are formed once per element;
+//  * the velocity-gradient trace (src/domain.jl:2023-2081, 2156-2158) is
+//    trace(C^T W(v)) / det, with C the cofactors of the Jacobian and W(v) the
+//    Walsh coefficients of the velocities.
+// Products are contracted into FMAs.
+#pragma once
+
+#include <math.h>
+
+#include "lulesh_internal.h"
+
+namespace lulesh {
+
+#define LDG(p) __ldg(p)
+
+// gamma[n][m] of calcFBHourglassForceForElems, src/domain.jl:1490-1499.
+__device__ __forceinline__ double gamma_nm(int n, int m) {
+  // column m is the Walsh function eta*zeta, xi*zeta, xi*eta, xi*eta*zeta
+  // over the corner signs xi = (-,+,+,-,-,+,+,-), eta = (-,-,+,+,-,-,+,+),
+  // zeta = (-,-,-,-,+,+,+,+).
+  const int xs = ((n == 1) | (n == 2) | (n == 5) | (n == 6)) ? 1 : -1;
+  const int es = ((n == 2) | (n == 3) | (n == 6) | (n == 7)) ? 1 : -1;
+  const int zs = (n >= 4) ? 1 : -1;
+  const int v = (m == 0) ? es * zs : (m == 1) ? xs * zs : (m == 2) ? xs * es : xs * es * zs;
+  return (double)v;
+}
+
+// First-order Walsh coefficients (xi, eta, zeta) of 8 corner values through
+// the four body diagonals: 11 FP64 adds.
+__device__ __forceinline__ void walsh1(const double v[8], double w[3]) {
+  const double a = v[6] - v[0], b = v[5] - v[3], c = v[7] - v[1], d = v[4] - v[2];
+  const double apb = a + b, cpd = c + d;
+  w[0] = apb - cpd;
+  w[1] = (a - b) + (c - d);
+  w[2] = apb + cpd;
+}
+
+// First-order (w1: xi, eta, zeta) and higher-order (w2: eta*zeta, xi*zeta,
+// xi*eta, xi*eta*zeta = the four hourglass modes) Walsh coefficients: 23 adds.
+__device__ __forceinline__ void walsh7(const double v[8], double w1[3], double w2[4]) {
+  const double sa = v[0] + v[1], da = v[1] - v[0];
+  const double sb = v[3] + v[2], db = v[2] - v[3];
+  const double sc = v[4] + v[5], dc = v[5] - v[4];
+  const double sd = v[7] + v[6], dd = v[6] - v[7];
+  const double ss1 = sa + sb, sd1 = sb - sa, ds1 = da + db, dd1 = db - da;
+  const double ss2 = sc + sd, sd2 = sd - sc, ds2 = dc + dd, dd2 = dd - dc;
+  w1[0] = ds1 + ds2;
+  w1[1] = sd1 + sd2;
+  w1[2] = ss2 - ss1;
+  w2[0] = sd2 - sd1;
+  w2[1] = ds2 - ds1;
+  w2[2] = dd1 + dd2;
+  w2[3] = dd2 - dd1;
+}
+
+__device__ __forceinline__ void cross(double ax, double ay, double az, double bx, double by,
+                                      double bz, double& cx, double& cy, double& cz) {
+  cx = fma(ay, bz, -az * by);
+  cy = fma(az, bx, -ax * bz);
+  cz = fma(ax, by, -ay * bx);
+}
+
+// triple_product of calcElemVolume, src/utils.jl:40-43.
+__device__ __forceinline__ double triple(double x1, double y1, double z1, double x2, double y2,
+                                        double z2, double x3, double y3, double z3) {
+  const double t1 = fma(y2, z3, -z2 * y3);
+  const double t2 = fma(z1, y3, -y1 * z3);
+  const double t3 = fma(y1, z2, -z1 * y2);
+  return fma(x1, t1, fma(x2, t2, x3 * t3));
+}
+
+// Integer-pipe helpers for exact tests on FP64 values (keeps DSETP off the
+// scarce FP64 pipe). Valid for non-NaN inputs.
+__device__ __forceinline__ bool le_zero(double a) {  // a <= 0.0
+  return __double_as_longlong(a) <= 0;  // +0 -> 0, -0 and negatives -> sign bit
+}
+__device__ __forceinline__ bool gt_zero(double a) {  // a > 0.0
+  return __double_as_longlong(a) > 0;
+}
+__device__ __forceinline__ bool abs_lt(double a, double c) {  // |a| < c for c >= 0
+  return (unsigned long long)(__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) <
+         (unsigned long long)__double_as_longlong(c);
+}
+
+// timeIncrement!, src/domain.jl:920-961, shared by the host API and the
+// device run loop.
+__host__ __device__ inline void time_increment(double& time, double& deltatime, long long& cycle,
+                                               double dtcourant, double dthydro,
+                                               const Params& prm) {
+  double targetdt = prm.stoptime - time;
+  if (prm.dtfixed <= 0.0 && cycle != 0) {
+    const double olddt = deltatime;
+    double gnewdt = (double)INFINITY;  // typemax(Float64)
+    if (dtcourant < gnewdt) gnewdt = dtcourant / 2.0;
+    if (dthydro < gnewdt) gnewdt = dthydro * 2.0 / 3.0;
+    double newdt = gnewdt;
+    const double ratio = newdt / olddt;
+    if (ratio >= 1.0) {
+      if (ratio < prm.deltatimemultlb) newdt = olddt;
+      else if (ratio > prm.deltatimemultub) newdt = olddt * prm.deltatimemultub;
+    }
+    // Julia min: NaN-propagating
+    if (newdt != newdt) {
+    } else if (prm.dtmax != prm.dtmax) {
+      newdt = prm.dtmax;
+    } else if (prm.dtmax < newdt) {
+      newdt = prm.dtmax;
+    }
+    deltatime = newdt;
+  }
+  if (deltatime < targetdt && targetdt < 4.0 * deltatime / 3.0) targetdt = 2.0 * deltatime / 3.0;
+  if (targetdt < deltatime) deltatime = targetdt;
+  time = time + deltatime;
+  cycle += 1;
+}
+
+}  // namespace lulesh

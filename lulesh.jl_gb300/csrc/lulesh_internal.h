@@ -1,0 +1,81 @@
+// Internal structures of the GB300 LagrangeLeapFrog library.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lulesh {
+
+// Boundary-condition masks, src/bc.jl:3-30.
+enum : uint32_t {
+  XI_M = 0x00007, XI_M_SYMM = 0x00001, XI_M_FREE = 0x00002, XI_M_COMM = 0x00004,
+  XI_P = 0x00038, XI_P_SYMM = 0x00008, XI_P_FREE = 0x00010, XI_P_COMM = 0x00020,
+  ETA_M = 0x001c0, ETA_M_SYMM = 0x00040, ETA_M_FREE = 0x00080, ETA_M_COMM = 0x00100,
+  ETA_P = 0x00e00, ETA_P_SYMM = 0x00200, ETA_P_FREE = 0x00400, ETA_P_COMM = 0x00800,
+  ZETA_M = 0x07000, ZETA_M_SYMM = 0x01000, ZETA_M_FREE = 0x02000, ZETA_M_COMM = 0x04000,
+  ZETA_P = 0x38000, ZETA_P_SYMM = 0x08000, ZETA_P_FREE = 0x10000, ZETA_P_COMM = 0x20000,
+};
+
+// Status bits OR-ed by the kernels into DevState::status; the host maps the
+// first set bit (reference order) to a lulesh_status / lulesh_site.
+enum : uint32_t {
+  ST_EARLY = 1u << 0,       // detJ <= 0, src/domain.jl:1104
+  ST_HOURGLASS = 1u << 1,   // v <= 0, src/domain.jl:1727
+  ST_KINEMATICS = 1u << 2,  // vnew <= 0, src/domain.jl:2118
+  ST_BAD_BC = 1u << 3,      // invalid elemBC, src/domain.jl:2343
+  ST_QSTOP = 1u << 4,       // q > qstop, src/domain.jl:2567-2580
+  ST_MATERIAL = 1u << 5,    // clamped v <= 0, src/domain.jl:2905
+  ST_UPDATE = 1u << 6,      // new v <= 0, src/domain.jl:2926
+};
+
+// Per-problem parameters passed by value to every kernel.
+struct Params {
+  double u_cut, hgcoef, qstop, monoq_max_slope, monoq_limiter_mult, e_cut, p_cut, q_cut, v_cut;
+  double qlc_monoq, qqc_monoq, qqc, eosvmax, eosvmin, pmin, emin, dvovmax, refdens;
+  double dtfixed, deltatimemultlb, deltatimemultub, stoptime, dtmax;
+};
+
+// Device-resident step state. acc_* are running minima (bit patterns of
+// non-negative doubles, so an unsigned min is the FP min) filled by the
+// material kernel and folded into dtcourant/dthydro by timeIncrement.
+struct DevState {
+  double time, deltatime, dtcourant, dthydro;
+  long long cycle;
+  unsigned long long acc_courant, acc_hydro;
+  unsigned int status;
+  int done;             // device run loop: 1 once stoptime/num_iters/error is reached
+  long long iters_left;  // device run loop: cycles still allowed
+  long long first;       // device run loop: 1 before the first cycle of a run call
+};
+
+constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
+
+// Pointers of one problem's device fields. Element arrays have E entries,
+// node arrays N; corner arrays 8E in corner-major order (c*E + e).
+struct DevDomain {
+  int E, N, nx;
+  int mode;
+  // nodes
+  double *x, *y, *z, *xd, *yd, *zd;
+  double *nodalMass, *inv_nodalMass;
+  double *xdd, *ydd, *zdd, *fx, *fy, *fz;     // kept only with keep_aux
+  unsigned char* nodeBC;                      // bit0 symmX, bit1 symmY, bit2 symmZ
+  int *nodeElemStart;                         // N+1
+  int *cornerList;                            // 8E, values c*E + e
+  // elements
+  int* nodelist;                              // [8][E]
+  double *e, *p, *q, *v, *volo, *inv_volo, *elemMass, *ss;
+  double *ql, *qq, *vnew, *delv, *arealg, *vdov;
+  double *delv_xi, *delv_eta, *delv_zeta, *delx_xi, *delx_eta, *delx_zeta;
+  double *dxx, *dyy, *dzz;                    // kept only with keep_aux
+  unsigned int* elemBC;
+  int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;
+  // region batching (cost model only)
+  int* regElemlist0;                          // E, 0-based element ids grouped by region
+  int* regOfSlot;                             // E, region rep count per slot
+  // corner forces [8][E]
+  double *fcx, *fcy, *fcz;
+  DevState* st;
+};
+
+}  // namespace lulesh

@@ -1,0 +1,662 @@
+// The LagrangeLeapFrog step as four sm_103a kernels (one thread per element
+// or node, FP64 throughout):
+//   k_force      calcVolumeForceForElems: stress integration + FB hourglass,
+//                one 8-corner force triple per element corner
+//                (src/domain.jl:963-1762)
+//   k_node       deterministic corner-force gather in nodeElemCornerList
+//                order + acceleration, symmetry BCs, velocity and position
+//                (src/domain.jl:1112-1127, 1676-1693, 1781-1838)
+//   k_kinematics calcKinematicsForElems + calcLagrangeElements +
+//                calcMonotonicQGradientsForElems (src/domain.jl:2099-2320)
+//   k_material   calcMonotonicQRegionForElems + qstop check +
+//                applyMaterialPropertiesForElems/evalEOSForElems +
+//                updateVolumesForElems + Courant/hydro dt minima
+//                (src/domain.jl:2322-3064)
+// plus k_time_increment (timeIncrement!, src/domain.jl:920-961) for the
+// device-resident run loop.
+#include "lulesh_device.cuh"
+#include "lulesh_kernels.h"
+
+namespace lulesh {
+
+// Each kernel stops at once when an earlier kernel of the step (or of the
+// device run loop) recorded an error or finished the run, as the reference
+// stops at its first raised error.
+__device__ __forceinline__ bool step_off(const DevState* st) {
+  return (*(volatile const unsigned int*)&st->status) != 0u || (*(volatile const int*)&st->done) != 0;
+}
+
+// ---------------------------------------------------------------------------
+// k_force
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) {
+  const int E = d.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  if (step_off(d.st)) return;
+
+  int nd[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) nd[c] = LDG(&d.nodelist[c * E + e]);
+  double x[8], y[8], z[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    x[c] = LDG(&d.x[nd[c]]);
+    y[c] = LDG(&d.y[nd[c]]);
+    z[c] = LDG(&d.z[nd[c]]);
+  }
+
+  // Walsh coefficients: W1 = Jacobian columns (xi, eta, zeta), HM = modes.
+  double wx[3], wy[3], wz[3], hmx[4], hmy[4], hmz[4];
+  walsh7(x, wx, hmx);
+  walsh7(y, wy, hmy);
+  walsh7(z, wz, hmz);
+
+  // integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
+  // sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
+  {
+    const double cxet = fma(wz[0], wy[2], -(wy[0] * wz[2]));
+    const double cyet = fma(wx[0], wz[2], -(wz[0] * wx[2]));
+    const double czet = fma(wy[0], wx[2], -(wx[0] * wy[2]));
+    const double det = fma(wx[1], cxet, fma(wy[1], cyet, wz[1] * czet));
+    if (le_zero(det)) atomicOr(&d.st->status, ST_EARLY);
+  }
+
+  // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
+  // face-diagonal cross products; true B = -Bc/8.
+  double Bx[8], By[8], Bz[8];
+  {
+    // face diagonals (p2 - p0, p3 - p1) in the reference's argument order
+    constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
+                              {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
+    double nx[6], ny[6], nz[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const double d1x = x[fd[f][0]] - x[fd[f][1]], d1y = y[fd[f][0]] - y[fd[f][1]],
+                   d1z = z[fd[f][0]] - z[fd[f][1]];
+      const double d2x = x[fd[f][2]] - x[fd[f][3]], d2y = y[fd[f][2]] - y[fd[f][3]],
+                   d2z = z[fd[f][2]] - z[fd[f][3]];
+      cross(d1x, d1y, d1z, d2x, d2y, d2z, nx[f], ny[f], nz[f]);
+    }
+    // node -> its three faces (faces numbered 0..5 = reference faces 1..6)
+    Bx[0] = (nx[0] + nx[1]) + nx[4]; By[0] = (ny[0] + ny[1]) + ny[4]; Bz[0] = (nz[0] + nz[1]) + nz[4];
+    if (!(MODE & 1)) {
+      // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice, no areaZ
+      By[0] = By[0] + ny[4];
+      Bz[0] = nz[0] + nz[1];
+    }
+    Bx[1] = (nx[0] + nx[1]) + nx[2]; By[1] = (ny[0] + ny[1]) + ny[2]; Bz[1] = (nz[0] + nz[1]) + nz[2];
+    Bx[2] = (nx[0] + nx[2]) + nx[3]; By[2] = (ny[0] + ny[2]) + ny[3]; Bz[2] = (nz[0] + nz[2]) + nz[3];
+    Bx[3] = (nx[0] + nx[3]) + nx[4]; By[3] = (ny[0] + ny[3]) + ny[4]; Bz[3] = (nz[0] + nz[3]) + nz[4];
+    Bx[4] = (nx[1] + nx[4]) + nx[5]; By[4] = (ny[1] + ny[4]) + ny[5]; Bz[4] = (nz[1] + nz[4]) + nz[5];
+    Bx[5] = (nx[1] + nx[2]) + nx[5]; By[5] = (ny[1] + ny[2]) + ny[5]; Bz[5] = (nz[1] + nz[2]) + nz[5];
+    Bx[6] = (nx[2] + nx[3]) + nx[5]; By[6] = (ny[2] + ny[3]) + ny[5]; Bz[6] = (nz[2] + nz[3]) + nz[5];
+    Bx[7] = (nx[3] + nx[4]) + nx[5]; By[7] = (ny[3] + ny[4]) + ny[5]; Bz[7] = (nz[3] + nz[4]) + nz[5];
+  }
+
+  // calcElemVolumeDerivative (src/domain.jl:1213-1256), times 12, from the
+  // 12 edge sums. The n-th call differentiates w.r.t. node owner[n]; the
+  // reference stores it in slot n (slots 1 and 3 exchanged).
+  double dvx[8], dvy[8], dvz[8];
+  {
+    // edges: 01 03 04 12 15 23 26 37 45 47 56 67
+    double ex[12], ey[12], ez[12];
+    constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
+    constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
+#pragma unroll
+    for (int k = 0; k < 12; ++k) {
+      ex[k] = x[ea[k]] + x[eb[k]];
+      ey[k] = y[ea[k]] + y[eb[k]];
+      ez[k] = z[ea[k]] + z[eb[k]];
+    }
+    constexpr int perm[8][6] = {{1, 2, 3, 4, 5, 7}, {0, 1, 2, 7, 4, 6}, {3, 0, 1, 6, 7, 5},
+                                {2, 3, 0, 5, 6, 4}, {7, 6, 5, 0, 3, 1}, {4, 7, 6, 1, 0, 2},
+                                {5, 4, 7, 2, 1, 3}, {6, 5, 4, 3, 2, 0}};
+    constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int* q = perm[n];
+      // edge index of an unordered node pair
+      auto eidx = [](int a, int b) -> int {
+        const int lo = a < b ? a : b, hi = a < b ? b : a;
+        return lo == 0 ? (hi == 1 ? 0 : hi == 3 ? 1 : 2)
+             : lo == 1 ? (hi == 2 ? 3 : 4)
+             : lo == 2 ? (hi == 3 ? 5 : 6)
+             : lo == 3 ? 7
+             : lo == 4 ? (hi == 5 ? 8 : 9)
+             : lo == 5 ? 10 : 11;
+      };
+      const int p12 = eidx(q[1], q[2]), p01 = eidx(q[0], q[1]), p04 = eidx(q[0], q[4]);
+      const int p34 = eidx(q[3], q[4]), p25 = eidx(q[2], q[5]), p35 = eidx(q[3], q[5]);
+      const double vx = fma(ey[p12], ez[p01], fma(-ey[p01], ez[p12], fma(ey[p04], ez[p34],
+                        fma(-ey[p34], ez[p04], fma(-ey[p25], ez[p35], ey[p35] * ez[p25])))));
+      const double vy = fma(-ex[p12], ez[p01], fma(ex[p01], ez[p12], fma(-ex[p04], ez[p34],
+                        fma(ex[p34], ez[p04], fma(ex[p25], ez[p35], -(ex[p35] * ez[p25]))))));
+      const double vz = fma(-ey[p12], ex[p01], fma(ey[p01], ex[p12], fma(-ey[p04], ex[p34],
+                        fma(ey[p34], ex[p04], fma(ey[p25], ex[p35], -(ey[p35] * ex[p25]))))));
+      const int slot = (MODE & 2) ? owner[n] : n;
+      dvx[slot] = vx; dvy[slot] = vy; dvz[slot] = vz;
+    }
+  }
+
+  // calcHourglassControlForElems (src/domain.jl:1696-1736): determ = volo*v.
+  const double v = LDG(&d.v[e]);
+  const double determ = LDG(&d.volo[e]) * v;
+  if (le_zero(v)) atomicOr(&d.st->status, ST_HOURGLASS);
+
+  // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
+  const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
+
+  double fx[8], fy[8], fz[8];
+  if (prm.hgcoef > 0.0) {
+    // hourgam (src/domain.jl:1527-1549) with volinv/12 folded into the modes
+    const double vi12 = 1.0 / (12.0 * determ);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) { hmx[m] *= vi12; hmy[m] *= vi12; hmz[m] *= vi12; }
+    double hg[8][4];
+#pragma unroll
+    for (int n = 0; n < 8; ++n)
+#pragma unroll
+      for (int m = 0; m < 4; ++m)
+        hg[n][m] = fma(-dvz[n], hmz[m], fma(-dvy[n], hmy[m], fma(-dvx[n], hmx[m], gamma_nm(n, m))));
+
+    // coefficient = -hgcoef*0.01*ss*mass/cbrt(determ) (src/domain.jl:1605)
+    const double coef = ((-prm.hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * rcbrt(determ);
+
+    // calcElemFBHourglassForce (src/domain.jl:1258-1460), one velocity
+    // component at a time to bound register use.
+    const double* vel[3] = {d.xd, d.yd, d.zd};
+    const double* Bc[3] = {Bx, By, Bz};
+    double* fo[3] = {fx, fy, fz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double vv[8];
+#pragma unroll
+      for (int c = 0; c < 8; ++c) vv[c] = LDG(&vel[k][nd[c]]);
+      double h[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        double s = hg[0][m] * vv[0];
+#pragma unroll
+        for (int n = 1; n < 8; ++n) s = fma(hg[n][m], vv[n], s);
+        h[m] = coef * s;
+      }
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        const double hgf = fma(hg[n][0], h[0], fma(hg[n][1], h[1], fma(hg[n][2], h[2], hg[n][3] * h[3])));
+        fo[k][n] = fma(s8, Bc[k][n], hgf);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) { fx[n] = s8 * Bx[n]; fy[n] = s8 * By[n]; fz[n] = s8 * Bz[n]; }
+  }
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    d.fcx[c * E + e] = fx[c];
+    d.fcy[c * E + e] = fy[c];
+    d.fcz[c * E + e] = fz[c];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_node
+// ---------------------------------------------------------------------------
+template <bool AUX>
+__global__ void __launch_bounds__(kNodeBlock) k_node(DevDomain d, Params prm) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= d.N) return;
+  if (step_off(d.st)) return;
+  const double dt = d.st->deltatime;
+  const int s = LDG(&d.nodeElemStart[i]), t = LDG(&d.nodeElemStart[i + 1]);
+  double fx = 0.0, fy = 0.0, fz = 0.0;
+  if (s < t) {
+    const int c0 = LDG(&d.cornerList[s]);
+    fx = LDG(&d.fcx[c0]); fy = LDG(&d.fcy[c0]); fz = LDG(&d.fcz[c0]);
+    for (int j = s + 1; j < t; ++j) {
+      const int c = LDG(&d.cornerList[j]);
+      fx += LDG(&d.fcx[c]); fy += LDG(&d.fcy[c]); fz += LDG(&d.fcz[c]);
+    }
+  }
+  const double im = LDG(&d.inv_nodalMass[i]);
+  double ax = fx * im, ay = fy * im, az = fz * im;
+  const unsigned bc = d.nodeBC[i];
+  if (bc & 1u) ax = 0.0;
+  if (bc & 2u) ay = 0.0;
+  if (bc & 4u) az = 0.0;
+  double xd = fma(ax, dt, d.xd[i]);
+  double yd = fma(ay, dt, d.yd[i]);
+  double zd = fma(az, dt, d.zd[i]);
+  if (abs_lt(xd, prm.u_cut)) xd = 0.0;
+  if (abs_lt(yd, prm.u_cut)) yd = 0.0;
+  if (abs_lt(zd, prm.u_cut)) zd = 0.0;
+  d.xd[i] = xd; d.yd[i] = yd; d.zd[i] = zd;
+  d.x[i] = fma(xd, dt, d.x[i]);
+  d.y[i] = fma(yd, dt, d.y[i]);
+  d.z[i] = fma(zd, dt, d.z[i]);
+  if (AUX) {
+    d.fx[i] = fx; d.fy[i] = fy; d.fz[i] = fz;
+    d.xdd[i] = ax; d.ydd[i] = ay; d.zdd[i] = az;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_kinematics
+// ---------------------------------------------------------------------------
+template <bool AUX>
+__global__ void __launch_bounds__(kKinBlock) k_kinematics(DevDomain d, Params prm) {
+  const int E = d.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  if (step_off(d.st)) return;
+  const double dt = d.st->deltatime;
+
+  int nd[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) nd[c] = LDG(&d.nodelist[c * E + e]);
+  double x[8], y[8], z[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    x[c] = LDG(&d.x[nd[c]]);
+    y[c] = LDG(&d.y[nd[c]]);
+    z[c] = LDG(&d.z[nd[c]]);
+  }
+
+  // calcElemVolume (src/utils.jl:36-116); its 12 differences are the face
+  // diagonals that calcElemCharacteristicLength needs too.
+  double volume, charLength = 0.0;
+  {
+    double d61[3], d70[3], d63[3], d20[3], d50[3], d64[3], d31[3], d72[3], d43[3], d57[3], d14[3], d25[3];
+    const double* P[3] = {x, y, z};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double* p = P[k];
+      d61[k] = p[6] - p[1]; d70[k] = p[7] - p[0]; d63[k] = p[6] - p[3]; d20[k] = p[2] - p[0];
+      d50[k] = p[5] - p[0]; d64[k] = p[6] - p[4]; d31[k] = p[3] - p[1]; d72[k] = p[7] - p[2];
+      d43[k] = p[4] - p[3]; d57[k] = p[5] - p[7]; d14[k] = p[1] - p[4]; d25[k] = p[2] - p[5];
+    }
+    const double v12 =
+        triple(d31[0] + d72[0], d63[0], d20[0], d31[1] + d72[1], d63[1], d20[1], d31[2] + d72[2], d63[2], d20[2]) +
+        triple(d43[0] + d57[0], d64[0], d70[0], d43[1] + d57[1], d64[1], d70[1], d43[2] + d57[2], d64[2], d70[2]) +
+        triple(d14[0] + d25[0], d61[0], d50[0], d14[1] + d25[1], d61[1], d50[1], d14[2] + d25[2], d61[2], d50[2]);
+    volume = v12 * (1.0 / 12.0);
+    // areaFace (src/domain.jl:1874-1891) for the six faces; f, g from the
+    // face diagonals.
+    auto face = [&](const double* a, const double* b, double sf, double sg) {
+      double f[3], g[3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { f[k] = fma(sf, b[k], a[k]); g[k] = fma(sg, b[k], a[k]); }
+      const double ff = fma(f[0], f[0], fma(f[1], f[1], f[2] * f[2]));
+      const double gg = fma(g[0], g[0], fma(g[1], g[1], g[2] * g[2]));
+      const double fg = fma(f[0], g[0], fma(f[1], g[1], f[2] * g[2]));
+      const double area = fma(ff, gg, -(fg * fg));
+      charLength = fmax(area, charLength);
+    };
+    face(d20, d31, -1.0, 1.0);   // nodes 1,2,3,4
+    face(d64, d57, 1.0, -1.0);   // 5,6,7,8
+    face(d50, d14, 1.0, -1.0);   // 1,2,6,5
+    face(d61, d25, 1.0, -1.0);   // 2,3,7,6
+    face(d72, d63, -1.0, 1.0);   // 3,4,8,7
+    face(d43, d70, -1.0, 1.0);   // 4,1,5,8
+  }
+  const double vnew = volume * LDG(&d.inv_volo[e]);
+  if (le_zero(vnew)) atomicOr(&d.st->status, ST_KINEMATICS);
+  d.vnew[e] = vnew;
+  d.delv[e] = vnew - LDG(&d.v[e]);
+  d.arealg[e] = (4.0 * volume) * rsqrt(charLength);
+
+  // Velocity gradient trace at the half-step position (src/domain.jl:2128-2158)
+  double wx[3], wy[3], wz[3];
+  walsh1(x, wx); walsh1(y, wy); walsh1(z, wz);
+  double vxw[3], vyw[3], vzw[3];
+  {
+    double v8[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v8[c] = LDG(&d.xd[nd[c]]);
+    walsh1(v8, vxw);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v8[c] = LDG(&d.yd[nd[c]]);
+    walsh1(v8, vyw);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) v8[c] = LDG(&d.zd[nd[c]]);
+    walsh1(v8, vzw);
+  }
+  {
+    const double dt2 = -0.5 * dt;
+    double F[3][3];  // F[k][a]: coordinate k, direction a (xi, eta, zeta)
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      F[0][a] = fma(dt2, vxw[a], wx[a]);
+      F[1][a] = fma(dt2, vyw[a], wy[a]);
+      F[2][a] = fma(dt2, vzw[a], wz[a]);
+    }
+    // cofactors (src/domain.jl:1976-1987)
+    const double Cxxi = fma(F[1][1], F[2][2], -(F[2][1] * F[1][2]));
+    const double Cxet = fma(F[2][0], F[1][2], -(F[1][0] * F[2][2]));
+    const double Cxze = fma(F[1][0], F[2][1], -(F[2][0] * F[1][1]));
+    const double Cyxi = fma(F[2][1], F[0][2], -(F[0][1] * F[2][2]));
+    const double Cyet = fma(F[0][0], F[2][2], -(F[2][0] * F[0][2]));
+    const double Cyze = fma(F[2][0], F[0][1], -(F[0][0] * F[2][1]));
+    const double Czxi = fma(F[0][1], F[1][2], -(F[1][1] * F[0][2]));
+    const double Czet = fma(F[1][0], F[0][2], -(F[0][0] * F[1][2]));
+    const double Czze = fma(F[0][0], F[1][1], -(F[1][0] * F[0][1]));
+    const double det = fma(F[0][1], Cxet, fma(F[1][1], Cyet, F[2][1] * Czet));
+    const double d1 = fma(Cxxi, vxw[0], fma(Cxet, vxw[1], Cxze * vxw[2]));
+    const double d2 = fma(Cyxi, vyw[0], fma(Cyet, vyw[1], Cyze * vyw[2]));
+    const double d3 = fma(Czxi, vzw[0], fma(Czet, vzw[1], Czze * vzw[2]));
+    const double inv = 1.0 / det;
+    const double vdov = ((d1 + d2) + d3) * inv;
+    d.vdov[e] = vdov;
+    if (AUX) {
+      const double third = vdov / 3.0;
+      d.dxx[e] = d1 * inv - third;
+      d.dyy[e] = d2 * inv - third;
+      d.dzz[e] = d3 * inv - third;
+    }
+  }
+
+  // calcMonotonicQGradientsForElems (src/domain.jl:2175-2320). With the
+  // reference's dxi = W_xi/4 etc.: delx = 16*vol/sqrt(|A|^2 + 256*ptiny) and
+  // delv = norm/64 * (A . W(v)) for the cross product A of two Walsh vectors.
+  {
+    const double ptiny = 1.e-36;
+    const double vol = LDG(&d.volo[e]) * vnew;
+    const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
+    const double vol16 = 16.0 * vol;
+    double ax, ay, az;
+    // zeta: xi x eta
+    cross(wx[0], wy[0], wz[0], wx[1], wy[1], wz[1], ax, ay, az);
+    d.delx_zeta[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delv_zeta[e] = norm64 * fma(ax, vxw[2], fma(ay, vyw[2], az * vzw[2]));
+    // xi: eta x zeta
+    cross(wx[1], wy[1], wz[1], wx[2], wy[2], wz[2], ax, ay, az);
+    d.delx_xi[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delv_xi[e] = norm64 * fma(ax, vxw[0], fma(ay, vyw[0], az * vzw[0]));
+    // eta: zeta x xi
+    cross(wx[2], wy[2], wz[2], wx[0], wy[0], wz[0], ax, ay, az);
+    d.delx_eta[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delv_eta[e] = norm64 * fma(ax, vxw[1], fma(ay, vyw[1], az * vzw[1]));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// k_material
+// ---------------------------------------------------------------------------
+
+// One limiter direction, src/domain.jl:2330-2376.
+__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm) {
+  const double norm = 1.0 / (self + 1.e-36);
+  dm *= norm;
+  dp *= norm;
+  double phi = 0.5 * (dm + dp);
+  dm *= prm.monoq_limiter_mult;
+  dp *= prm.monoq_limiter_mult;
+  if (dm < phi) phi = dm;
+  if (dp < phi) phi = dp;
+  if (phi < 0.0) phi = 0.0;
+  if (phi > prm.monoq_max_slope) phi = prm.monoq_max_slope;
+  return phi;
+}
+
+// Neighbour value for one face of the limiter (the four BC cases).
+__device__ __forceinline__ double monoq_neighbour(const double* dv, unsigned mask, unsigned bits,
+                                                  unsigned symm, unsigned freeb, unsigned comm,
+                                                  int idx, int self, int E, bool& bad) {
+  const unsigned c = mask & bits;
+  if (c == 0u || c == comm) {
+    if (idx < 0 || idx >= E) { bad = true; return 0.0; }
+    return LDG(&dv[idx]);
+  }
+  if (c == symm) return LDG(&dv[self]);
+  if (c == freeb) return 0.0;
+  bad = true;
+  return 0.0;
+}
+
+// TINY-guarded sound-speed square root, src/domain.jl:2655-2659.
+__device__ __forceinline__ double ssc_sqrt(double ssc) {
+  return (ssc <= 0.111111e-36) ? 0.333333e-18 : sqrt(ssc);
+}
+
+__device__ __forceinline__ void block_min2(unsigned long long a, unsigned long long b,
+                                           unsigned long long* ga, unsigned long long* gb) {
+  __shared__ unsigned long long sa[32], sb[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long ta = __shfl_xor_sync(0xffffffffu, a, o);
+    const unsigned long long tb = __shfl_xor_sync(0xffffffffu, b, o);
+    a = ta < a ? ta : a;
+    b = tb < b ? tb : b;
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { sa[w] = a; sb[w] = b; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = blockDim.x >> 5;
+    a = l < nw ? sa[l] : kInfBits;
+    b = l < nw ? sb[l] : kInfBits;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ta = __shfl_xor_sync(0xffffffffu, a, o);
+      const unsigned long long tb = __shfl_xor_sync(0xffffffffu, b, o);
+      a = ta < a ? ta : a;
+      b = tb < b ? tb : b;
+    }
+    if (l == 0) {
+      if (a != kInfBits) atomicMin(ga, a);
+      if (b != kInfBits) atomicMin(gb, b);
+    }
+  }
+}
+
+template <int MODE, bool AUX>
+__global__ void __launch_bounds__(kMatBlock) k_material(DevDomain d, Params prm) {
+  const int E = d.E;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  // every thread of the block takes part in the dt reduction
+  unsigned long long courant = kInfBits, hydro = kInfBits;
+  const bool live = (i < E) && !step_off(d.st);
+  if (live) {
+    unsigned int err = 0u;
+    // ---- calcMonotonicQRegionForElems, src/domain.jl:2322-2513 ----
+    const unsigned mask = LDG(&d.elemBC[i]);
+    const double dvxi = LDG(&d.delv_xi[i]), dveta = LDG(&d.delv_eta[i]), dvzeta = LDG(&d.delv_zeta[i]);
+    bool bad = false;
+    // xi-plus: the reference indexes delv_xi[lxip[i]] without +1 (:2349)
+    const int ixp = (MODE & 4) ? LDG(&d.lxip[i]) : LDG(&d.lxip[i]) - 1;
+    double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
+    double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
+    const double phixi = monoq_phi(dvxi, dm, dp, prm);
+    dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
+    dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);
+    const double phieta = monoq_phi(dveta, dm, dp, prm);
+    dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, E, bad);
+    dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, E, bad);
+    const double phizeta = monoq_phi(dvzeta, dm, dp, prm);
+    if (bad) err |= ST_BAD_BC;
+
+    const double vdov = LDG(&d.vdov[i]);
+    const double vnew = LDG(&d.vnew[i]);
+    const double volo = LDG(&d.volo[i]);
+    double qlin, qquad;
+    if (gt_zero(vdov)) {
+      qlin = 0.0;
+      qquad = 0.0;
+    } else {
+      double dxxi = dvxi * LDG(&d.delx_xi[i]);
+      double dxeta = dveta * LDG(&d.delx_eta[i]);
+      double dxzeta = dvzeta * LDG(&d.delx_zeta[i]);
+      if (gt_zero(dxxi)) dxxi = 0.0;
+      if (gt_zero(dxeta)) dxeta = 0.0;
+      if (gt_zero(dxzeta)) dxzeta = 0.0;
+      const double rho = LDG(&d.elemMass[i]) / (volo * vnew);
+      qlin = (-prm.qlc_monoq * rho) *
+             fma(dxxi, 1.0 - phixi, fma(dxeta, 1.0 - phieta, dxzeta * (1.0 - phizeta)));
+      qquad = (prm.qqc_monoq * rho) *
+              fma(dxxi * dxxi, fma(-phixi, phixi, 1.0),
+                  fma(dxeta * dxeta, fma(-phieta, phieta, 1.0), (dxzeta * dxzeta) * fma(-phizeta, phizeta, 1.0)));
+    }
+    if (AUX) { d.ql[i] = qlin; d.qq[i] = qquad; }
+
+    // ---- qstop check on the old q, src/domain.jl:2567-2582 ----
+    const double q_old_in = d.q[i];
+    if (q_old_in > prm.qstop) err |= ST_QSTOP;
+
+    // ---- applyMaterialPropertiesForElems, src/domain.jl:2860-2910 ----
+    double vnewc = vnew;
+    if (prm.eosvmin != 0.0 && vnewc < prm.eosvmin) vnewc = prm.eosvmin;
+    if (prm.eosvmax != 0.0 && vnewc > prm.eosvmax) vnewc = prm.eosvmax;
+    {
+      double vc = LDG(&d.v[i]);
+      if (prm.eosvmin != 0.0 && vc < prm.eosvmin) vc = prm.eosvmin;
+      if (prm.eosvmax != 0.0 && vc > prm.eosvmax) vc = prm.eosvmax;
+      if (le_zero(vc)) err |= ST_MATERIAL;
+    }
+
+    // ---- evalEOSForElems + calcEnergyForElems + calcSoundSpeedForElems,
+    //      src/domain.jl:2617-2857, per element ----
+    const double delvc = LDG(&d.delv[i]);
+    const double e_old = d.e[i];
+    double p_old = d.p[i];
+    const double q_old = q_old_in;
+    double compression = 1.0 / vnewc - 1.0;
+    const double vchalf = fma(delvc, -0.5, vnewc);
+    double compHalfStep = 1.0 / vchalf - 1.0;
+    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) compHalfStep = compression;
+    if (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) { p_old = 0.0; compression = 0.0; compHalfStep = 0.0; }
+    const double c1s = 2.0 / 3.0;
+    const double inv_rho0 = 1.0 / prm.refdens;
+    const bool vmax_hit = vnewc >= prm.eosvmax;
+    // calcPressureForElems (src/domain.jl:2585-2614) for one element
+    auto pressure = [&](double enew, double bvc) -> double {
+      double pn = bvc * enew;
+      if (abs_lt(pn, prm.p_cut)) pn = 0.0;
+      if (vmax_hit) pn = 0.0;
+      if (pn < prm.pmin) pn = prm.pmin;
+      return pn;
+    };
+    const double pq_old = p_old + q_old;
+    double e_new = fma(-0.5 * delvc, pq_old, e_old);
+    if (e_new < prm.emin) e_new = prm.emin;
+    const double bvc_half = c1s * (compHalfStep + 1.0);
+    const double pHalfStep = pressure(e_new, bvc_half);
+    const double vhalf = 1.0 / (1.0 + compHalfStep);
+    const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
+    double q_new = 0.0;
+    if (compress) {
+      const double ssc = fma(c1s, e_new, ((vhalf * vhalf) * bvc_half) * pHalfStep) * inv_rho0;
+      q_new = fma(ssc_sqrt(ssc), qlin, qquad);
+    }
+    e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
+    if (abs_lt(e_new, prm.e_cut)) e_new = 0.0;
+    if (e_new < prm.emin) e_new = prm.emin;
+    const double bvc = c1s * (compression + 1.0);
+    double p_new = pressure(e_new, bvc);
+    const double vv_bvc = (vnewc * vnewc) * bvc;
+    double q_tilde = 0.0;
+    if (compress) {
+      const double ssc = fma(c1s, e_new, vv_bvc * p_new) * inv_rho0;
+      q_tilde = fma(ssc_sqrt(ssc), qlin, qquad);
+    }
+    e_new = e_new - ((fma(7.0, pq_old, -8.0 * (pHalfStep + q_new)) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
+    if (abs_lt(e_new, prm.e_cut)) e_new = 0.0;
+    if (e_new < prm.emin) e_new = prm.emin;
+    p_new = pressure(e_new, bvc);
+    // the last q evaluation and the sound speed share one expression
+    const double ss_new = ssc_sqrt(fma(c1s, e_new, vv_bvc * p_new) * inv_rho0);
+    if (compress) {
+      q_new = fma(ss_new, qlin, qquad);
+      if (abs_lt(q_new, prm.q_cut)) q_new = 0.0;
+    }
+    d.p[i] = p_new;
+    d.e[i] = e_new;
+    d.q[i] = q_new;
+    d.ss[i] = ss_new;
+
+    // ---- updateVolumesForElems, src/domain.jl:2912-2930 ----
+    double tmpV = vnew;
+    if (abs_lt(tmpV - 1.0, prm.v_cut)) tmpV = 1.0;
+    d.v[i] = tmpV;
+    if (le_zero(tmpV)) err |= ST_UPDATE;
+
+    // ---- Courant and hydro constraints, src/domain.jl:2964-3054 ----
+    if (vdov != 0.0) {
+      const double arealg = LDG(&d.arealg[i]);
+      double dtf = ss_new * ss_new;
+      if (vdov < 0.0) dtf = fma(((64.0 * prm.qqc) * prm.qqc) * (arealg * arealg), vdov * vdov, dtf);
+      const double dtc = arealg * rsqrt(dtf);
+      const double dth = prm.dvovmax / (fabs(vdov) + 1.e-20);
+      courant = (unsigned long long)__double_as_longlong(dtc);
+      hydro = (unsigned long long)__double_as_longlong(dth);
+    }
+    if (err) atomicOr(&d.st->status, err);
+  }
+  block_min2(courant, hydro, &d.st->acc_courant, &d.st->acc_hydro);
+}
+
+// ---------------------------------------------------------------------------
+// k_time_increment (device run loop)
+// ---------------------------------------------------------------------------
+__global__ void k_time_increment(DevState* st, Params prm, long long num_iters) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (st->done) return;
+  if (st->status) { st->done = 1; return; }
+  // fold the previous step's minima (src/domain.jl:3012-3014, 3050-3052)
+  if (st->acc_courant != kInfBits) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
+  if (st->acc_hydro != kInfBits) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
+  st->acc_courant = kInfBits;
+  st->acc_hydro = kInfBits;
+  // examples/benchmark.jl:82-98: while time < stoptime ... break if cycle >= num_iters
+  if (!(st->time < prm.stoptime) || (!st->first && st->cycle >= num_iters)) { st->done = 1; return; }
+  st->first = 0;
+  double time = st->time, dt = st->deltatime;
+  long long cycle = st->cycle;
+  time_increment(time, dt, cycle, st->dtcourant, st->dthydro, prm);
+  st->time = time;
+  st->deltatime = dt;
+  st->cycle = cycle;
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_force(const DevDomain& d, const Params& prm, cudaStream_t s) {
+  const int grid = (d.E + kForceBlock - 1) / kForceBlock;
+  switch (d.mode & 3) {
+    case 0: k_force<0><<<grid, kForceBlock, 0, s>>>(d, prm); break;
+    case 1: k_force<1><<<grid, kForceBlock, 0, s>>>(d, prm); break;
+    case 2: k_force<2><<<grid, kForceBlock, 0, s>>>(d, prm); break;
+    default: k_force<3><<<grid, kForceBlock, 0, s>>>(d, prm); break;
+  }
+}
+
+void launch_node(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
+  const int grid = (d.N + kNodeBlock - 1) / kNodeBlock;
+  if (aux) k_node<true><<<grid, kNodeBlock, 0, s>>>(d, prm);
+  else k_node<false><<<grid, kNodeBlock, 0, s>>>(d, prm);
+}
+
+void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
+  const int grid = (d.E + kKinBlock - 1) / kKinBlock;
+  if (aux) k_kinematics<true><<<grid, kKinBlock, 0, s>>>(d, prm);
+  else k_kinematics<false><<<grid, kKinBlock, 0, s>>>(d, prm);
+}
+
+void launch_material(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
+  const int grid = (d.E + kMatBlock - 1) / kMatBlock;
+  const bool fix = (d.mode & 4) != 0;
+  if (fix) {
+    if (aux) k_material<4, true><<<grid, kMatBlock, 0, s>>>(d, prm);
+    else k_material<4, false><<<grid, kMatBlock, 0, s>>>(d, prm);
+  } else {
+    if (aux) k_material<0, true><<<grid, kMatBlock, 0, s>>>(d, prm);
+    else k_material<0, false><<<grid, kMatBlock, 0, s>>>(d, prm);
+  }
+}
+
+void launch_time_increment(DevState* st, const Params& prm, long long num_iters, cudaStream_t s) {
+  k_time_increment<<<1, 32, 0, s>>>(st, prm, num_iters);
+}
+
+}  // namespace lulesh

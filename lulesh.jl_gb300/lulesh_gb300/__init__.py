@@ -1,0 +1,328 @@
+"""Python mirror of LULESH.jl's single-rank API over liblulesh_gb300.so.
+
+The reference's public surface (src/LULESH.jl:58-60) is `LuleshProblem`,
+`Domain`, `timeIncrement!`, `lagrangeLeapFrog` and
+`verifyAndWriteFinalOutput`; this module keeps those names and their meaning
+(`timeIncrement!` is spelled `timeIncrement`). The state lives on the GPU;
+`Domain` attributes read or write it through the C ABI declared in
+include/lulesh_gb300.h. Errors the reference raises with `error(...)` raise
+`LuleshError` with the same message.
+
+There is no CPU fallback: importing works without a GPU, but creating a
+Domain needs the compiled library and a CUDA device, and fails loudly
+otherwise.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+__all__ = [
+    "LuleshProblem", "Domain", "timeIncrement", "lagrangeLeapFrog", "run",
+    "verifyAndWriteFinalOutput", "LuleshError", "load_library", "library_path",
+    "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2",
+]
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_PKG = os.path.dirname(_HERE)
+
+MODE_FAITHFUL = 0
+FIX_NORMALS = 1
+FIX_VOLUDER = 2
+FIX_LXIP = 4
+MODE_LULESH2 = 7
+
+# lulesh_field ids (include/lulesh_gb300.h) -> (id, kind)
+_ELEM_F64 = ["e", "p", "q", "ql", "qq", "v", "volo", "delv", "vdov", "arealg", "ss", "elemMass",
+             "vnew", "delv_xi", "delv_eta", "delv_zeta", "delx_xi", "delx_eta", "delx_zeta",
+             "dxx", "dyy", "dzz"]
+_NODE_F64 = ["x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy", "fz", "nodalMass"]
+_I64 = ["nodelist", "lxim", "lxip", "letam", "letap", "lzetam", "lzetap", "symmX", "symmY",
+        "symmZ", "nodeElemCount", "nodeElemStart", "nodeElemCornerList", "matElemlist",
+        "regNumList", "regElemlist", "regCSR", "regReps", "regSorted", "regElemSize"]
+FIELDS = {}
+for _i, _n in enumerate(_ELEM_F64):
+    FIELDS[_n] = (_i, np.float64)
+for _i, _n in enumerate(_NODE_F64):
+    FIELDS[_n] = (32 + _i, np.float64)
+for _i, _n in enumerate(_I64):
+    FIELDS[_n] = (64 + _i, np.int64)
+FIELDS["elemBC"] = (96, np.uint32)
+
+SCALARS = {n: i for i, n in enumerate([
+    "dtfixed", "deltatimemultlb", "deltatimemultub", "stoptime", "dtmax", "dthydro", "dtcourant",
+    "time", "deltatime", "u_cut", "hgcoef", "qstop", "monoq_max_slope", "monoq_limiter_mult",
+    "e_cut", "p_cut", "ss4o3", "q_cut", "v_cut", "qlc_monoq", "qqc_monoq", "qqc", "eosvmax",
+    "eosvmin", "pmin", "emin", "dvovmax", "refdens", "cycle"])}
+
+# Reference messages per (status, site): src/domain.jl error(...) calls.
+_MESSAGES = {
+    (1, 1): "Early Volume Error",
+    (1, 2): "Volume Error: Volume is negative",
+    (1, 3): "Mid Volume Error",
+    (1, 4): "Volume Error: calcKinematicsForElems",
+    (1, 5): "Volume Error :2157",
+    (1, 6): "Volume Error :2887",
+    (1, 7): "Volume Error :2908",
+    (2, 0): "QStopError",
+    (3, 0): "Error",
+}
+
+
+class LuleshError(RuntimeError):
+    """A step error; `.status` and `.site` hold the C ABI codes."""
+
+    def __init__(self, msg, status=0, site=0):
+        super().__init__(msg)
+        self.status = status
+        self.site = site
+
+
+class _Params(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int32), ("nr", ctypes.c_int32), ("balance", ctypes.c_int32),
+                ("cost", ctypes.c_int32), ("mode", ctypes.c_int32), ("region_reps", ctypes.c_int32),
+                ("keep_aux", ctypes.c_int32), ("device", ctypes.c_int32),
+                ("region_seed", ctypes.c_uint64)]
+
+
+class _Scalars(ctypes.Structure):
+    _fields_ = [("time", ctypes.c_double), ("deltatime", ctypes.c_double),
+                ("dtcourant", ctypes.c_double), ("dthydro", ctypes.c_double),
+                ("cycle", ctypes.c_int64), ("status", ctypes.c_int32), ("site", ctypes.c_int32)]
+
+
+_LIB = None
+
+
+def library_path():
+    """Path of the in-tree shared library built by lulesh.jl_gb300/build.py."""
+    return os.environ.get("LULESH_GB300_LIB", os.path.join(_PKG, "lib", "liblulesh_gb300.so"))
+
+
+def load_library():
+    """Load liblulesh_gb300.so and declare its C signatures (no GPU needed)."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = library_path()
+    if not os.path.exists(path):
+        raise RuntimeError(
+            f"liblulesh_gb300.so not found at {path}; build it with "
+            "`python lulesh.jl_gb300/build.py` (the GPU path has no CPU fallback)")
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    i32, i64, dbl = ctypes.c_int32, ctypes.c_int64, ctypes.c_double
+    sig = {
+        "lulesh_default_params": (None, [ctypes.POINTER(_Params), i32]),
+        "lulesh_create": (ctypes.c_int, [ctypes.POINTER(_Params), ctypes.POINTER(P)]),
+        "lulesh_destroy": (ctypes.c_int, [P]),
+        "lulesh_time_increment": (ctypes.c_int, [P]),
+        "lulesh_lagrange_leapfrog": (ctypes.c_int, [P]),
+        "lulesh_run": (ctypes.c_int, [P, i64, ctypes.POINTER(_Scalars)]),
+        "lulesh_get_scalars": (ctypes.c_int, [P, ctypes.POINTER(_Scalars)]),
+        "lulesh_get_scalar": (ctypes.c_int, [P, i32, ctypes.POINTER(dbl)]),
+        "lulesh_set_scalar": (ctypes.c_int, [P, i32, dbl]),
+        "lulesh_field_length": (ctypes.c_int, [P, i32, ctypes.POINTER(i64)]),
+        "lulesh_download_field": (ctypes.c_int, [P, i32, P, i64]),
+        "lulesh_upload_field": (ctypes.c_int, [P, i32, P, i64]),
+        "lulesh_verify": (ctypes.c_int, [P, ctypes.POINTER(dbl)]),
+        "lulesh_sizes": (ctypes.c_int, [P, ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "lulesh_get_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "lulesh_enable_timing": (ctypes.c_int, [P, i32]),
+        "lulesh_kernel_times": (ctypes.c_int, [P, ctypes.POINTER(dbl), i32, ctypes.POINTER(i32)]),
+        "lulesh_kernel_name": (ctypes.c_char_p, [i32]),
+        "lulesh_status_string": (ctypes.c_char_p, [i32]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(L, name)
+        fn.restype = res
+        fn.argtypes = args
+    _LIB = L
+    return L
+
+
+def _check(rc, what):
+    if rc == 0:
+        return
+    L = load_library()
+    raise LuleshError(f"{what}: {L.lulesh_status_string(rc).decode()}", rc)
+
+
+class LuleshProblem:
+    """LuleshProblem (src/LULESH.jl:31-49) for one rank on one GPU.
+
+    `devicetype` and `floattype` of the reference are fixed: device FP64.
+    """
+
+    def __init__(self, num_iters=10, structured=True, nx=45, nr=11, balance=1, cost=1,
+                 mode=MODE_FAITHFUL, region_reps=False, keep_aux=False, device=0, region_seed=0):
+        if not structured:
+            raise LuleshError("Reading unstructured mesh is currently missing in the Julia version of LULESH.")
+        self.num_iters = int(num_iters)
+        self.structured = True
+        self.nx = int(nx)
+        self.nr = int(nr)
+        self.balance = int(balance)
+        self.cost = int(cost)
+        self.mode = int(mode)
+        self.region_reps = bool(region_reps)
+        self.keep_aux = bool(keep_aux)
+        self.device = int(device)
+        self.region_seed = int(region_seed)
+        # single rank: col = row = plane = 0, side = 1 (initMeshDecomp at one rank)
+        self.col = self.row = self.plane = 0
+        self.side = 1
+
+
+class Domain:
+    """The reference's Domain{Float64} (src/types.jl) held on the GPU.
+
+    Field attributes (`domain.e`, `domain.x`, ...) return host numpy copies;
+    assigning an array uploads it. Scalars (`domain.time`, `domain.hgcoef`,
+    ...) read and write the handle's Domain scalars.
+    """
+
+    def __init__(self, prob):
+        L = load_library()
+        p = _Params()
+        L.lulesh_default_params(ctypes.byref(p), prob.nx)
+        p.nr, p.balance, p.cost, p.mode = prob.nr, prob.balance, prob.cost, prob.mode
+        p.region_reps, p.keep_aux, p.device = int(prob.region_reps), int(prob.keep_aux), prob.device
+        p.region_seed = prob.region_seed
+        h = ctypes.c_void_p()
+        _check(L.lulesh_create(ctypes.byref(p), ctypes.byref(h)), "Domain(prob)")
+        object.__setattr__(self, "_h", h)
+        object.__setattr__(self, "_L", L)
+        object.__setattr__(self, "prob", prob)
+        ne, nn = ctypes.c_int64(), ctypes.c_int64()
+        L.lulesh_sizes(h, ctypes.byref(ne), ctypes.byref(nn))
+        object.__setattr__(self, "numElem", ne.value)
+        object.__setattr__(self, "numNode", nn.value)
+        object.__setattr__(self, "sizeX", prob.nx)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            self._L.lulesh_destroy(self._h)
+            object.__setattr__(self, "_h", None)
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def field(self, name):
+        fid, dt = FIELDS[name]
+        n = ctypes.c_int64()
+        _check(self._L.lulesh_field_length(self._h, fid, ctypes.byref(n)), f"length of {name}")
+        out = np.empty(n.value, dtype=dt)
+        _check(self._L.lulesh_download_field(self._h, fid, out.ctypes.data_as(ctypes.c_void_p), n.value),
+               f"download {name}")
+        return out
+
+    def set_field(self, name, values):
+        fid, dt = FIELDS[name]
+        arr = np.ascontiguousarray(values, dtype=dt)
+        _check(self._L.lulesh_upload_field(self._h, fid, arr.ctypes.data_as(ctypes.c_void_p), arr.size),
+               f"upload {name}")
+
+    def scalars(self):
+        s = _Scalars()
+        _check(self._L.lulesh_get_scalars(self._h, ctypes.byref(s)), "scalars")
+        return {k: getattr(s, k) for k, _ in _Scalars._fields_}
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(self._L.lulesh_get_stream(self._h, ctypes.byref(s)), "stream")
+        return s.value
+
+    def enable_timing(self, on=True):
+        _check(self._L.lulesh_enable_timing(self._h, int(on)), "timing")
+
+    def kernel_times(self):
+        ms = (ctypes.c_double * 16)()
+        n = ctypes.c_int32()
+        _check(self._L.lulesh_kernel_times(self._h, ms, 16, ctypes.byref(n)), "kernel times")
+        return {self._L.lulesh_kernel_name(i).decode(): ms[i] for i in range(n.value)}
+
+    def __getattr__(self, name):
+        if name in FIELDS:
+            return self.field(name)
+        if name in SCALARS:
+            v = ctypes.c_double()
+            _check(self._L.lulesh_get_scalar(self._h, SCALARS[name], ctypes.byref(v)), name)
+            return int(v.value) if name == "cycle" else v.value
+        raise AttributeError(name)
+
+    def __setattr__(self, name, value):
+        if name in FIELDS:
+            self.set_field(name, value)
+        elif name in SCALARS:
+            _check(self._L.lulesh_set_scalar(self._h, SCALARS[name], float(value)), name)
+        else:
+            object.__setattr__(self, name, value)
+
+
+def _raise_step(domain, rc):
+    s = domain.scalars()
+    msg = _MESSAGES.get((rc, s["site"] if rc == 1 else 0), None)
+    if msg is None:
+        msg = load_library().lulesh_status_string(rc).decode()
+    raise LuleshError(msg, rc, s["site"])
+
+
+def timeIncrement(domain):
+    """timeIncrement!(domain), src/domain.jl:920-961."""
+    _check(domain._L.lulesh_time_increment(domain._h), "timeIncrement!")
+
+
+def lagrangeLeapFrog(domain):
+    """lagrangeLeapFrog(domain), src/domain.jl:3067-3080 (one step on the GPU)."""
+    rc = domain._L.lulesh_lagrange_leapfrog(domain._h)
+    if rc:
+        _raise_step(domain, rc)
+
+
+def run(domain, num_iters):
+    """The examples/benchmark.jl:82-98 loop, device-resident; returns the scalars."""
+    s = _Scalars()
+    rc = domain._L.lulesh_run(domain._h, int(num_iters), ctypes.byref(s))
+    if rc:
+        _raise_step(domain, rc)
+    return {k: getattr(s, k) for k, _ in _Scalars._fields_}
+
+
+def verify(domain):
+    """(origin energy, MaxAbsDiff, TotalAbsDiff, MaxRelDiff), src/utils.jl:124-158."""
+    out = (ctypes.c_double * 4)()
+    _check(domain._L.lulesh_verify(domain._h, out), "verify")
+    return tuple(out)
+
+
+def verifyAndWriteFinalOutput(elapsed_time, domain, nx, numRanks=1, file=None):
+    """Prints the reference's final report (src/utils.jl:124-164); returns its numbers."""
+    import sys
+    f = file or sys.stdout
+    e0, maxabs, total, maxrel = verify(domain)
+    cyc = domain.cycle
+    grind1 = ((elapsed_time * 1e6) / cyc) / (nx * nx * nx) if cyc else float("nan")
+    grind2 = ((elapsed_time * 1e6) / cyc) / (nx * nx * nx * numRanks) if cyc else float("nan")
+    print("Run completed:", file=f)
+    print(f"   Problem size        =  {nx}", file=f)
+    print(f"   MPI tasks           =  {numRanks}", file=f)
+    print(f"   Iteration count     =  {cyc}", file=f)
+    print(f"   Final Origin Energy =  {e0:.6e}", file=f)
+    print("   Testing Plane 0 of Energy Array on rank 0:", file=f)
+    print(f"        MaxAbsDiff   = {maxabs:.6e}", file=f)
+    print(f"        TotalAbsDiff = {total:.6e}", file=f)
+    print(f"        MaxRelDiff   = {maxrel:.6e}", file=f)
+    print(f"\nElapsed time         = {elapsed_time:.2f} (s)", file=f)
+    # the reference prints elapsed_time where it means grindTime2 (src/utils.jl:162)
+    print(f"Grind time (us/z/c)  =  {grind1:.8f}  (per dom)  ({elapsed_time:.8f} overall)", file=f)
+    print(f"FOM                  = {1000.0 / grind2:.8f} (z/s)\n", file=f)
+    return {"origin_energy": e0, "MaxAbsDiff": maxabs, "TotalAbsDiff": total, "MaxRelDiff": maxrel,
+            "cycle": cyc, "grind_us": grind2, "fom_kzs": 1000.0 / grind2}

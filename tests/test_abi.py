@@ -1,0 +1,77 @@
+"""CPU checks of the C ABI: the library loads and exports what the headers declare."""
+import ctypes
+import glob
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADERS = sorted(glob.glob(os.path.join(ROOT, "include", "*.h")))
+DECL = re.compile(r"^\s*(?:[A-Za-z_][\w\s\*]*?)\b(lulesh_\w+)\s*\(", re.M)
+
+
+def declared_functions():
+    names = []
+    for h in HEADERS:
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names += [n for n in DECL.findall(text)]
+    return sorted(set(names))
+
+
+def enum_values(header, prefix):
+    text = re.sub(r"/\*.*?\*/", "", open(header).read(), flags=re.S)
+    vals, cur = {}, -1
+    for m in re.finditer(r"\b(" + prefix + r"\w+)\s*(?:=\s*(\d+))?\s*[,}\n]", text):
+        cur = int(m.group(2)) if m.group(2) else cur + 1
+        vals[m.group(1)] = cur
+    return vals
+
+
+def test_headers_declare_functions():
+    names = declared_functions()
+    assert "lulesh_create" in names and "lulesh_lagrange_leapfrog" in names
+    assert len(names) >= 18
+
+
+def test_library_exports_every_declared_symbol(gpu_lib):
+    lib = ctypes.CDLL(gpu_lib.library_path())
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_calls_that_need_no_gpu(gpu_lib):
+    L = gpu_lib.load_library()
+    p = gpu_lib._Params()
+    L.lulesh_default_params(ctypes.byref(p), 30)
+    assert (p.nx, p.nr, p.balance, p.cost, p.mode) == (30, 11, 1, 1, 0)
+    assert L.lulesh_status_string(2) == b"QStopError"
+    assert L.lulesh_kernel_name(1) == b"k_force"
+    # invalid problems are rejected before any CUDA call
+    h = ctypes.c_void_p()
+    p.nx = 0
+    assert L.lulesh_create(ctypes.byref(p), ctypes.byref(h)) == 6
+    p.nx, p.mode = 8, 9
+    assert L.lulesh_create(ctypes.byref(p), ctypes.byref(h)) == 6
+    assert L.lulesh_destroy(None) == 6
+
+
+def test_python_ids_match_header(gpu_lib):
+    h = os.path.join(ROOT, "include", "lulesh_gb300.h")
+    fields = enum_values(h, "LULESH_F_")
+    for name, (fid, _) in gpu_lib.FIELDS.items():
+        key = "LULESH_F_" + name.upper()
+        assert fields[key] == fid, name
+    scal = enum_values(h, "LULESH_S_")
+    for name, sid in gpu_lib.SCALARS.items():
+        assert scal["LULESH_S_" + name.upper()] == sid, name
+
+
+def test_no_fallback_without_library(tmp_path, monkeypatch):
+    import lulesh_gb300
+    monkeypatch.setenv("LULESH_GB300_LIB", str(tmp_path / "missing.so"))
+    monkeypatch.setattr(lulesh_gb300, "_LIB", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        lulesh_gb300.load_library()

@@ -1,0 +1,239 @@
+"""GPU parity of liblulesh_gb300 against the CPU oracle (through the C ABI).
+
+Tolerances (the benchmark spec's FP64 bar): the same cycle count and final time
+(relative 1e-12), origin energy to relative 1e-9 and every field to a maximum
+relative error of 1e-8, with the field's cut-off (or 1e-12 of its largest
+magnitude) as the floor of the denominator. Integer and setup fields must be
+bit-identical.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, field_floor, rel_err
+
+pytestmark = pytest.mark.gpu
+
+FIELD_TOL = 1e-8
+STATE_F64 = ["e", "p", "q", "v", "ss", "x", "y", "z", "xd", "yd", "zd"]
+STEP_F64 = STATE_F64 + ["vnew", "delv", "arealg", "vdov", "delv_xi", "delv_eta", "delv_zeta",
+                        "delx_xi", "delx_eta", "delx_zeta"]
+AUX_F64 = ["fx", "fy", "fz", "xdd", "ydd", "zdd", "dxx", "dyy", "dzz", "ql", "qq"]
+INDEX_FIELDS = ["nodelist", "lxim", "lxip", "letam", "letap", "lzetam", "lzetap", "symmX", "symmY",
+                "symmZ", "nodeElemCount", "nodeElemStart", "nodeElemCornerList", "matElemlist",
+                "regNumList", "regElemlist", "regCSR", "regReps", "regSorted", "regElemSize"]
+
+
+def pair(L, oracle_mod, nx, mode=0, nr=11, keep_aux=False, **kw):
+    g = L.Domain(L.LuleshProblem(nx=nx, nr=nr, mode=mode, keep_aux=keep_aux, **kw))
+    o = oracle_mod.OracleDomain(nx, nr=nr, mode=mode)
+    return g, o
+
+
+# The kept auxiliary fields are nodal sums with heavy cancellation (forces,
+# accelerations) or deviatoric differences; their floor is 1e-7 of the
+# field's largest magnitude.
+AUX_FLOOR = 1e-7
+
+
+def assert_fields(g, o, names, tol=FIELD_TOL, where=""):
+    worst = {}
+    for n in names:
+        a, b = g.field(n), o.field(n)
+        assert a.shape == b.shape, n
+        floor = field_floor(n, b)
+        if n in AUX_F64:
+            floor = max(floor, AUX_FLOOR * float(np.max(np.abs(b))))
+        worst[n] = rel_err(a, b, floor)
+    bad = {k: v for k, v in worst.items() if not (v <= tol)}
+    assert not bad, f"{where} fields beyond {tol}: {bad}"
+    return worst
+
+
+def assert_scalars(g, o, rel=1e-12):
+    for s in ["time", "deltatime", "dtcourant", "dthydro"]:
+        assert getattr(g, s) == pytest.approx(o.get(s), rel=rel), s
+    assert g.cycle == o.get("cycle")
+
+
+def test_setup_is_bit_identical(gpu_lib, oracle_mod):
+    g, o = pair(gpu_lib, oracle_mod, 7, nr=11, balance=2, cost=3)
+    for n in INDEX_FIELDS:
+        assert np.array_equal(g.field(n), o.field(n)), n
+    assert np.array_equal(g.field("elemBC"), o.field("elemBC"))
+    for n in ["x", "y", "z", "volo", "elemMass", "nodalMass", "e", "v", "p", "q", "ss", "xd"]:
+        assert np.array_equal(g.field(n), o.field(n)), n
+    assert g.deltatime == o.get("deltatime")
+    for s in gpu_lib.SCALARS:
+        if s != "cycle":
+            assert getattr(g, s) == o.get(s), s
+
+
+@pytest.mark.parametrize("mode", [0, 1, 2, 4, 7])
+def test_first_steps_match(gpu_lib, oracle_mod, mode):
+    g, o = pair(gpu_lib, oracle_mod, 6, mode=mode, keep_aux=True)
+    for step in range(4):
+        gpu_lib.timeIncrement(g)
+        o.time_increment()
+        gpu_lib.lagrangeLeapFrog(g)
+        assert o.lagrange_leapfrog() == 0
+        assert_scalars(g, o)
+        assert_fields(g, o, STEP_F64 + AUX_F64, tol=1e-10, where=f"step {step}")
+
+
+@pytest.mark.parametrize("mode", [0, 7])
+def test_one_step_from_developed_state(gpu_lib, oracle_mod, mode):
+    """Load the oracle's state after 120 cycles into the GPU and take one step."""
+    nx = 12
+    g, o = pair(gpu_lib, oracle_mod, nx, mode=mode, keep_aux=True)
+    assert o.run(120) == 0
+    for n in STATE_F64:
+        g.set_field(n, o.field(n))
+    for s in ["time", "deltatime", "dtcourant", "dthydro", "cycle"]:
+        setattr(g, s, o.get(s))
+    gpu_lib.timeIncrement(g)
+    o.time_increment()
+    gpu_lib.lagrangeLeapFrog(g)
+    assert o.lagrange_leapfrog() == 0
+    assert_scalars(g, o)
+    assert_fields(g, o, STEP_F64 + AUX_F64, tol=1e-10)
+
+
+GOLDEN = json.load(open(os.path.join(ROOT, "tests", "golden", "oracle_runs.json")))
+
+
+@pytest.mark.parametrize("name", sorted(GOLDEN))
+def test_run_parity(gpu_lib, oracle_mod, name):
+    c = GOLDEN[name]
+    g, o = pair(gpu_lib, oracle_mod, c["nx"], mode=c["mode"])
+    s = gpu_lib.run(g, c["num_iters"])
+    assert o.run(c["num_iters"]) == 0
+    assert s["cycle"] == o.get("cycle") == c["cycle"]
+    assert s["time"] == pytest.approx(o.get("time"), rel=1e-12)
+    assert g.field("e")[0] == pytest.approx(o.field("e")[0], rel=1e-9)
+    assert_fields(g, o, STATE_F64 + ["arealg", "vdov", "delv"])
+    # LULESH's own symmetry check gives the same numbers
+    e0, maxabs, total, maxrel = gpu_lib.verify(g)
+    omaxabs, ototal, omaxrel = o.symmetry()
+    scale = np.abs(o.field("e")[: c["nx"] ** 2]).max()
+    assert abs(maxabs - omaxabs) <= 1e-8 * scale
+    assert abs(total - ototal) <= 1e-8 * scale * c["nx"] ** 2
+
+
+def test_run_equals_stepwise_and_is_deterministic(gpu_lib, oracle_mod):
+    a = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10))
+    b = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10))
+    c = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10))
+    gpu_lib.run(a, 75)
+    gpu_lib.run(c, 75)
+    for _ in range(75):
+        gpu_lib.timeIncrement(b)
+        gpu_lib.lagrangeLeapFrog(b)
+    for n in STATE_F64 + ["vdov", "arealg"]:
+        assert np.array_equal(a.field(n), b.field(n)), n
+        assert np.array_equal(a.field(n), c.field(n)), n
+    assert a.time == b.time and a.dtcourant == b.dtcourant and a.cycle == b.cycle == 75
+
+
+def test_run_to_stoptime_stops_exactly(gpu_lib):
+    g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10, mode=gpu_lib.MODE_LULESH2))
+    s = gpu_lib.run(g, 10**9)
+    assert s["time"] == 1e-2
+    s2 = gpu_lib.run(g, 10**9)  # time >= stoptime: the loop does not enter
+    assert s2["cycle"] == s["cycle"]
+
+
+def test_num_iters_semantics(gpu_lib):
+    g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=6))
+    assert gpu_lib.run(g, 5)["cycle"] == 5
+    assert gpu_lib.run(g, 5)["cycle"] == 6   # benchmark.jl always takes one step
+    assert gpu_lib.run(g, 40)["cycle"] == 40
+
+
+# ---- errors: the reference's error(...) sites, provoked on the host ----------
+
+def test_qstop_error(gpu_lib, oracle_mod):
+    g, o = pair(gpu_lib, oracle_mod, 6)
+    gpu_lib.run(g, 10)
+    o.run(10)
+    assert o.field("q").max() > 0.0
+    g.qstop = 1e-30
+    o.set("qstop", 1e-30)
+    gpu_lib.timeIncrement(g)
+    o.time_increment()
+    with pytest.raises(gpu_lib.LuleshError, match="QStopError"):
+        gpu_lib.lagrangeLeapFrog(g)
+    assert o.lagrange_leapfrog() == 2
+
+
+def test_inverted_element_volume_error(gpu_lib, oracle_mod):
+    g, o = pair(gpu_lib, oracle_mod, 4)
+    x = g.field("x")
+    x[1] = -0.9  # drag a node of element 0 through its neighbour
+    g.set_field("x", x)
+    o.view("x")[1] = -0.9
+    gpu_lib.timeIncrement(g)
+    o.time_increment()
+    with pytest.raises(gpu_lib.LuleshError, match="Early Volume Error"):
+        gpu_lib.lagrangeLeapFrog(g)
+    assert o.lagrange_leapfrog() == 1 and o.error_site() == 1
+
+
+def test_negative_relative_volume_error(gpu_lib, oracle_mod):
+    g, o = pair(gpu_lib, oracle_mod, 4)
+    v = g.field("v")
+    v[5] = -1.0
+    g.set_field("v", v)
+    o.view("v")[5] = -1.0
+    gpu_lib.timeIncrement(g)
+    o.time_increment()
+    with pytest.raises(gpu_lib.LuleshError, match="Volume Error: Volume is negative"):
+        gpu_lib.lagrangeLeapFrog(g)
+    assert o.lagrange_leapfrog() == 1 and o.error_site() == 2
+
+
+def test_bad_bc_mask_error(gpu_lib, oracle_mod):
+    g, o = pair(gpu_lib, oracle_mod, 4)
+    bc = g.field("elemBC")
+    bc[0] |= 0x2  # XI_M_SYMM | XI_M_FREE is not a valid case
+    g.set_field("elemBC", bc)
+    o.view("elemBC")[0] |= 0x2
+    gpu_lib.timeIncrement(g)
+    o.time_increment()
+    with pytest.raises(gpu_lib.LuleshError, match="^Error$"):
+        gpu_lib.lagrangeLeapFrog(g)
+    assert o.lagrange_leapfrog() == 3
+
+
+def test_error_stops_device_run(gpu_lib):
+    g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=6))
+    gpu_lib.run(g, 10)
+    assert g.field("q").max() > 0.0
+    g.qstop = 1e-30
+    with pytest.raises(gpu_lib.LuleshError, match="QStopError"):
+        gpu_lib.run(g, 50)
+    assert g.cycle == 11  # the failing cycle's timeIncrement ran, nothing after
+
+
+# ---- full-size checks -----------------------------------------------------------
+
+def test_full_size_s150_matches_oracle(gpu_lib, oracle_mod):
+    """The benchmark mesh (150^3) for a few cycles against the oracle."""
+    g, o = pair(gpu_lib, oracle_mod, 150, mode=0)
+    gpu_lib.run(g, 3)
+    assert o.run(3) == 0
+    assert_scalars(g, o)
+    assert_fields(g, o, STATE_F64 + ["vdov", "arealg"])
+
+
+def test_full_size_s150_is_deterministic(gpu_lib):
+    a = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=150))
+    b = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=150))
+    gpu_lib.run(a, 6)
+    gpu_lib.run(b, 6)
+    for n in ["e", "xd", "q", "ss"]:
+        assert np.array_equal(a.field(n), b.field(n)), n
+    a.close()
+    b.close()
