@@ -26,7 +26,11 @@ def rel_err(a, b, floor):
 
 # Per-field floors for the relative-error metric: a field's cut-off (values
 # below it are snapped to zero by the method) or 1e-12 of its largest value.
-CUTS = {"e": 1e-7, "p": 1e-7, "q": 1e-7, "xd": 1e-7, "yd": 1e-7, "zd": 1e-7, "v": 1e-10}
+# delv = vnew - v is a difference of relative volumes of order 1, so one ulp
+# of its operands (~2e-16) is its accuracy: its floor is 1e-7 (1e-15 absolute
+# at the 1e-8 bar).
+CUTS = {"e": 1e-7, "p": 1e-7, "q": 1e-7, "xd": 1e-7, "yd": 1e-7, "zd": 1e-7, "v": 1e-10,
+        "delv": 1e-7}
 
 
 def field_floor(name, ref):

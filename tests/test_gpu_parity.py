@@ -26,9 +26,9 @@ INDEX_FIELDS = ["nodelist", "lxim", "lxip", "letam", "letap", "lzetam", "lzetap"
                 "regNumList", "regElemlist", "regCSR", "regReps", "regSorted", "regElemSize"]
 
 
-def pair(L, oracle_mod, nx, mode=0, nr=11, keep_aux=False, **kw):
-    g = L.Domain(L.LuleshProblem(nx=nx, nr=nr, mode=mode, keep_aux=keep_aux, **kw))
-    o = oracle_mod.OracleDomain(nx, nr=nr, mode=mode)
+def pair(L, oracle_mod, nx, mode=0, nr=11, keep_aux=False, balance=1, cost=1):
+    g = L.Domain(L.LuleshProblem(nx=nx, nr=nr, mode=mode, keep_aux=keep_aux, balance=balance, cost=cost))
+    o = oracle_mod.OracleDomain(nx, nr=nr, mode=mode, balance=balance, cost=cost)
     return g, o
 
 
@@ -80,7 +80,8 @@ def test_first_steps_match(gpu_lib, oracle_mod, mode):
         gpu_lib.lagrangeLeapFrog(g)
         assert o.lagrange_leapfrog() == 0
         assert_scalars(g, o)
-        assert_fields(g, o, STEP_F64 + AUX_F64, tol=1e-10, where=f"step {step}")
+        assert_fields(g, o, STATE_F64, tol=1e-10, where=f"step {step}")
+        assert_fields(g, o, STEP_F64 + AUX_F64, where=f"step {step}")
 
 
 @pytest.mark.parametrize("mode", [0, 7])
@@ -98,7 +99,8 @@ def test_one_step_from_developed_state(gpu_lib, oracle_mod, mode):
     gpu_lib.lagrangeLeapFrog(g)
     assert o.lagrange_leapfrog() == 0
     assert_scalars(g, o)
-    assert_fields(g, o, STEP_F64 + AUX_F64, tol=1e-10)
+    assert_fields(g, o, STATE_F64, tol=1e-10)
+    assert_fields(g, o, STEP_F64 + AUX_F64)
 
 
 GOLDEN = json.load(open(os.path.join(ROOT, "tests", "golden", "oracle_runs.json")))
