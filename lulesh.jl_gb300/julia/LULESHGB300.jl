@@ -1,0 +1,177 @@
+# Julia binding of liblulesh_gb300 for LULESH.jl (single rank, one GPU).
+#
+# `GPUDomain(prob)` replaces `Domain(prob)`; `timeIncrement!` and
+# `lagrangeLeapFrog` get methods for it, so the loop of
+# examples/benchmark.jl:82-98 runs unchanged:
+#
+#     using LULESH, LULESHGB300
+#     prob = LuleshProblem(num_iters, true, nx, nr, balance, cost, Vector, Float64, nothing)
+#     domain = GPUDomain(prob)
+#     while domain.time < domain.stoptime
+#         timeIncrement!(domain)
+#         lagrangeLeapFrog(domain)
+#         domain.cycle >= num_iters && break
+#     end
+#     verifyAndWriteFinalOutput(elapsed, domain, nx, 1)
+#
+# Scalars (`domain.time`, `domain.hgcoef`, ...) and fields (`domain.e`,
+# `domain.x`, ...) read through to the device; a field read returns a host
+# copy, `setproperty!` of a field uploads it.
+module LULESHGB300
+
+using LULESH
+
+export GPUDomain, LuleshGPUError
+
+const libpath = get(ENV, "LULESH_GB300_LIB",
+                    joinpath(@__DIR__, "..", "lib", "liblulesh_gb300.so"))
+
+# lulesh_params / lulesh_scalars of include/lulesh_gb300.h
+struct Params
+    nx::Int32
+    nr::Int32
+    balance::Int32
+    cost::Int32
+    mode::Int32
+    region_reps::Int32
+    keep_aux::Int32
+    device::Int32
+    region_seed::UInt64
+end
+
+struct Scalars
+    time::Float64
+    deltatime::Float64
+    dtcourant::Float64
+    dthydro::Float64
+    cycle::Int64
+    status::Int32
+    site::Int32
+end
+
+const FIELD_IDS = Dict{Symbol,Tuple{Int32,DataType}}()
+let elem = (:e, :p, :q, :ql, :qq, :v, :volo, :delv, :vdov, :arealg, :ss, :elemMass, :vnew,
+            :delv_xi, :delv_eta, :delv_zeta, :delx_xi, :delx_eta, :delx_zeta, :dxx, :dyy, :dzz),
+    node = (:x, :y, :z, :xd, :yd, :zd, :xdd, :ydd, :zdd, :fx, :fy, :fz, :nodalMass),
+    idx = (:nodelist, :lxim, :lxip, :letam, :letap, :lzetam, :lzetap, :symmX, :symmY, :symmZ,
+           :nodeElemCount, :nodeElemStart, :nodeElemCornerList, :matElemlist, :regNumList,
+           :regElemlist, :regCSR, :regReps, :regSorted, :regElemSize)
+    for (i, s) in enumerate(elem); FIELD_IDS[s] = (Int32(i - 1), Float64); end
+    for (i, s) in enumerate(node); FIELD_IDS[s] = (Int32(31 + i), Float64); end
+    for (i, s) in enumerate(idx); FIELD_IDS[s] = (Int32(63 + i), Int64); end
+    FIELD_IDS[:elemBC] = (Int32(96), UInt32)
+end
+
+const SCALAR_IDS = Dict(s => Int32(i - 1) for (i, s) in enumerate((
+    :dtfixed, :deltatimemultlb, :deltatimemultub, :stoptime, :dtmax, :dthydro, :dtcourant, :time,
+    :deltatime, :u_cut, :hgcoef, :qstop, :monoq_max_slope, :monoq_limiter_mult, :e_cut, :p_cut,
+    :ss4o3, :q_cut, :v_cut, :qlc_monoq, :qqc_monoq, :qqc, :eosvmax, :eosvmin, :pmin, :emin,
+    :dvovmax, :refdens, :cycle)))
+
+# the reference's error(...) messages per (status, site)
+const MESSAGES = Dict((1, 1) => "Early Volume Error", (1, 2) => "Volume Error: Volume is negative",
+                      (1, 3) => "Mid Volume Error", (1, 4) => "Volume Error: calcKinematicsForElems",
+                      (1, 5) => "Volume Error :2157", (1, 6) => "Volume Error :2887",
+                      (1, 7) => "Volume Error :2908", (2, 0) => "QStopError", (3, 0) => "Error")
+
+struct LuleshGPUError <: Exception
+    msg::String
+    status::Int32
+end
+Base.showerror(io::IO, e::LuleshGPUError) = print(io, e.msg)
+
+mutable struct GPUDomain
+    handle::Ptr{Cvoid}
+    nx::Int
+    function GPUDomain(prob::LuleshProblem; mode::Integer=0, device::Integer=0, keep_aux::Bool=false)
+        prob.structured || error("Reading unstructured mesh is currently missing in the Julia version of LULESH.")
+        p = Ref{Params}()
+        ccall((:lulesh_default_params, libpath), Cvoid, (Ptr{Params}, Int32), p, prob.nx)
+        p[] = Params(prob.nx, prob.nr, prob.balance, prob.cost, mode, 0, keep_aux, device, 0)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:lulesh_create, libpath), Cint, (Ptr{Params}, Ptr{Ptr{Cvoid}}), p, h)
+        rc == 0 || throw(LuleshGPUError("Domain(prob) failed with status $rc", rc))
+        d = new(h[], prob.nx)
+        finalizer(d) do x
+            x.handle == C_NULL || ccall((:lulesh_destroy, libpath), Cint, (Ptr{Cvoid},), x.handle)
+            x.handle = C_NULL
+        end
+        return d
+    end
+end
+
+function step_error(d::GPUDomain, rc)
+    s = Ref{Scalars}()
+    ccall((:lulesh_get_scalars, libpath), Cint, (Ptr{Cvoid}, Ptr{Scalars}), getfield(d, :handle), s)
+    key = (Int(rc), rc == 1 ? Int(s[].site) : 0)
+    throw(LuleshGPUError(get(MESSAGES, key, "status $rc"), rc))
+end
+
+function LULESH.timeIncrement!(d::GPUDomain)
+    rc = ccall((:lulesh_time_increment, libpath), Cint, (Ptr{Cvoid},), getfield(d, :handle))
+    rc == 0 || step_error(d, rc)
+    return nothing
+end
+
+function LULESH.lagrangeLeapFrog(d::GPUDomain)
+    rc = ccall((:lulesh_lagrange_leapfrog, libpath), Cint, (Ptr{Cvoid},), getfield(d, :handle))
+    rc == 0 || step_error(d, rc)
+    return nothing
+end
+
+# examples/benchmark.jl's whole loop on the device (no per-cycle host sync)
+function run!(d::GPUDomain, num_iters::Integer)
+    s = Ref{Scalars}()
+    rc = ccall((:lulesh_run, libpath), Cint, (Ptr{Cvoid}, Int64, Ptr{Scalars}),
+               getfield(d, :handle), num_iters, s)
+    rc == 0 || step_error(d, rc)
+    return s[]
+end
+
+function Base.getproperty(d::GPUDomain, s::Symbol)
+    s in (:handle, :nx) && return getfield(d, s)
+    h = getfield(d, :handle)
+    if haskey(SCALAR_IDS, s)
+        v = Ref{Float64}()
+        ccall((:lulesh_get_scalar, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}), h, SCALAR_IDS[s], v)
+        return s === :cycle ? Int(v[]) : v[]
+    elseif haskey(FIELD_IDS, s)
+        id, T = FIELD_IDS[s]
+        n = Ref{Int64}()
+        ccall((:lulesh_field_length, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Int64}), h, id, n)
+        out = Vector{T}(undef, n[])
+        rc = ccall((:lulesh_download_field, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Cvoid}, Int64),
+                   h, id, out, n[])
+        rc == 0 || throw(LuleshGPUError("download of $s failed", rc))
+        return out
+    elseif s === :numElem
+        return getfield(d, :nx)^3
+    elseif s === :numNode
+        return (getfield(d, :nx) + 1)^3
+    end
+    error("GPUDomain has no field $s")
+end
+
+function Base.setproperty!(d::GPUDomain, s::Symbol, v)
+    h = getfield(d, :handle)
+    if haskey(SCALAR_IDS, s)
+        ccall((:lulesh_set_scalar, libpath), Cint, (Ptr{Cvoid}, Int32, Float64), h, SCALAR_IDS[s], v)
+    elseif haskey(FIELD_IDS, s)
+        id, T = FIELD_IDS[s]
+        a = convert(Vector{T}, v)
+        rc = ccall((:lulesh_upload_field, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Cvoid}, Int64),
+                   h, id, a, length(a))
+        rc == 0 || throw(LuleshGPUError("upload of $s failed", rc))
+    else
+        setfield!(d, s, v)
+    end
+    return v
+end
+
+# verifyAndWriteFinalOutput reads domain.cycle and domain.e[...] only
+LULESH.verifyAndWriteFinalOutput(t, d::GPUDomain, nx, ranks) = begin
+    e = d.e
+    LULESH.verifyAndWriteFinalOutput(t, (cycle = d.cycle, e = e), nx, ranks)
+end
+
+end # module
