@@ -181,6 +181,44 @@ const char* lulesh_kernel_name(int32_t index);
  * step is bound by. */
 int lulesh_measure_fp64_peak(int32_t device, double* fma_per_s, double* add_per_s);
 
+/* ---- Nodal forces without device allocation -----------------------------
+ * No counterpart in the reference. For callers that keep the Domain's arrays
+ * in device memory they manage themselves and must not let a library
+ * allocate device memory (for example a Julia program whose CuArrays come
+ * from its own memory pool, or an application that budgets every byte of
+ * device memory up front). The caller passes device pointers to its own
+ * arrays in the reference's Domain layout; the corner-force scratch the
+ * computation needs is a fixed array inside the library, so the call makes no
+ * cudaMalloc, cudaFree or other allocating call.
+ *   - at most LULESH_STATIC_MAX_ELEMS elements; larger problems are rejected
+ *     with LULESH_ERR_ARGUMENT. The fixed array (6 MiB) stays resident on
+ *     every GPU that loads the library until the process exits.
+ *   - every call shares that array: calls that overlap on the GPU (two
+ *     streams or two host threads at once) race and give wrong forces.
+ *   - the first call on a device looks up the array's address on that
+ *     device; make it before any stream capture.
+ * Computes fx, fy, fz exactly as calcForceForNodes (src/domain.jl:1764-1779)
+ * does from the given state, on `stream` (a cudaStream_t, 0 for the legacy
+ * default stream), and synchronizes that stream before returning.
+ * Returns LULESH_ERR_VOLUME (with *site EARLY or HOURGLASS) on the
+ * reference's volume checks. */
+#define LULESH_STATIC_MAX_ELEMS 32768
+
+typedef struct {
+  int64_t num_elem, num_node;
+  const int64_t* nodelist;            /* 8*num_elem, element-major, 0-based node ids */
+  const int64_t* nodeElemStart;       /* num_node, 0-based offsets into nodeElemCornerList */
+  const int64_t* nodeElemCount;       /* num_node */
+  const int64_t* nodeElemCornerList;  /* 8*num_elem, 1-based corner ids 8*e + c + 1 */
+  const double *x, *y, *z, *xd, *yd, *zd;          /* num_node */
+  const double *p, *q, *ss, *v, *volo, *elemMass;  /* num_elem */
+  double hgcoef;
+  int32_t mode;                       /* LULESH_MODE_* bits */
+  double *fx, *fy, *fz;               /* num_node outputs */
+} lulesh_force_args;
+
+int lulesh_calc_force_for_nodes_static(const lulesh_force_args* args, void* stream, int32_t* site);
+
 /* Human-readable text of a status code. */
 const char* lulesh_status_string(int32_t status);
 
