@@ -176,6 +176,68 @@ int lulesh_enable_timing(lulesh_domain* dom, int32_t enable);
 int lulesh_kernel_times(lulesh_domain* dom, double* ms, int32_t max_kernels, int32_t* n_kernels);
 const char* lulesh_kernel_name(int32_t index);
 
+/* ---- Launch tuning --------------------------------------------------------
+ * Threads per block of the four step kernels. lulesh_autotune tries each
+ * candidate for one kernel at a time on the live problem (cycles timed with
+ * CUDA events), keeps the fastest, and restores the problem's state. */
+typedef struct {
+  int32_t force_block;   /* k_force: 64, 128 or 256 */
+  int32_t node_block;    /* k_node: 128, 256 or 512 */
+  int32_t kin_block;     /* k_kinematics: 64, 128 or 256 */
+  int32_t mat_block;     /* k_material: 64, 128 or 256 */
+} lulesh_tuning;
+
+int lulesh_get_tuning(const lulesh_domain* dom, lulesh_tuning* out);
+int lulesh_set_tuning(lulesh_domain* dom, const lulesh_tuning* t);
+int lulesh_autotune(lulesh_domain* dom, int32_t cycles, lulesh_tuning* chosen);
+
+/* ---- Batched ensemble -------------------------------------------------------
+ * Many independent single-rank Sedov problems advanced together: all
+ * instances' elements and nodes are packed into one index space, so every
+ * kernel launch covers every instance whatever their sizes; each instance
+ * keeps its own dt, time, cycle and status, computed on the device. A run is
+ * a sequence of CUDA-graph launches with no host work per cycle. The
+ * reference has one problem per process; this batches Domain(prob) /
+ * timeIncrement! / lagrangeLeapFrog over instances. */
+typedef struct {
+  int32_t nx, nr, balance, cost;
+  double einit;           /* energy deposited in the origin element; 0 = 3.948746e7*(nx/45)^3 */
+  double hgcoef;          /* hourglass coefficient (the reference's default is 3.0) */
+  uint64_t region_seed;
+} lulesh_instance;
+
+typedef struct lulesh_ensemble lulesh_ensemble;
+
+/* Seeded instance draw (std::mt19937_64(seed)): nx uniform in [nx_min, nx_max],
+ * einit = the default for nx times exp(U[ln 0.5, ln 2]), hgcoef uniform in
+ * [2, 4], nr = 1 or 11 with probability 1/2 each, balance = cost = 1. */
+int lulesh_ens_sedov_instances(uint64_t seed, int32_t n, int32_t nx_min, int32_t nx_max,
+                               lulesh_instance* out);
+
+int lulesh_ens_create(const lulesh_instance* instances, int32_t n, int32_t mode, int32_t device,
+                      lulesh_ensemble** out);
+int lulesh_ens_destroy(lulesh_ensemble* ens);
+
+/* examples/benchmark.jl's loop for every instance at once: each instance
+ * steps until its time reaches stoptime or its cycle reaches num_iters.
+ * Returns the first non-zero instance status (others keep running). */
+int lulesh_ens_run(lulesh_ensemble* ens, int64_t num_iters);
+
+/* Returns every instance to its initial state (as created). */
+int lulesh_ens_reset(lulesh_ensemble* ens);
+
+int lulesh_ens_sizes(const lulesh_ensemble* ens, int32_t* n, int64_t* total_elem, int64_t* total_node);
+int lulesh_ens_get_scalars(const lulesh_ensemble* ens, int32_t instance, lulesh_scalars* out);
+int lulesh_ens_field_length(const lulesh_ensemble* ens, int32_t instance, int32_t field, int64_t* count);
+/* FP64 element and node fields of one instance (index fields: use a single
+ * problem handle). */
+int lulesh_ens_download_field(lulesh_ensemble* ens, int32_t instance, int32_t field, void* host,
+                              int64_t count);
+int lulesh_ens_get_stream(lulesh_ensemble* ens, void** stream);
+int lulesh_ens_get_tuning(const lulesh_ensemble* ens, lulesh_tuning* out);
+int lulesh_ens_set_tuning(lulesh_ensemble* ens, const lulesh_tuning* t);
+int lulesh_ens_autotune(lulesh_ensemble* ens, int32_t cycles, lulesh_tuning* chosen);
+
 /* Diagnostic without a reference counterpart: measures the device's FP64
  * FMA and add issue rates (instructions per second), the roof this FP64
  * step is bound by. */

@@ -12,6 +12,7 @@
 #include "lulesh_internal.h"
 #include "lulesh_kernels.h"
 #include "lulesh_setup.h"
+#include "lulesh_arena.h"
 #include "lulesh_device.cuh"
 
 using namespace lulesh;
@@ -51,6 +52,7 @@ struct lulesh_domain {
   bool timing = false;
   std::vector<cudaEvent_t> ring;
   int ring_used = 0;
+  Tuning tuning;
   double kernel_ms[kNumKernels] = {};
   int64_t cycle_i() const { return (int64_t)sc[LULESH_S_CYCLE]; }
 };
@@ -135,55 +137,7 @@ static void state_from_device_mirror(lulesh_domain* d) {
 // ---------------------------------------------------------------------------
 // device memory layout
 // ---------------------------------------------------------------------------
-namespace {
-struct Carver {
-  char* base;
-  size_t off = 0;
-  template <class T> T* take(size_t n) {
-    off = (off + 255) & ~size_t(255);
-    T* p = reinterpret_cast<T*>(base ? base + off : nullptr);
-    off += n * sizeof(T);
-    return p;
-  }
-};
-}  // namespace
-
-static size_t layout(DevDomain& dd, char* base, int64_t E, int64_t N, bool aux) {
-  Carver c{base};
-  dd.x = c.take<double>(N); dd.y = c.take<double>(N); dd.z = c.take<double>(N);
-  dd.xd = c.take<double>(N); dd.yd = c.take<double>(N); dd.zd = c.take<double>(N);
-  dd.nodalMass = c.take<double>(N); dd.inv_nodalMass = c.take<double>(N);
-  if (aux) {
-    dd.xdd = c.take<double>(N); dd.ydd = c.take<double>(N); dd.zdd = c.take<double>(N);
-    dd.fx = c.take<double>(N); dd.fy = c.take<double>(N); dd.fz = c.take<double>(N);
-  } else {
-    dd.xdd = dd.ydd = dd.zdd = dd.fx = dd.fy = dd.fz = nullptr;
-  }
-  dd.nodeBC = c.take<unsigned char>(N);
-  dd.nodeElemStart = c.take<int>(N + 1);
-  dd.cornerList = c.take<int>(8 * E);
-  dd.nodelist = c.take<int>(8 * E);
-  dd.e = c.take<double>(E); dd.p = c.take<double>(E); dd.q = c.take<double>(E); dd.v = c.take<double>(E);
-  dd.volo = c.take<double>(E); dd.inv_volo = c.take<double>(E); dd.elemMass = c.take<double>(E);
-  dd.ss = c.take<double>(E); dd.ql = c.take<double>(E); dd.qq = c.take<double>(E);
-  dd.vnew = c.take<double>(E); dd.delv = c.take<double>(E); dd.arealg = c.take<double>(E);
-  dd.vdov = c.take<double>(E);
-  dd.delv_xi = c.take<double>(E); dd.delv_eta = c.take<double>(E); dd.delv_zeta = c.take<double>(E);
-  dd.delx_xi = c.take<double>(E); dd.delx_eta = c.take<double>(E); dd.delx_zeta = c.take<double>(E);
-  if (aux) {
-    dd.dxx = c.take<double>(E); dd.dyy = c.take<double>(E); dd.dzz = c.take<double>(E);
-  } else {
-    dd.dxx = dd.dyy = dd.dzz = nullptr;
-  }
-  dd.elemBC = c.take<unsigned int>(E);
-  dd.lxim = c.take<int>(E); dd.lxip = c.take<int>(E); dd.letam = c.take<int>(E);
-  dd.letap = c.take<int>(E); dd.lzetam = c.take<int>(E); dd.lzetap = c.take<int>(E);
-  dd.regElemlist0 = nullptr;
-  dd.regOfSlot = nullptr;
-  dd.fcx = c.take<double>(8 * E); dd.fcy = c.take<double>(8 * E); dd.fcz = c.take<double>(8 * E);
-  dd.st = c.take<DevState>(1);
-  return c.off + 256;
-}
+// (the arena layout is shared with the ensemble: lulesh_arena.h)
 
 template <class T>
 static int h2d(T* dst, const T* src, size_t n, cudaStream_t s) {
@@ -285,15 +239,15 @@ static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_incre
     d->ring_used += 1;
   }
   if (ev) cudaEventRecord(ev[0], s);
-  if (with_time_increment) launch_time_increment(d->dd.st, prm, num_iters, s);
+  if (with_time_increment) launch_time_increment(d->dd.st, 1, prm, num_iters, s);
   if (ev) cudaEventRecord(ev[1], s);
-  launch_force(d->dd, prm, s);
+  launch_force(d->dd, prm, d->tuning, s);
   if (ev) cudaEventRecord(ev[2], s);
-  launch_node(d->dd, prm, aux, s);
+  launch_node(d->dd, prm, aux, d->tuning, s);
   if (ev) cudaEventRecord(ev[3], s);
-  launch_kinematics(d->dd, prm, aux, s);
+  launch_kinematics(d->dd, prm, aux, d->tuning, s);
   if (ev) cudaEventRecord(ev[4], s);
-  launch_material(d->dd, prm, aux, s);
+  launch_material(d->dd, prm, aux, d->tuning, s);
   if (ev) cudaEventRecord(ev[5], s);
   CK(cudaGetLastError());
   return LULESH_OK;
@@ -357,10 +311,10 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
 
   const bool aux = params->keep_aux != 0;
   DevDomain& dd = d->dd;
-  const size_t bytes = layout(dd, nullptr, m.E, m.N, aux);
+  const size_t bytes = layout(dd, nullptr, m.E, m.N, aux, 0);
   cudaError_t err = cudaMalloc(&d->arena, bytes);
   if (err != cudaSuccess) { delete d; cudaGetLastError(); return LULESH_ERR_MEMORY; }
-  layout(dd, (char*)d->arena, m.E, m.N, aux);
+  layout(dd, (char*)d->arena, m.E, m.N, aux, 0);
   dd.E = (int)m.E;
   dd.N = (int)m.N;
   dd.nx = nx;
@@ -799,6 +753,68 @@ int lulesh_verify(lulesh_domain* d, double out[4]) {
   out[2] = total;
   out[3] = maxRel;
   return LULESH_OK;
+}
+
+int lulesh_get_tuning(const lulesh_domain* d, lulesh_tuning* out) {
+  if (!d || !out) return LULESH_ERR_ARGUMENT;
+  out->force_block = d->tuning.force;
+  out->node_block = d->tuning.node;
+  out->kin_block = d->tuning.kin;
+  out->mat_block = d->tuning.mat;
+  return LULESH_OK;
+}
+
+int lulesh_set_tuning(lulesh_domain* d, const lulesh_tuning* t) {
+  auto elem_ok = [](int b) { return b == 64 || b == 128 || b == 256; };
+  if (!d || !t || !elem_ok(t->force_block) || !elem_ok(t->kin_block) || !elem_ok(t->mat_block) ||
+      !(t->node_block == 128 || t->node_block == 256 || t->node_block == 512))
+    return LULESH_ERR_ARGUMENT;
+  d->tuning.force = t->force_block;
+  d->tuning.node = t->node_block;
+  d->tuning.kin = t->kin_block;
+  d->tuning.mat = t->mat_block;
+  drop_graph(d);
+  return LULESH_OK;
+}
+
+int lulesh_autotune(lulesh_domain* d, int32_t cycles, lulesh_tuning* chosen) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  CK(cudaSetDevice(d->params.device));
+  cudaStream_t s = d->stream;
+  // save the fields the tuning cycles change, then restore them and the scalars
+  DevDomain& dd = d->dd;
+  double* node_f[6] = {dd.x, dd.y, dd.z, dd.xd, dd.yd, dd.zd};
+  double* elem_f[5] = {dd.e, dd.p, dd.q, dd.v, dd.ss};
+  const size_t nb = (size_t)d->N * sizeof(double), eb = (size_t)d->E * sizeof(double);
+  char* save = nullptr;
+  CK(cudaMalloc(&save, 6 * nb + 5 * eb));
+  auto copy_all = [&](bool to_save) -> cudaError_t {
+    char* p = save;
+    cudaError_t e = cudaSuccess;
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k, p += nb)
+      e = cudaMemcpyAsync(to_save ? (void*)p : (void*)node_f[k], to_save ? (const void*)node_f[k] : (const void*)p,
+                          nb, cudaMemcpyDeviceToDevice, s);
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k, p += eb)
+      e = cudaMemcpyAsync(to_save ? (void*)p : (void*)elem_f[k], to_save ? (const void*)elem_f[k] : (const void*)p,
+                          eb, cudaMemcpyDeviceToDevice, s);
+    return e;
+  };
+  double sc_saved[LULESH_S_COUNT];
+  std::memcpy(sc_saved, d->sc, sizeof(sc_saved));
+  cudaError_t err = copy_all(true);
+  if (err == cudaSuccess) {
+    state_to_device_mirror(d);
+    d->hst->first = 0;
+    err = cudaMemcpyAsync(dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s);
+  }
+  if (err == cudaSuccess) err = autotune_blocks(dd, make_params(d), d->params.keep_aux != 0, 1, s, cycles, d->tuning);
+  if (err == cudaSuccess) err = copy_all(false);
+  if (err == cudaSuccess) err = cudaStreamSynchronize(s);
+  cudaFree(save);
+  std::memcpy(d->sc, sc_saved, sizeof(sc_saved));
+  drop_graph(d);
+  CK(err);
+  return chosen ? lulesh_get_tuning(d, chosen) : LULESH_OK;
 }
 
 }  // extern "C"

@@ -75,7 +75,13 @@ struct DevDomain {
   int* regOfSlot;                             // E, region rep count per slot
   // corner forces [8][E]
   double *fcx, *fcy, *fcz;
+  // step state: one entry, or one per instance of an ensemble
   DevState* st;
+  // ensemble only: instance of every element and node, per-instance hgcoef
+  const int* elemInst;
+  const int* nodeInst;
+  const double* instHg;
+  int ninst;
 };
 
 }  // namespace lulesh

@@ -29,12 +29,15 @@ __device__ __forceinline__ bool step_off(const DevState* st) {
 // ---------------------------------------------------------------------------
 // k_force
 // ---------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) {
+template <int MODE, bool ENS>
+__global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
-  if (step_off(d.st)) return;
+  const int inst = ENS ? LDG(&d.elemInst[e]) : 0;
+  DevState* const st = d.st + inst;
+  if (step_off(st)) return;
+  const double hgcoef = ENS ? LDG(&d.instHg[inst]) : prm.hgcoef;
 
   int nd[8];
 #pragma unroll
@@ -60,7 +63,7 @@ __global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) 
     const double cyet = fma(wx[0], wz[2], -(wz[0] * wx[2]));
     const double czet = fma(wy[0], wx[2], -(wx[0] * wy[2]));
     const double det = fma(wx[1], cxet, fma(wy[1], cyet, wz[1] * czet));
-    if (le_zero(det)) atomicOr(&d.st->status, ST_EARLY);
+    if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
   }
 
   // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
@@ -143,13 +146,13 @@ __global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) 
   // calcHourglassControlForElems (src/domain.jl:1696-1736): determ = volo*v.
   const double v = LDG(&d.v[e]);
   const double determ = LDG(&d.volo[e]) * v;
-  if (le_zero(v)) atomicOr(&d.st->status, ST_HOURGLASS);
+  if (le_zero(v)) atomicOr(&st->status, ST_HOURGLASS);
 
   // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
   const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
 
   double fx[8], fy[8], fz[8];
-  if (prm.hgcoef > 0.0) {
+  if (hgcoef > 0.0) {
     // hourgam (src/domain.jl:1527-1549) with volinv/12 folded into the modes
     const double vi12 = 1.0 / (12.0 * determ);
 #pragma unroll
@@ -162,7 +165,7 @@ __global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) 
         hg[n][m] = fma(-dvz[n], hmz[m], fma(-dvy[n], hmy[m], fma(-dvx[n], hmx[m], gamma_nm(n, m))));
 
     // coefficient = -hgcoef*0.01*ss*mass/cbrt(determ) (src/domain.jl:1605)
-    const double coef = ((-prm.hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * rcbrt(determ);
+    const double coef = ((-hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * rcbrt(determ);
 
     // calcElemFBHourglassForce (src/domain.jl:1258-1460), one velocity
     // component at a time to bound register use.
@@ -203,12 +206,13 @@ __global__ void __launch_bounds__(kForceBlock) k_force(DevDomain d, Params prm) 
 // ---------------------------------------------------------------------------
 // k_node
 // ---------------------------------------------------------------------------
-template <bool AUX>
-__global__ void __launch_bounds__(kNodeBlock) k_node(DevDomain d, Params prm) {
+template <bool AUX, bool ENS>
+__global__ void __launch_bounds__(kMaxNodeBlock) k_node(DevDomain d, Params prm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.N) return;
-  if (step_off(d.st)) return;
-  const double dt = d.st->deltatime;
+  const DevState* st = d.st + (ENS ? LDG(&d.nodeInst[i]) : 0);
+  if (step_off(st)) return;
+  const double dt = st->deltatime;
   const int s = LDG(&d.nodeElemStart[i]), t = LDG(&d.nodeElemStart[i + 1]);
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (s < t) {
@@ -244,13 +248,14 @@ __global__ void __launch_bounds__(kNodeBlock) k_node(DevDomain d, Params prm) {
 // ---------------------------------------------------------------------------
 // k_kinematics
 // ---------------------------------------------------------------------------
-template <bool AUX>
-__global__ void __launch_bounds__(kKinBlock) k_kinematics(DevDomain d, Params prm) {
+template <bool AUX, bool ENS>
+__global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
-  if (step_off(d.st)) return;
-  const double dt = d.st->deltatime;
+  DevState* const st = d.st + (ENS ? LDG(&d.elemInst[e]) : 0);
+  if (step_off(st)) return;
+  const double dt = st->deltatime;
 
   int nd[8];
 #pragma unroll
@@ -301,7 +306,7 @@ __global__ void __launch_bounds__(kKinBlock) k_kinematics(DevDomain d, Params pr
     face(d43, d70, -1.0, 1.0);   // 4,1,5,8
   }
   const double vnew = volume * LDG(&d.inv_volo[e]);
-  if (le_zero(vnew)) atomicOr(&d.st->status, ST_KINEMATICS);
+  if (le_zero(vnew)) atomicOr(&st->status, ST_KINEMATICS);
   d.vnew[e] = vnew;
   d.delv[e] = vnew - LDG(&d.v[e]);
   d.arealg[e] = (4.0 * volume) * rsqrt(charLength);
@@ -450,13 +455,40 @@ __device__ __forceinline__ void block_min2(unsigned long long a, unsigned long l
   }
 }
 
-template <int MODE, bool AUX>
-__global__ void __launch_bounds__(kMatBlock) k_material(DevDomain d, Params prm) {
+// Per-instance minima of an ensemble: a warp whose elements all belong to one
+// instance reduces first; a warp straddling two instances (or the ragged
+// tail) falls back to one atomic per thread. Every lane must call this.
+__device__ __forceinline__ void warp_min2_by_instance(unsigned long long a, unsigned long long b, int inst,
+                                                      DevState* st) {
+  const unsigned full = 0xffffffffu;
+  const int inst0 = __shfl_sync(full, inst, 0);
+  if (__all_sync(full, inst == inst0)) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long ta = __shfl_xor_sync(full, a, o);
+      const unsigned long long tb = __shfl_xor_sync(full, b, o);
+      a = ta < a ? ta : a;
+      b = tb < b ? tb : b;
+    }
+    if ((threadIdx.x & 31) == 0) {
+      if (a != kInfBits) atomicMin(&st[inst0].acc_courant, a);
+      if (b != kInfBits) atomicMin(&st[inst0].acc_hydro, b);
+    }
+  } else {
+    if (a != kInfBits) atomicMin(&st[inst].acc_courant, a);
+    if (b != kInfBits) atomicMin(&st[inst].acc_hydro, b);
+  }
+}
+
+template <int MODE, bool AUX, bool ENS>
+__global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params prm) {
   const int E = d.E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   // every thread of the block takes part in the dt reduction
   unsigned long long courant = kInfBits, hydro = kInfBits;
-  const bool live = (i < E) && !step_off(d.st);
+  const int inst = (ENS && i < E) ? LDG(&d.elemInst[i]) : 0;
+  DevState* const st = d.st + inst;
+  const bool live = (i < E) && !step_off(st);
   if (live) {
     unsigned int err = 0u;
     // ---- calcMonotonicQRegionForElems, src/domain.jl:2322-2513 ----
@@ -590,16 +622,16 @@ __global__ void __launch_bounds__(kMatBlock) k_material(DevDomain d, Params prm)
       courant = (unsigned long long)__double_as_longlong(dtc);
       hydro = (unsigned long long)__double_as_longlong(dth);
     }
-    if (err) atomicOr(&d.st->status, err);
+    if (err) atomicOr(&st->status, err);
   }
-  block_min2(courant, hydro, &d.st->acc_courant, &d.st->acc_hydro);
+  if (ENS) warp_min2_by_instance(courant, hydro, inst, d.st);
+  else block_min2(courant, hydro, &d.st->acc_courant, &d.st->acc_hydro);
 }
 
 // ---------------------------------------------------------------------------
-// k_time_increment (device run loop)
+// k_time_increment (device run loop): one thread per problem
 // ---------------------------------------------------------------------------
-__global__ void k_time_increment(DevState* st, Params prm, long long num_iters) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ void advance_time(DevState* st, const Params& prm, long long num_iters) {
   if (st->done) return;
   if (st->status) { st->done = 1; return; }
   // fold the previous step's minima (src/domain.jl:3012-3014, 3050-3052)
@@ -618,45 +650,65 @@ __global__ void k_time_increment(DevState* st, Params prm, long long num_iters) 
   st->cycle = cycle;
 }
 
+__global__ void k_time_increment(DevState* st, int n, Params prm, long long num_iters) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) advance_time(st + k, prm, num_iters);
+}
+
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_force(const DevDomain& d, const Params& prm, cudaStream_t s) {
-  const int grid = (d.E + kForceBlock - 1) / kForceBlock;
+// An ensemble (d.elemInst set) runs the ENS instantiations, which read each
+// element's or node's instance; the plain path runs ENS = false.
+void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaStream_t s) {
+  const int bs = t.force;
+  const int grid = (d.E + bs - 1) / bs;
+  const bool ens = d.elemInst != nullptr;
+#define LULESH_FORCE(M) \
+  (ens ? k_force<M, true><<<grid, bs, 0, s>>>(d, prm) : k_force<M, false><<<grid, bs, 0, s>>>(d, prm))
   switch (d.mode & 3) {
-    case 0: k_force<0><<<grid, kForceBlock, 0, s>>>(d, prm); break;
-    case 1: k_force<1><<<grid, kForceBlock, 0, s>>>(d, prm); break;
-    case 2: k_force<2><<<grid, kForceBlock, 0, s>>>(d, prm); break;
-    default: k_force<3><<<grid, kForceBlock, 0, s>>>(d, prm); break;
+    case 0: LULESH_FORCE(0); break;
+    case 1: LULESH_FORCE(1); break;
+    case 2: LULESH_FORCE(2); break;
+    default: LULESH_FORCE(3); break;
   }
+#undef LULESH_FORCE
 }
 
-void launch_node(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
-  const int grid = (d.N + kNodeBlock - 1) / kNodeBlock;
-  if (aux) k_node<true><<<grid, kNodeBlock, 0, s>>>(d, prm);
-  else k_node<false><<<grid, kNodeBlock, 0, s>>>(d, prm);
+void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
+  const int bs = t.node;
+  const int grid = (d.N + bs - 1) / bs;
+  if (d.nodeInst) k_node<false, true><<<grid, bs, 0, s>>>(d, prm);
+  else if (aux) k_node<true, false><<<grid, bs, 0, s>>>(d, prm);
+  else k_node<false, false><<<grid, bs, 0, s>>>(d, prm);
 }
 
-void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
-  const int grid = (d.E + kKinBlock - 1) / kKinBlock;
-  if (aux) k_kinematics<true><<<grid, kKinBlock, 0, s>>>(d, prm);
-  else k_kinematics<false><<<grid, kKinBlock, 0, s>>>(d, prm);
+void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
+  const int bs = t.kin;
+  const int grid = (d.E + bs - 1) / bs;
+  if (d.elemInst) k_kinematics<false, true><<<grid, bs, 0, s>>>(d, prm);
+  else if (aux) k_kinematics<true, false><<<grid, bs, 0, s>>>(d, prm);
+  else k_kinematics<false, false><<<grid, bs, 0, s>>>(d, prm);
 }
 
-void launch_material(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s) {
-  const int grid = (d.E + kMatBlock - 1) / kMatBlock;
+void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
+  const int bs = t.mat;
+  const int grid = (d.E + bs - 1) / bs;
   const bool fix = (d.mode & 4) != 0;
-  if (fix) {
-    if (aux) k_material<4, true><<<grid, kMatBlock, 0, s>>>(d, prm);
-    else k_material<4, false><<<grid, kMatBlock, 0, s>>>(d, prm);
+  if (d.elemInst) {
+    if (fix) k_material<4, false, true><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<0, false, true><<<grid, bs, 0, s>>>(d, prm);
+  } else if (fix) {
+    if (aux) k_material<4, true, false><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<4, false, false><<<grid, bs, 0, s>>>(d, prm);
   } else {
-    if (aux) k_material<0, true><<<grid, kMatBlock, 0, s>>>(d, prm);
-    else k_material<0, false><<<grid, kMatBlock, 0, s>>>(d, prm);
+    if (aux) k_material<0, true, false><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<0, false, false><<<grid, bs, 0, s>>>(d, prm);
   }
 }
 
-void launch_time_increment(DevState* st, const Params& prm, long long num_iters, cudaStream_t s) {
-  k_time_increment<<<1, 32, 0, s>>>(st, prm, num_iters);
+void launch_time_increment(DevState* st, int n, const Params& prm, long long num_iters, cudaStream_t s) {
+  k_time_increment<<<(n + 127) / 128, 128, 0, s>>>(st, n, prm, num_iters);
 }
 
 }  // namespace lulesh

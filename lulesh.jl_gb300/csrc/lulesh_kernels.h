@@ -7,15 +7,30 @@
 
 namespace lulesh {
 
-constexpr int kForceBlock = 128;
-constexpr int kNodeBlock = 256;
-constexpr int kKinBlock = 128;
-constexpr int kMatBlock = 128;
+// Element kernels are compiled for blocks of up to kMaxElemBlock threads and
+// the node kernel for up to kMaxNodeBlock (the register budget is the same
+// 255 per thread either way), so the block size is a launch-time choice.
+constexpr int kMaxElemBlock = 256;
+constexpr int kMaxNodeBlock = 512;
 
-void launch_force(const DevDomain& d, const Params& prm, cudaStream_t s);
-void launch_node(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s);
-void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s);
-void launch_material(const DevDomain& d, const Params& prm, bool aux, cudaStream_t s);
-void launch_time_increment(DevState* st, const Params& prm, long long num_iters, cudaStream_t s);
+// Launch configuration chosen by the autotuner (defaults are the block sizes
+// that measured best for the 150^3 problem).
+struct Tuning {
+  int force = 128;
+  int node = 256;
+  int kin = 128;
+  int mat = 128;
+};
+
+void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaStream_t s);
+void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
+void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
+void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
+void launch_time_increment(DevState* st, int n, const Params& prm, long long num_iters, cudaStream_t s);
+
+// Picks block sizes for the four step kernels by timing them on the live
+// problem (lulesh_tune.cu); the state advances, so callers save and restore it.
+cudaError_t autotune_blocks(const DevDomain& d, const Params& prm, bool aux, int ninst, cudaStream_t s,
+                            int cycles, Tuning& t);
 
 }  // namespace lulesh

@@ -108,7 +108,7 @@ void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed) {
   m.regElemSize = size;
 }
 
-void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t seed) {
+void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t seed, double einit) {
   const int64_t en = nx + 1;
   m.nx = nx;
   m.E = (int64_t)nx * nx * nx;
@@ -201,7 +201,7 @@ void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t see
 
   // energy deposit and initial dt (src/domain.jl:738-749)
   const double scale = (double)nx / 45.0;
-  m.einit = 3.948746e+7 * scale * scale * scale;
+  m.einit = einit > 0.0 ? einit : 3.948746e+7 * scale * scale * scale;
   m.deltatime = (0.5 * std::cbrt(m.volo[0])) / std::sqrt(2.0 * m.einit);
 
   // element neighbours (setupElementConnectivities, src/domain.jl:793-820),

@@ -21,8 +21,10 @@ struct HostMesh {
   double einit = 0.0, deltatime = 0.0;
 };
 
-// Builds the nx^3 single-rank Sedov mesh exactly as Domain(prob) does.
-void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t seed);
+// Builds the nx^3 single-rank Sedov mesh exactly as Domain(prob) does. A
+// positive einit replaces the energy deposited in the origin element (and
+// the initial dt computed from it); 0 keeps 3.948746e7*(nx/45)^3.
+void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t seed, double einit = 0.0);
 
 // createRegionIndexSets! (results-neutral region layout).
 void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed);

@@ -91,6 +91,22 @@ class _Scalars(ctypes.Structure):
                 ("cycle", ctypes.c_int64), ("status", ctypes.c_int32), ("site", ctypes.c_int32)]
 
 
+class Instance(ctypes.Structure):
+    """lulesh_instance: one Sedov problem of an ensemble."""
+    _fields_ = [("nx", ctypes.c_int32), ("nr", ctypes.c_int32), ("balance", ctypes.c_int32),
+                ("cost", ctypes.c_int32), ("einit", ctypes.c_double), ("hgcoef", ctypes.c_double),
+                ("region_seed", ctypes.c_uint64)]
+
+
+class Tuning(ctypes.Structure):
+    """lulesh_tuning: threads per block of the four step kernels."""
+    _fields_ = [("force_block", ctypes.c_int32), ("node_block", ctypes.c_int32),
+                ("kin_block", ctypes.c_int32), ("mat_block", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _LIB = None
 
 
@@ -132,6 +148,23 @@ def load_library():
         "lulesh_kernel_times": (ctypes.c_int, [P, ctypes.POINTER(dbl), i32, ctypes.POINTER(i32)]),
         "lulesh_kernel_name": (ctypes.c_char_p, [i32]),
         "lulesh_status_string": (ctypes.c_char_p, [i32]),
+        "lulesh_measure_fp64_peak": (ctypes.c_int, [i32, ctypes.POINTER(dbl), ctypes.POINTER(dbl)]),
+        "lulesh_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
+        "lulesh_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
+        "lulesh_autotune": (ctypes.c_int, [P, i32, ctypes.POINTER(Tuning)]),
+        "lulesh_ens_sedov_instances": (ctypes.c_int, [ctypes.c_uint64, i32, i32, i32, ctypes.POINTER(Instance)]),
+        "lulesh_ens_create": (ctypes.c_int, [ctypes.POINTER(Instance), i32, i32, i32, ctypes.POINTER(P)]),
+        "lulesh_ens_destroy": (ctypes.c_int, [P]),
+        "lulesh_ens_run": (ctypes.c_int, [P, i64]),
+        "lulesh_ens_reset": (ctypes.c_int, [P]),
+        "lulesh_ens_sizes": (ctypes.c_int, [P, ctypes.POINTER(i32), ctypes.POINTER(i64), ctypes.POINTER(i64)]),
+        "lulesh_ens_get_scalars": (ctypes.c_int, [P, i32, ctypes.POINTER(_Scalars)]),
+        "lulesh_ens_field_length": (ctypes.c_int, [P, i32, i32, ctypes.POINTER(i64)]),
+        "lulesh_ens_download_field": (ctypes.c_int, [P, i32, i32, P, i64]),
+        "lulesh_ens_get_stream": (ctypes.c_int, [P, ctypes.POINTER(P)]),
+        "lulesh_ens_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
+        "lulesh_ens_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
+        "lulesh_ens_autotune": (ctypes.c_int, [P, i32, ctypes.POINTER(Tuning)]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -249,6 +282,24 @@ class Domain:
         _check(self._L.lulesh_kernel_times(self._h, ms, 16, ctypes.byref(n)), "kernel times")
         return {self._L.lulesh_kernel_name(i).decode(): ms[i] for i in range(n.value)}
 
+    def tuning(self):
+        t = Tuning()
+        _check(self._L.lulesh_get_tuning(self._h, ctypes.byref(t)), "tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **blocks):
+        t = Tuning()
+        self._L.lulesh_get_tuning(self._h, ctypes.byref(t))
+        for k, v in blocks.items():
+            setattr(t, k, int(v))
+        _check(self._L.lulesh_set_tuning(self._h, ctypes.byref(t)), "set tuning")
+
+    def autotune(self, cycles=3):
+        """Times each kernel's candidate block sizes on this problem; the state is kept."""
+        t = Tuning()
+        _check(self._L.lulesh_autotune(self._h, int(cycles), ctypes.byref(t)), "autotune")
+        return t.as_dict()
+
     def __getattr__(self, name):
         if name in FIELDS:
             return self.field(name)
@@ -326,3 +377,98 @@ def verifyAndWriteFinalOutput(elapsed_time, domain, nx, numRanks=1, file=None):
     print(f"FOM                  = {1000.0 / grind2:.8f} (z/s)\n", file=f)
     return {"origin_energy": e0, "MaxAbsDiff": maxabs, "TotalAbsDiff": total, "MaxRelDiff": maxrel,
             "cycle": cyc, "grind_us": grind2, "fom_kzs": 1000.0 / grind2}
+
+
+def sedov_instances(seed=0xC4, n=256, nx_min=16, nx_max=64):
+    """The seeded instance draw of lulesh_ens_sedov_instances (list of dicts)."""
+    L = load_library()
+    arr = (Instance * n)()
+    _check(L.lulesh_ens_sedov_instances(int(seed), int(n), int(nx_min), int(nx_max), arr), "instances")
+    return [{k: getattr(a, k) for k, _ in Instance._fields_} for a in arr]
+
+
+class Ensemble:
+    """Many independent Sedov problems advanced together on one GPU.
+
+    `instances` is a list of dicts with the lulesh_instance keys (nx, nr,
+    balance, cost, einit, hgcoef, region_seed); missing keys take the
+    reference's defaults. `run(num_iters)` runs examples/benchmark.jl's loop
+    for every instance at once, device-resident.
+    """
+
+    def __init__(self, instances, mode=MODE_FAITHFUL, device=0):
+        L = load_library()
+        n = len(instances)
+        arr = (Instance * n)()
+        for a, spec in zip(arr, instances):
+            a.nx = int(spec["nx"])
+            a.nr = int(spec.get("nr", 11))
+            a.balance = int(spec.get("balance", 1))
+            a.cost = int(spec.get("cost", 1))
+            a.einit = float(spec.get("einit", 0.0))
+            a.hgcoef = float(spec.get("hgcoef", 3.0))
+            a.region_seed = int(spec.get("region_seed", 0))
+        h = ctypes.c_void_p()
+        _check(L.lulesh_ens_create(arr, n, int(mode), int(device), ctypes.byref(h)), "ensemble create")
+        self._L, self._h, self.n = L, h, n
+        self.instances = [dict(s) for s in instances]
+        c = ctypes.c_int32()
+        te, tn = ctypes.c_int64(), ctypes.c_int64()
+        L.lulesh_ens_sizes(h, ctypes.byref(c), ctypes.byref(te), ctypes.byref(tn))
+        self.total_elem, self.total_node = te.value, tn.value
+
+    def close(self):
+        if self._h:
+            self._L.lulesh_ens_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, num_iters):
+        rc = self._L.lulesh_ens_run(self._h, int(num_iters))
+        if rc:
+            raise LuleshError(f"ensemble run: {self._L.lulesh_status_string(rc).decode()}", rc)
+
+    def reset(self):
+        _check(self._L.lulesh_ens_reset(self._h), "ensemble reset")
+
+    def scalars(self, i):
+        s = _Scalars()
+        _check(self._L.lulesh_ens_get_scalars(self._h, int(i), ctypes.byref(s)), "ensemble scalars")
+        return {k: getattr(s, k) for k, _ in _Scalars._fields_}
+
+    def field(self, i, name):
+        fid, dt = FIELDS[name]
+        n = ctypes.c_int64()
+        _check(self._L.lulesh_ens_field_length(self._h, int(i), fid, ctypes.byref(n)), f"length of {name}")
+        out = np.empty(n.value, dtype=dt)
+        _check(self._L.lulesh_ens_download_field(self._h, int(i), fid, out.ctypes.data_as(ctypes.c_void_p),
+                                                 n.value), f"download {name}")
+        return out
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _check(self._L.lulesh_ens_get_stream(self._h, ctypes.byref(s)), "stream")
+        return s.value
+
+    def tuning(self):
+        t = Tuning()
+        _check(self._L.lulesh_ens_get_tuning(self._h, ctypes.byref(t)), "tuning")
+        return t.as_dict()
+
+    def set_tuning(self, **blocks):
+        t = Tuning()
+        self._L.lulesh_ens_get_tuning(self._h, ctypes.byref(t))
+        for k, v in blocks.items():
+            setattr(t, k, int(v))
+        _check(self._L.lulesh_ens_set_tuning(self._h, ctypes.byref(t)), "set tuning")
+
+    def autotune(self, cycles=3):
+        """Picks block sizes on this ensemble, then returns it to its initial state."""
+        t = Tuning()
+        _check(self._L.lulesh_ens_autotune(self._h, int(cycles), ctypes.byref(t)), "autotune")
+        return t.as_dict()

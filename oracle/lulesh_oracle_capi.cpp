@@ -125,6 +125,14 @@ int ora_set_scalar(void* h, const char* name, double v) {
   return 0;
 }
 
+// Replaces the deposited origin energy and the initial dt computed from it,
+// as src/domain.jl:738-749 does for the default energy.
+void ora_set_einit(void* h, double einit) {
+  D* d = static_cast<D*>(h);
+  d->e[0] = einit;
+  d->deltatime = (0.5 * std::cbrt(d->volo[0])) / std::sqrt(2.0 * einit);
+}
+
 int ora_time_increment(void* h) { timeIncrement(*static_cast<D*>(h)); return 0; }
 int ora_lagrange_leapfrog(void* h) { return lagrangeLeapFrog(*static_cast<D*>(h)); }
 int ora_lagrange_nodal(void* h) { return lagrangeNodal(*static_cast<D*>(h)); }

@@ -63,6 +63,8 @@ def load(openmp=True):
     L.ora_get_scalar.argtypes = [P, ctypes.c_char_p, ctypes.POINTER(ctypes.c_double)]
     L.ora_set_scalar.argtypes = [P, ctypes.c_char_p, ctypes.c_double]
     L.ora_symmetry.argtypes = [P, ctypes.POINTER(ctypes.c_double)]
+    L.ora_set_einit.argtypes = [P, ctypes.c_double]
+    L.ora_set_einit.restype = None
     L.ora_max_threads.restype = ctypes.c_int
     L.ora_set_threads.argtypes = [ctypes.c_int]
     _libs[key] = L
@@ -131,6 +133,10 @@ class OracleDomain:
             return
         if self.L.ora_set_scalar(self.h, name.encode(), float(value)) != 0:
             raise KeyError(name)
+
+    def set_einit(self, einit):
+        """Deposit `einit` in the origin element (and recompute the initial dt)."""
+        self.L.ora_set_einit(self.h, float(einit))
 
     def time_increment(self):
         self.L.ora_time_increment(self.h)

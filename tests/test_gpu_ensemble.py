@@ -1,0 +1,112 @@
+"""The batched ensemble: every instance against the oracle and against the
+single-problem GPU path, plus reset, autotuning and the seeded draw."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import field_floor, rel_err
+
+STATE = ["e", "p", "q", "v", "ss", "x", "y", "z", "xd", "yd", "zd"]
+
+# Uneven sizes, energies and hourglass coefficients; nr = 1 and 11.
+SMALL = [
+    {"nx": 5, "nr": 11, "hgcoef": 3.0, "einit": 0.0},
+    {"nx": 9, "nr": 1, "hgcoef": 2.2, "einit": 1.7 * 3.948746e7 * (9 / 45) ** 3},
+    {"nx": 3, "nr": 11, "hgcoef": 3.9, "einit": 0.6 * 3.948746e7 * (3 / 45) ** 3},
+    {"nx": 12, "nr": 11, "hgcoef": 2.6, "einit": 0.0},
+    {"nx": 7, "nr": 1, "hgcoef": 0.0, "einit": 0.0},
+]
+
+
+def test_instance_draw_is_seeded_and_in_range(gpu_lib):
+    a = gpu_lib.sedov_instances(0xC4, 256, 16, 64)
+    b = gpu_lib.sedov_instances(0xC4, 256, 16, 64)
+    assert a == b
+    assert a != gpu_lib.sedov_instances(0xC5, 256, 16, 64)
+    for s in a:
+        assert 16 <= s["nx"] <= 64
+        assert 2.0 <= s["hgcoef"] <= 4.0
+        assert s["nr"] in (1, 11)
+        f = s["einit"] / (3.948746e7 * (s["nx"] / 45.0) ** 3)
+        assert 0.5 <= f <= 2.0
+    assert 60 < sum(s["nr"] == 11 for s in a) < 196
+    assert len({s["nx"] for s in a}) > 30
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("mode", [0, 7])
+def test_ensemble_matches_oracle(gpu_lib, oracle_mod, mode):
+    ens = gpu_lib.Ensemble(SMALL, mode=mode)
+    iters = 60
+    ens.run(iters)
+    for i, spec in enumerate(SMALL):
+        o = oracle_mod.OracleDomain(spec["nx"], nr=spec["nr"], mode=mode)
+        o.set("hgcoef", spec["hgcoef"])
+        if spec["einit"] > 0:
+            o.set_einit(spec["einit"])
+        assert o.run(iters) == 0
+        s = ens.scalars(i)
+        assert s["cycle"] == o.get("cycle") == iters, i
+        assert s["time"] == pytest.approx(o.get("time"), rel=1e-12), i
+        for f in STATE:
+            a, b = ens.field(i, f), o.field(f)
+            assert rel_err(a, b, field_floor(f, b)) <= 1e-8, (i, f)
+
+
+@pytest.mark.gpu
+def test_ensemble_equals_single_problem_path(gpu_lib):
+    """Instance i of the ensemble and a single-problem handle with the same
+    parameters step through bit-identical states."""
+    ens = gpu_lib.Ensemble(SMALL)
+    init = [ens.scalars(i) for i in range(len(SMALL))]
+    ens.run(40)
+    for i, spec in enumerate(SMALL):
+        g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=spec["nx"], nr=spec["nr"]))
+        g.hgcoef = spec["hgcoef"]
+        if spec["einit"] > 0:
+            e = g.field("e")
+            e[0] = spec["einit"]
+            g.set_field("e", e)
+        g.deltatime = init[i]["deltatime"]
+        gpu_lib.run(g, 40)
+        for f in STATE:
+            assert np.array_equal(ens.field(i, f), g.field(f)), (i, f)
+        assert ens.scalars(i)["time"] == g.time
+
+
+@pytest.mark.gpu
+def test_reset_and_tuning_do_not_change_results(gpu_lib):
+    ens = gpu_lib.Ensemble(SMALL)
+    ens.run(25)
+    first = [ens.field(i, "e") for i in range(len(SMALL))]
+    chosen = ens.autotune(cycles=2)
+    assert chosen["force_block"] in (64, 128, 256) and chosen["node_block"] in (128, 256, 512)
+    assert all(ens.scalars(i)["cycle"] == 0 for i in range(len(SMALL)))  # back to the start
+    ens.set_tuning(force_block=64, kin_block=256, mat_block=64, node_block=512)
+    ens.run(25)
+    for i in range(len(SMALL)):
+        assert np.array_equal(ens.field(i, "e"), first[i]), i
+    ens.reset()
+    assert ens.scalars(0)["cycle"] == 0 and ens.scalars(0)["time"] == 0.0
+
+
+@pytest.mark.gpu
+def test_single_problem_autotune_keeps_state(gpu_lib):
+    g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=20))
+    gpu_lib.run(g, 10)
+    before = {f: g.field(f) for f in ("e", "xd")}
+    t0, c0 = g.time, g.cycle
+    g.autotune(cycles=2)
+    assert g.time == t0 and g.cycle == c0
+    for f, v in before.items():
+        assert np.array_equal(g.field(f), v), f
+
+
+@pytest.mark.gpu
+def test_ensemble_stops_each_instance_at_stoptime(gpu_lib):
+    ens = gpu_lib.Ensemble([{"nx": 4}, {"nx": 6, "hgcoef": 2.5}], mode=7)
+    ens.run(10**9)
+    for i in range(2):
+        s = ens.scalars(i)
+        assert s["time"] == 1e-2 and s["status"] == 0, (i, s)
