@@ -194,6 +194,52 @@ def run_reference(args):
     return 0
 
 
+def ensemble_leg(L, torch, dev, n, cycles):
+    """Config C4: n seeded Sedov instances (nx in [16, 64], einit x U-log[0.5, 2],
+    hgcoef in [2, 4], nr 1 or 11) advanced `cycles` cycles as one device-resident
+    ensemble, against looping the single-problem GPU path over the same instances."""
+    inst = L.sedov_instances(0xC4, n, 16, 64)
+    ens = L.Ensemble(inst, mode=0, device=dev)
+    tuning = ens.autotune(cycles=2)  # returns the ensemble to its initial state
+    init_dt = [ens.scalars(i)["deltatime"] for i in range(n)]
+    stream = torch.cuda.ExternalStream(ens.stream(), device=dev)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize(dev)
+    a.record(stream)
+    ens.run(cycles)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    ens_s = a.elapsed_time(b) * 1e-3
+    done = sum(ens.scalars(i)["cycle"] == cycles for i in range(n))
+    total_elems = ens.total_elem
+    ens.close()
+    # the same instances, one single-problem handle after another (setup untimed)
+    loop_s = 0.0
+    for i, spec in enumerate(inst):
+        g = L.Domain(L.LuleshProblem(nx=spec["nx"], nr=spec["nr"], device=dev))
+        g.hgcoef = spec["hgcoef"]
+        e = g.field("e")
+        e[0] = spec["einit"]
+        g.set_field("e", e)
+        g.deltatime = init_dt[i]
+        s = torch.cuda.ExternalStream(g.stream(), device=dev)
+        torch.cuda.synchronize(dev)
+        a.record(s)
+        L.run(g, cycles)
+        b.record(s)
+        torch.cuda.synchronize(dev)
+        loop_s += a.elapsed_time(b) * 1e-3
+        g.close()
+    return {"config": f"{n} Sedov instances, nx uniform in [16, 64] (seed 0xC4), {cycles} cycles each, FP64",
+            "instances": n, "cycles": cycles, "total_elements": total_elems,
+            "instances_completed": done,
+            "problems_per_s": n / ens_s, "seconds": ens_s,
+            "looped_plain_problems_per_s": n / loop_s, "looped_plain_seconds": loop_s,
+            "speedup_vs_looped_plain": loop_s / ens_s,
+            "zones_cycles_per_s": total_elems * cycles / ens_s,
+            "tuning": tuning}
+
+
 def run_ours(args):
     world, rank, local = _dist()
     import torch
@@ -212,8 +258,10 @@ def run_ours(args):
     fma_s, add_s = ctypes.c_double(), ctypes.c_double()
     L.load_library().lulesh_measure_fp64_peak(dev, ctypes.byref(fma_s), ctypes.byref(add_s))
 
-    # warm-up, then the timed region: exactly K cycles, device-resident, with
-    # per-kernel CUDA events on the library's stream
+    # block sizes picked on this problem (the state is restored), then warm-up,
+    # then the timed region: exactly K cycles, device-resident, with per-kernel
+    # CUDA events on the library's stream
+    tuning = g.autotune(cycles=2) if not args.no_tune else g.tuning()
     g.enable_timing(True)
     L.run(g, g.cycle + args.warmup)
     g.kernel_times()
@@ -284,6 +332,11 @@ def run_ours(args):
         fp64.update({"kernel": "k_force", "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
                      "fp64_inst_per_launch": prof["fp64_inst_per_launch"]})
 
+    ensemble = None
+    if not args.no_ensemble:
+        g.close()
+        ensemble = ensemble_leg(L, torch, dev, args.ens_instances, args.ens_cycles)
+
     cpu = None
     if world == 1 and not args.no_cpu:
         rate, used, n, dt = cpu_oracle_rate(args.nx, args.cpu_seconds)
@@ -304,7 +357,7 @@ def run_ours(args):
             "kernel_ms_per_cycle": {k: v / cycles for k, v in ktimes.items()},
             "dominant_kernel": dominant,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
-            "clocks": clocks.summary()}
+            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble}
     print(json.dumps(line), flush=True)
     g.close()
     return 0
@@ -320,6 +373,10 @@ def main():
     ap.add_argument("--mode", type=int, default=0)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-tune", action="store_true", help="keep the default block sizes")
+    ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
+    ap.add_argument("--ens-instances", type=int, default=256)
+    ap.add_argument("--ens-cycles", type=int, default=300)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

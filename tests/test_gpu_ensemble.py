@@ -47,7 +47,9 @@ def test_ensemble_matches_oracle(gpu_lib, oracle_mod, mode):
             o.set_einit(spec["einit"])
         assert o.run(iters) == 0
         s = ens.scalars(i)
-        assert s["cycle"] == o.get("cycle") == iters, i
+        # small instances reach stoptime before iters cycles (3^3: 16 cycles)
+        assert s["cycle"] == o.get("cycle"), i
+        assert s["cycle"] == iters or o.get("time") >= o.get("stoptime"), i
         assert s["time"] == pytest.approx(o.get("time"), rel=1e-12), i
         for f in STATE:
             a, b = ens.field(i, f), o.field(f)
