@@ -281,6 +281,48 @@ typedef struct {
 
 int lulesh_calc_force_for_nodes_static(const lulesh_force_args* args, void* stream, int32_t* site);
 
+/* ---- Reverse-mode adjoint of a run -------------------------------------------
+ * The reference differentiates its step with Enzyme (the optional Enzyme
+ * extension of LULESH.jl); this is a hand-written adjoint of the same run.
+ * The objective of the state S after the run is
+ *     L(S) = sum_e w_e e_e + sum_n 0.5 w_n |u_n|^2,
+ * w_e = elemMass_e if the element's centroid in the initial mesh lies
+ * within `radius` of the origin (else 0), w_n = nodalMass_n likewise for the
+ * node's initial position: the total energy within that radius. Callers can
+ * replace it with a linear objective sum_f <seed_f, field_f> over state fields
+ * (lulesh_adj_set_seed). The state fields are x y z xd yd zd (node) and e p q
+ * v ss (element); the gradient w.r.t. the run's initial value of each is
+ * returned (lulesh_adj_get_gradient), with dL/dhgcoef in the result.
+ * Memory: one state per checkpoint plus checkpoint_every cycles of tape
+ * (about 8*(12*E + 5*N) bytes per taped cycle). The derivative is that of the
+ * branches the forward run took (dt minima, clamps, limiter cases). */
+typedef struct lulesh_adjoint lulesh_adjoint;
+
+typedef struct {
+  double loss;          /* L at the end of the run */
+  double grad_hgcoef;   /* dL/dhgcoef */
+  double forward_ms;    /* checkpointed forward sweep, host wall clock */
+  double reverse_ms;    /* objective + recompute + transpose, host wall clock */
+  int64_t cycles;
+  int32_t checkpoints;
+  int32_t status;
+} lulesh_adj_result;
+
+int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_every, lulesh_adjoint** out);
+int lulesh_adj_destroy(lulesh_adjoint* adj);
+/* Linear objective weights for one state field (replaces the energy
+ * objective until lulesh_adj_clear_seeds). */
+int lulesh_adj_set_seed(lulesh_adjoint* adj, int32_t field, const double* weights, int64_t count);
+int lulesh_adj_clear_seeds(lulesh_adjoint* adj);
+/* The objective at the domain's current state. */
+int lulesh_adj_loss(lulesh_adjoint* adj, double* loss);
+/* Runs up to num_cycles cycles (timeIncrement! + lagrangeLeapFrog each; fewer
+ * if time reaches stoptime first) from the domain's current state, leaves the
+ * domain at the final state, and computes the gradient of the objective
+ * w.r.t. the initial state and hgcoef. result->cycles is the number run. */
+int lulesh_adj_gradient(lulesh_adjoint* adj, int64_t num_cycles, lulesh_adj_result* result);
+int lulesh_adj_get_gradient(lulesh_adjoint* adj, int32_t field, double* host, int64_t count);
+
 /* Human-readable text of a status code. */
 const char* lulesh_status_string(int32_t status);
 

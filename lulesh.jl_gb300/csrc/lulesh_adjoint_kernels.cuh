@@ -1,0 +1,879 @@
+// Reverse-mode adjoint kernels of the LagrangeLeapFrog step.
+//
+// Each kernel is the hand-written transpose (vector-Jacobian product) of one
+// forward kernel of lulesh_kernels.cu, in the same formulation (Walsh
+// coefficients, face-diagonal cross products, edge sums). Forward values are
+// recomputed from the cycle's tape (start state, end positions/velocities,
+// accelerations, kinematics outputs); every branch (cut-offs, clamps, limiter
+// cases, the characteristic-length face, velocity snaps) is read from the
+// tape the taping forward kernels wrote, so the derivative is that of the
+// branches actually taken. Node sums are transposed into per-corner buffers
+// and gathered back in nodeElemCornerList order; neighbour reads of the Q
+// limiter are transposed into per-face slots and gathered through an inverse
+// neighbour list: no atomics, so gradients are bitwise reproducible.
+#pragma once
+
+#include "lulesh_device.cuh"
+
+namespace lulesh {
+
+constexpr int kAdjBlock = 128;
+
+struct AdjDev {
+  int E, N;
+  // constants of the problem
+  const int* nodelist;        // [8][E]
+  const int* nodeElemStart;   // N+1
+  const int* cornerList;      // 8E, values c*E + e
+  const unsigned char* nodeBC;
+  const double *inv_nodalMass, *volo, *inv_volo, *elemMass;
+  const unsigned* elemBC;
+  const int *lxim, *lxip, *letam, *letap, *lzetam, *lzetap;
+  const int *nbStart, *nbList;  // inverse neighbour lists (entries slot*E + j)
+  // cycle start state S0 and end positions/velocities S1
+  const double *x0, *y0, *z0, *xd0, *yd0, *zd0, *e0, *p0, *q0, *v0, *ss0;
+  const double *x1, *y1, *z1, *xd1, *yd1, *zd1;
+  // tape of the cycle
+  const double *ax, *ay, *az;                 // accelerations (N)
+  const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
+  const double *dvl[3], *dxl[3];              // delv_{xi,eta,zeta}, delx_{xi,eta,zeta}
+  const unsigned long long* flags;
+  // adjoints of the state (in place: S1 on entry, S0 on exit)
+  double *lx, *ly, *lz, *lxd, *lyd, *lzd;     // N
+  double *le, *lp, *lq, *lss, *lv;            // E
+  // adjoints of intermediate quantities
+  double *lfx, *lfy, *lfz;                    // N
+  double *lvnew, *ldelv, *larealg, *lvdov;    // E
+  double *ldv[3], *ldx[3];                    // E
+  double* lnb;                                // [6][E]: limiter neighbour slots
+  double *cX, *cV;                            // [3][8][E] corner buffers
+  double *part_dt, *part_dtn, *part_hg;       // per-block partial sums (kinematics, node, force)
+};
+
+// Deterministic block sum (fixed tree order); thread 0 writes the block's sum.
+__device__ __forceinline__ void block_sum_to(double v, double* out) {
+  __shared__ double sh[kAdjBlock];
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  for (int s = kAdjBlock / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
+}
+
+// Walsh sign of node n in direction a (xi, eta, zeta) as walsh1 uses it.
+__device__ __forceinline__ double walsh_sign(int a, int n) {
+  if (a == 0) return ((n == 1) | (n == 2) | (n == 5) | (n == 6)) ? 1.0 : -1.0;
+  if (a == 1) return ((n == 2) | (n == 3) | (n == 6) | (n == 7)) ? 1.0 : -1.0;
+  return (n >= 4) ? 1.0 : -1.0;
+}
+
+struct V3 {
+  double x, y, z;
+};
+__device__ __forceinline__ V3 v3(double x, double y, double z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 vcross(const V3& a, const V3& b) {
+  V3 c;
+  cross(a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z);
+  return c;
+}
+__device__ __forceinline__ double vdot(const V3& a, const V3& b) { return fma(a.x, b.x, fma(a.y, b.y, a.z * b.z)); }
+__device__ __forceinline__ void vaxpy(V3& y, double a, const V3& x) {
+  y.x = fma(a, x.x, y.x); y.y = fma(a, x.y, y.y); y.z = fma(a, x.z, y.z);
+}
+__device__ __forceinline__ void vadd(V3& y, const V3& x) { y.x += x.x; y.y += x.y; y.z += x.z; }
+
+// Resolved limiter neighbour: the element whose delv is read (self for a
+// symmetry face or the reference's self-reading xi-plus index), -1 for a free
+// face.
+__device__ __forceinline__ int limiter_index(unsigned mask, unsigned bits, unsigned symm, unsigned freeb,
+                                             unsigned comm, int idx, int self, int E) {
+  const unsigned c = mask & bits;
+  if (c == 0u || c == comm) return (idx >= 0 && idx < E) ? idx : -1;
+  if (c == symm) return self;
+  return -1;
+}
+
+// ---------------------------------------------------------------------------
+// ka_material: transpose of k_material (Q limiter, EOS, volume update,
+// Courant and hydro candidates).
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, int argmin_c, double lam_c,
+                                                          int argmin_h, double lam_h) {
+  const int E = a.E;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= E) return;
+  const unsigned long long fl = a.flags[i];
+  const double ptiny = 1.e-36;
+  const unsigned mask = a.elemBC[i];
+  // neighbour resolution exactly as the forward kernel
+  int im[3], ip[3];
+  im[0] = limiter_index(mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, a.lxim[i], i, E);
+  ip[0] = limiter_index(mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, (MODE & 4) ? a.lxip[i] : a.lxip[i] - 1, i, E);
+  im[1] = limiter_index(mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, a.letam[i], i, E);
+  ip[1] = limiter_index(mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, a.letap[i], i, E);
+  im[2] = limiter_index(mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, a.lzetam[i], i, E);
+  ip[2] = limiter_index(mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, a.lzetap[i], i, E);
+
+  double self[3], mv[3], pv[3], norm[3], phi[3], delx[3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    self[d] = a.dvl[d][i];
+    mv[d] = im[d] >= 0 ? a.dvl[d][im[d]] : 0.0;
+    pv[d] = ip[d] >= 0 ? a.dvl[d][ip[d]] : 0.0;
+    norm[d] = 1.0 / (self[d] + ptiny);
+    const int src = (int)((fl >> (3 * d)) & 7ull);
+    const double dm = mv[d] * norm[d], dp = pv[d] * norm[d];
+    phi[d] = src == PHI_MEAN ? 0.5 * (dm + dp)
+           : src == PHI_M ? dm * prm.monoq_limiter_mult
+           : src == PHI_P ? dp * prm.monoq_limiter_mult
+           : src == PHI_ZERO ? 0.0 : prm.monoq_max_slope;
+    delx[d] = a.dxl[d][i];
+  }
+  const double vdov = a.vdov[i], vnew = a.vnew[i], volo = a.volo[i], mass = a.elemMass[i];
+  const double delvc = a.delv[i], arealg = a.arealg[i];
+  const bool qzero = (fl & TF_QZERO) != 0;
+  double dx[3] = {0.0, 0.0, 0.0}, rho = 0.0, qlin = 0.0, qquad = 0.0, s1sum = 0.0, s2sum = 0.0;
+  if (!qzero) {
+#pragma unroll
+    for (int d = 0; d < 3; ++d) dx[d] = (fl & (TF_DXCLAMP0 << d)) ? 0.0 : self[d] * delx[d];
+    rho = mass / (volo * vnew);
+    s1sum = fma(dx[0], 1.0 - phi[0], fma(dx[1], 1.0 - phi[1], dx[2] * (1.0 - phi[2])));
+    s2sum = fma(dx[0] * dx[0], fma(-phi[0], phi[0], 1.0),
+                fma(dx[1] * dx[1], fma(-phi[1], phi[1], 1.0), (dx[2] * dx[2]) * fma(-phi[2], phi[2], 1.0)));
+    qlin = (-prm.qlc_monoq * rho) * s1sum;
+    qquad = (prm.qqc_monoq * rho) * s2sum;
+  }
+  // EOS forward (values only; branches from the tape)
+  const bool vmin_c = (fl & TF_VNEW_MIN) != 0, vmax_c = (fl & TF_VNEW_MAX) != 0;
+  const double vnewc = vmin_c ? prm.eosvmin : vmax_c ? prm.eosvmax : vnew;
+  const bool vmax_hit = (fl & TF_VMAX_HIT) != 0, half_eq = (fl & TF_HALF_EQ_COMP) != 0;
+  const double p_old = vmax_hit ? 0.0 : a.p0[i], q_old = a.q0[i], e_old = a.e0[i];
+  const double compression = vmax_hit ? 0.0 : 1.0 / vnewc - 1.0;
+  const double vchalf = fma(delvc, -0.5, vnewc);
+  const double chs = vmax_hit ? 0.0 : half_eq ? compression : 1.0 / vchalf - 1.0;
+  const double c1s = 2.0 / 3.0, irho0 = 1.0 / prm.refdens;
+  const double pq = p_old + q_old;
+  const bool e1min = (fl & TF_E1_MIN) != 0;
+  const double e1 = e1min ? prm.emin : fma(-0.5 * delvc, pq, e_old);
+  const double bvc_h = c1s * (chs + 1.0);
+  const bool pH_on = !vmax_hit && !(fl & (TF_PH_CUT | TF_PH_MIN));
+  const double pH = pH_on ? bvc_h * e1 : (fl & TF_PH_MIN) ? prm.pmin : 0.0;
+  const double vhalf = 1.0 / (1.0 + chs);
+  const bool comp = (fl & TF_COMPRESS) != 0;
+  const bool s1t = (fl & TF_S1_TINY) != 0, s2t = (fl & TF_S2_TINY) != 0, sst = (fl & TF_SS_TINY) != 0;
+  double ssc1 = 0.0, s1 = 0.0, qn1 = 0.0;
+  if (comp) {
+    ssc1 = fma(c1s, e1, ((vhalf * vhalf) * bvc_h) * pH) * irho0;
+    s1 = s1t ? 0.333333e-18 : sqrt(ssc1);
+    qn1 = fma(s1, qlin, qquad);
+  }
+  const bool e2fix = (fl & (TF_E2_CUT | TF_E2_MIN)) != 0;
+  const double k2 = fma(3.0, pq, -4.0 * (pH + qn1));
+  const double e2 = (fl & TF_E2_MIN) ? prm.emin : (fl & TF_E2_CUT) ? 0.0 : fma(0.5 * delvc, k2, e1);
+  const double bvc = c1s * (compression + 1.0);
+  const bool pn1_on = !vmax_hit && !(fl & (TF_PN1_CUT | TF_PN1_MIN));
+  const double pn1 = pn1_on ? bvc * e2 : (fl & TF_PN1_MIN) ? prm.pmin : 0.0;
+  const double vv_bvc = (vnewc * vnewc) * bvc;
+  double ssc2 = 0.0, s2 = 0.0, qt = 0.0;
+  if (comp) {
+    ssc2 = fma(c1s, e2, vv_bvc * pn1) * irho0;
+    s2 = s2t ? 0.333333e-18 : sqrt(ssc2);
+    qt = fma(s2, qlin, qquad);
+  }
+  const double k3 = fma(7.0, pq, -8.0 * (pH + qn1)) + (pn1 + qt);
+  const bool e3fix = (fl & (TF_E3_CUT | TF_E3_MIN)) != 0;
+  const double e3 = (fl & TF_E3_MIN) ? prm.emin : (fl & TF_E3_CUT) ? 0.0 : e2 - (k3 * delvc) * (1.0 / 6.0);
+  const bool pn2_on = !vmax_hit && !(fl & (TF_PN2_CUT | TF_PN2_MIN));
+  const double pn2 = pn2_on ? bvc * e3 : (fl & TF_PN2_MIN) ? prm.pmin : 0.0;
+  const double ssc3 = fma(c1s, e3, vv_bvc * pn2) * irho0;
+  const double ss = sst ? 0.333333e-18 : sqrt(ssc3);
+
+  // ---------------- reverse ----------------
+  double Le3 = a.le[i], Lpn2 = a.lp[i], Lq = a.lq[i], Lss = a.lss[i], Lv1 = a.lv[i];
+  double Lvnew = 0.0, Larealg = 0.0, Lvdov = 0.0, Ldelvc = 0.0;
+  // Courant and hydro candidates (only the arg-min element carries a seed)
+  if (i == argmin_c && vdov != 0.0) {
+    const double qqc2 = (64.0 * prm.qqc) * prm.qqc;
+    double dtf = ss * ss;
+    if (vdov < 0.0) dtf = fma(qqc2 * (arealg * arealg), vdov * vdov, dtf);
+    const double rs = rsqrt(dtf);
+    Larealg += lam_c * rs;
+    const double Ldtf = lam_c * arealg * (-0.5) * rs * rs * rs;
+    Lss += 2.0 * ss * Ldtf;
+    if (vdov < 0.0) {
+      Larealg += Ldtf * 2.0 * qqc2 * arealg * vdov * vdov;
+      Lvdov += Ldtf * 2.0 * qqc2 * arealg * arealg * vdov;
+    }
+  }
+  if (i == argmin_h && vdov != 0.0) {
+    const double den = fabs(vdov) + 1.e-20;
+    Lvdov += lam_h * (-prm.dvovmax / (den * den)) * (vdov < 0.0 ? -1.0 : 1.0);
+  }
+  if (!(fl & TF_V_SNAP)) Lvnew += Lv1;
+  double Lqlin = 0.0, Lqquad = 0.0;
+  // final q = ss*qlin + qquad
+  if (comp && !(fl & TF_Q_CUT)) { Lss += Lq * qlin; Lqlin += Lq * ss; Lqquad += Lq; }
+  double Lvv = 0.0, Lbvc = 0.0, Le2 = 0.0, Lpn1 = 0.0, Lpq = 0.0, LpH = 0.0, Lqn1 = 0.0, Lqt = 0.0;
+  // ss = sqrt(ssc3)
+  if (!sst) {
+    const double Lssc = Lss * 0.5 / ss * irho0;
+    Le3 += Lssc * c1s;
+    Lvv += Lssc * pn2;
+    Lpn2 += Lssc * vv_bvc;
+  }
+  if (pn2_on) { Lbvc += Lpn2 * e3; Le3 += Lpn2 * bvc; }
+  if (!e3fix) {
+    Le2 += Le3;
+    const double Lk = -Le3 * delvc * (1.0 / 6.0);
+    Ldelvc += -Le3 * k3 * (1.0 / 6.0);
+    Lpq += 7.0 * Lk; LpH += -8.0 * Lk; Lqn1 += -8.0 * Lk; Lpn1 += Lk; Lqt += Lk;
+  }
+  if (comp) {
+    Lqlin += Lqt * s2; Lqquad += Lqt;
+    if (!s2t) {
+      const double Lssc = Lqt * qlin * 0.5 / s2 * irho0;
+      Le2 += Lssc * c1s;
+      Lvv += Lssc * pn1;
+      Lpn1 += Lssc * vv_bvc;
+    }
+  }
+  double Lvnewc = 2.0 * vnewc * bvc * Lvv;
+  Lbvc += Lvv * (vnewc * vnewc);
+  if (pn1_on) { Lbvc += Lpn1 * e2; Le2 += Lpn1 * bvc; }
+  double Le1 = 0.0;
+  if (!e2fix) {
+    Le1 += Le2;
+    Ldelvc += Le2 * 0.5 * k2;
+    Lpq += Le2 * 1.5 * delvc;
+    LpH += -2.0 * delvc * Le2;
+    Lqn1 += -2.0 * delvc * Le2;
+  }
+  double Lchs = 0.0, Lbvch = 0.0;
+  if (comp) {
+    Lqlin += Lqn1 * s1; Lqquad += Lqn1;
+    if (!s1t) {
+      const double Lssc = Lqn1 * qlin * 0.5 / s1 * irho0;
+      Le1 += Lssc * c1s;
+      const double Lvhalf = Lssc * 2.0 * vhalf * bvc_h * pH;
+      Lbvch += Lssc * (vhalf * vhalf) * pH;
+      LpH += Lssc * (vhalf * vhalf) * bvc_h;
+      Lchs += -Lvhalf * vhalf * vhalf;
+    }
+  }
+  if (pH_on) { Lbvch += LpH * e1; Le1 += LpH * bvc_h; }
+  Lchs += Lbvch * c1s;
+  double Le_old = 0.0;
+  if (!e1min) {
+    Le_old += Le1;
+    Ldelvc += -0.5 * pq * Le1;
+    Lpq += -0.5 * delvc * Le1;
+  }
+  double Lcomp = Lbvc * c1s;
+  const double Lp_old = vmax_hit ? 0.0 : Lpq;
+  const double Lq_old = Lpq;
+  if (!vmax_hit) {
+    if (half_eq) Lcomp += Lchs;
+    else {
+      const double Lvch = -Lchs / (vchalf * vchalf);
+      Lvnewc += Lvch;
+      Ldelvc += -0.5 * Lvch;
+    }
+    Lvnewc += -Lcomp / (vnewc * vnewc);
+  }
+  if (!vmin_c && !vmax_c) Lvnew += Lvnewc;
+  // qlin / qquad
+  double Lself[3] = {0.0, 0.0, 0.0}, Ldx[3] = {0.0, 0.0, 0.0};
+  double Lphi[3] = {0.0, 0.0, 0.0};
+  if (!qzero) {
+    const double Lrho = Lqlin * (-prm.qlc_monoq) * s1sum + Lqquad * prm.qqc_monoq * s2sum;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const double Ldxd = Lqlin * (-prm.qlc_monoq * rho) * (1.0 - phi[d]) +
+                          Lqquad * (prm.qqc_monoq * rho) * 2.0 * dx[d] * fma(-phi[d], phi[d], 1.0);
+      Lphi[d] = Lqlin * (prm.qlc_monoq * rho) * dx[d] + Lqquad * (-prm.qqc_monoq * rho) * dx[d] * dx[d] * 2.0 * phi[d];
+      if (!(fl & (TF_DXCLAMP0 << d))) { Lself[d] += Ldxd * delx[d]; Ldx[d] += Ldxd * self[d]; }
+    }
+    Lvnew += -Lrho * rho / vnew;
+  }
+  // limiter
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    const int src = (int)((fl >> (3 * d)) & 7ull);
+    double Ldm = 0.0, Ldp = 0.0;
+    if (src == PHI_MEAN) { Ldm = 0.5 * Lphi[d]; Ldp = 0.5 * Lphi[d]; }
+    else if (src == PHI_M) Ldm = prm.monoq_limiter_mult * Lphi[d];
+    else if (src == PHI_P) Ldp = prm.monoq_limiter_mult * Lphi[d];
+    const double Lm = Ldm * norm[d], Lp = Ldp * norm[d];
+    const double Lnorm = Ldm * mv[d] + Ldp * pv[d];
+    Lself[d] += -Lnorm * norm[d] * norm[d];
+    double sm = 0.0, sp = 0.0;
+    if (im[d] == i) Lself[d] += Lm; else if (im[d] >= 0) sm = Lm;
+    if (ip[d] == i) Lself[d] += Lp; else if (ip[d] >= 0) sp = Lp;
+    a.lnb[(2 * d) * E + i] = sm;
+    a.lnb[(2 * d + 1) * E + i] = sp;
+    a.ldv[d][i] = Lself[d];
+    a.ldx[d][i] = Ldx[d];
+  }
+  a.lvdov[i] = Lvdov;
+  a.lvnew[i] = Lvnew;
+  a.ldelv[i] = Ldelvc;
+  a.larealg[i] = Larealg;
+  // adjoints of the cycle's start state from the material update
+  a.le[i] = Le_old;
+  a.lp[i] = Lp_old;
+  a.lq[i] = Lq_old;
+  a.lss[i] = 0.0;
+  a.lv[i] = 0.0;
+}
+
+// Limiter neighbour transposes: every element adds the slots of the
+// elements that read its delv (inverse neighbour list, fixed order).
+__global__ void __launch_bounds__(kAdjBlock) ka_nb_gather(AdjDev a) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= a.E) return;
+  double s[3] = {a.ldv[0][k], a.ldv[1][k], a.ldv[2][k]};
+  for (int j = a.nbStart[k]; j < a.nbStart[k + 1]; ++j) {
+    const int ent = a.nbList[j];
+    const int slot = ent / a.E;
+    s[slot >> 1] += a.lnb[ent];
+  }
+  a.ldv[0][k] = s[0];
+  a.ldv[1][k] = s[1];
+  a.ldv[2][k] = s[2];
+}
+
+// ---------------------------------------------------------------------------
+// ka_kinematics: transpose of k_kinematics (volume, characteristic length,
+// velocity-gradient trace, monotonic-Q gradients), into the corner buffers.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, double dt) {
+  const int E = a.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double Ldt = 0.0;
+  if (e < E) {
+    int nd[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
+    double X[3][8], V[3][8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      X[0][c] = a.x1[nd[c]]; X[1][c] = a.y1[nd[c]]; X[2][c] = a.z1[nd[c]];
+      V[0][c] = a.xd1[nd[c]]; V[1][c] = a.yd1[nd[c]]; V[2][c] = a.zd1[nd[c]];
+    }
+    double LX[3][8], LV[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) { LX[k][c] = 0.0; LV[k][c] = 0.0; }
+
+    const double vnew = a.vnew[e], volo = a.volo[e];
+    double Lvnew = a.lvnew[e] + a.ldelv[e];
+    a.lv[e] -= a.ldelv[e];  // delv = vnew - v
+    // Walsh vectors of positions and velocities
+    V3 W[3], VW[3];
+    {
+      double w[3][3], vw[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) { walsh1(X[k], w[k]); walsh1(V[k], vw[k]); }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) { W[d] = v3(w[0][d], w[1][d], w[2][d]); VW[d] = v3(vw[0][d], vw[1][d], vw[2][d]); }
+    }
+    V3 LW[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)}, LVW[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+    // ---- monotonic-Q gradients ----
+    {
+      const double ptiny = 1.e-36;
+      const double vol = volo * vnew;
+      const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
+      double Lvol = 0.0, Lnorm64 = 0.0;
+      // direction d uses A = P x Q and velocity vector VW[d]
+      const int Pi[3] = {1, 2, 0}, Qi[3] = {2, 0, 1};
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const V3 P = W[Pi[d]], Q = W[Qi[d]];
+        const V3 A = vcross(P, Q);
+        const double s2 = fma(A.x, A.x, fma(A.y, A.y, fma(A.z, A.z, 256.0 * ptiny)));
+        const double rs = rsqrt(s2);
+        const double Ldx = a.ldx[d][e], Ldv = a.ldv[d][e];
+        Lvol += Ldx * 16.0 * rs;
+        const double Ls2 = Ldx * 16.0 * vol * (-0.5) * rs * rs * rs;
+        V3 LA = v3(2.0 * A.x * Ls2, 2.0 * A.y * Ls2, 2.0 * A.z * Ls2);
+        const double dot = vdot(A, VW[d]);
+        Lnorm64 += Ldv * dot;
+        vaxpy(LA, Ldv * norm64, VW[d]);
+        vaxpy(LVW[d], Ldv * norm64, A);
+        vadd(LW[Pi[d]], vcross(Q, LA));
+        vadd(LW[Qi[d]], vcross(LA, P));
+      }
+      Lvol += Lnorm64 * (-64.0 * norm64 * norm64);
+      Lvnew += Lvol * volo;
+    }
+    // ---- velocity-gradient trace at the half step ----
+    {
+      const double dt2 = -0.5 * dt;
+      V3 F[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        F[d] = v3(fma(dt2, VW[d].x, W[d].x), fma(dt2, VW[d].y, W[d].y), fma(dt2, VW[d].z, W[d].z));
+      }
+      const V3 C0 = vcross(F[1], F[2]), C1 = vcross(F[2], F[0]), C2 = vcross(F[0], F[1]);
+      const double det = vdot(F[1], C1);
+      const double s = vdot(C0, VW[0]) + vdot(C1, VW[1]) + vdot(C2, VW[2]);
+      const double inv = 1.0 / det;
+      const double vdov = s * inv;
+      const double Ls = a.lvdov[e] * inv;
+      const double Ldet = -a.lvdov[e] * vdov * inv;
+      V3 LC[3];
+      LC[0] = v3(Ls * VW[0].x, Ls * VW[0].y, Ls * VW[0].z);
+      LC[1] = v3(Ls * VW[1].x, Ls * VW[1].y, Ls * VW[1].z);
+      LC[2] = v3(Ls * VW[2].x, Ls * VW[2].y, Ls * VW[2].z);
+      vaxpy(LVW[0], Ls, C0);
+      vaxpy(LVW[1], Ls, C1);
+      vaxpy(LVW[2], Ls, C2);
+      vaxpy(LC[1], Ldet, F[1]);
+      V3 LF[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+      vaxpy(LF[1], Ldet, C1);
+      // C0 = F1 x F2, C1 = F2 x F0, C2 = F0 x F1
+      vadd(LF[1], vcross(F[2], LC[0])); vadd(LF[2], vcross(LC[0], F[1]));
+      vadd(LF[2], vcross(F[0], LC[1])); vadd(LF[0], vcross(LC[1], F[2]));
+      vadd(LF[0], vcross(F[1], LC[2])); vadd(LF[1], vcross(LC[2], F[0]));
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        vadd(LW[d], LF[d]);
+        vaxpy(LVW[d], dt2, LF[d]);
+        Ldt += -0.5 * vdot(LF[d], VW[d]);
+      }
+    }
+    // Walsh transposes
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        const double s = walsh_sign(d, c);
+        LX[0][c] = fma(s, LW[d].x, LX[0][c]); LX[1][c] = fma(s, LW[d].y, LX[1][c]); LX[2][c] = fma(s, LW[d].z, LX[2][c]);
+        LV[0][c] = fma(s, LVW[d].x, LV[0][c]); LV[1][c] = fma(s, LVW[d].y, LV[1][c]); LV[2][c] = fma(s, LVW[d].z, LV[2][c]);
+      }
+    // ---- volume and characteristic length ----
+    {
+      auto dg = [&](int p, int q) { return v3(X[0][p] - X[0][q], X[1][p] - X[1][q], X[2][p] - X[2][q]); };
+      const V3 d61 = dg(6, 1), d70 = dg(7, 0), d63 = dg(6, 3), d20 = dg(2, 0), d50 = dg(5, 0), d64 = dg(6, 4);
+      const V3 d31 = dg(3, 1), d72 = dg(7, 2), d43 = dg(4, 3), d57 = dg(5, 7), d14 = dg(1, 4), d25 = dg(2, 5);
+      // the three triple products of calcElemVolume: U.(V x W)
+      V3 U1 = d31; vadd(U1, d72);
+      V3 U2 = d43; vadd(U2, d57);
+      V3 U3 = d14; vadd(U3, d25);
+      const double v12 = vdot(U1, vcross(d63, d20)) + vdot(U2, vcross(d64, d70)) + vdot(U3, vcross(d61, d50));
+      const double volume = v12 * (1.0 / 12.0);
+      // characteristic length from the face the tape recorded
+      const int f = (int)((a.flags[e] >> TF_FACE_SHIFT) & 7ull);
+      const V3 fa[6] = {d20, d64, d50, d61, d72, d43};
+      const V3 fb[6] = {d31, d57, d14, d25, d63, d70};
+      const V3 nf = vcross(fa[f], fb[f]);
+      const double cl = vdot(nf, nf);
+      const double rsc = rsqrt(cl);
+      const double Lar = a.larealg[e];
+      double Lvolume = Lar * 2.0 * rsc + Lvnew * a.inv_volo[e];
+      const double Lcl = Lar * 2.0 * volume * (-0.5) * rsc * rsc * rsc;
+      const V3 Ln = v3(2.0 * nf.x * Lcl, 2.0 * nf.y * Lcl, 2.0 * nf.z * Lcl);
+      const V3 Lfa = vcross(fb[f], Ln), Lfb = vcross(Ln, fa[f]);
+      const double Lv12 = Lvolume * (1.0 / 12.0);
+      // gradients of the diagonals
+      V3 L61 = v3(0, 0, 0), L70 = v3(0, 0, 0), L63 = v3(0, 0, 0), L20 = v3(0, 0, 0), L50 = v3(0, 0, 0), L64 = v3(0, 0, 0);
+      V3 L31 = v3(0, 0, 0), L72 = v3(0, 0, 0), L43 = v3(0, 0, 0), L57 = v3(0, 0, 0), L14 = v3(0, 0, 0), L25 = v3(0, 0, 0);
+      {
+        const V3 gU1 = vcross(d63, d20), gV1 = vcross(d20, U1), gW1 = vcross(U1, d63);
+        vaxpy(L31, Lv12, gU1); vaxpy(L72, Lv12, gU1); vaxpy(L63, Lv12, gV1); vaxpy(L20, Lv12, gW1);
+        const V3 gU2 = vcross(d64, d70), gV2 = vcross(d70, U2), gW2 = vcross(U2, d64);
+        vaxpy(L43, Lv12, gU2); vaxpy(L57, Lv12, gU2); vaxpy(L64, Lv12, gV2); vaxpy(L70, Lv12, gW2);
+        const V3 gU3 = vcross(d61, d50), gV3 = vcross(d50, U3), gW3 = vcross(U3, d61);
+        vaxpy(L14, Lv12, gU3); vaxpy(L25, Lv12, gU3); vaxpy(L61, Lv12, gV3); vaxpy(L50, Lv12, gW3);
+      }
+      V3* Lfa_t[6] = {&L20, &L64, &L50, &L61, &L72, &L43};
+      V3* Lfb_t[6] = {&L31, &L57, &L14, &L25, &L63, &L70};
+#pragma unroll
+      for (int q = 0; q < 6; ++q)
+        if (q == f) { vadd(*Lfa_t[q], Lfa); vadd(*Lfb_t[q], Lfb); }
+      auto put = [&](const V3& L, int p, int q) {
+        LX[0][p] += L.x; LX[1][p] += L.y; LX[2][p] += L.z;
+        LX[0][q] -= L.x; LX[1][q] -= L.y; LX[2][q] -= L.z;
+      };
+      put(L61, 6, 1); put(L70, 7, 0); put(L63, 6, 3); put(L20, 2, 0); put(L50, 5, 0); put(L64, 6, 4);
+      put(L31, 3, 1); put(L72, 7, 2); put(L43, 4, 3); put(L57, 5, 7); put(L14, 1, 4); put(L25, 2, 5);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) {
+        a.cX[(k * 8 + c) * E + e] = LX[k][c];
+        a.cV[(k * 8 + c) * E + e] = LV[k][c];
+      }
+  }
+  block_sum_to(Ldt, a.part_dt);
+}
+
+// Sums the corner buffers into node adjoints (added to what is there).
+__global__ void __launch_bounds__(kAdjBlock) ka_gather_corners(AdjDev a) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= a.N) return;
+  const int s = a.nodeElemStart[i], t = a.nodeElemStart[i + 1];
+  const long long E8 = 8ll * a.E;
+  double gx = 0, gy = 0, gz = 0, hx = 0, hy = 0, hz = 0;
+  for (int j = s; j < t; ++j) {
+    const int c = a.cornerList[j];
+    gx += a.cX[c]; gy += a.cX[E8 + c]; gz += a.cX[2 * E8 + c];
+    hx += a.cV[c]; hy += a.cV[E8 + c]; hz += a.cV[2 * E8 + c];
+  }
+  a.lx[i] += gx; a.ly[i] += gy; a.lz[i] += gz;
+  a.lxd[i] += hx; a.lyd[i] += hy; a.lzd[i] += hz;
+}
+
+// ---------------------------------------------------------------------------
+// ka_node: transpose of k_node (position and velocity update with the
+// velocity snap, acceleration = force / mass with the symmetry BCs).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, double dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double Ldt = 0.0;
+  if (i < a.N) {
+    const unsigned bc = a.nodeBC[i];
+    const double im = a.inv_nodalMass[i];
+    double* Lx[3] = {a.lx, a.ly, a.lz};
+    double* Lxd[3] = {a.lxd, a.lyd, a.lzd};
+    double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+    const double* xd1[3] = {a.xd1, a.yd1, a.zd1};
+    const double* acc[3] = {a.ax, a.ay, a.az};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double lxn = Lx[k][i];
+      const double v1 = xd1[k][i];
+      double lv = Lxd[k][i] + lxn * dt;   // x1 = x0 + xd1*dt
+      Ldt += lxn * v1;
+      double lf = 0.0;
+      if (v1 == 0.0) {
+        lv = 0.0;                        // snapped to zero (|v| < u_cut)
+      } else {
+        const double acc_k = acc[k][i];
+        Ldt += lv * acc_k;               // xd1 = xd0 + a*dt
+        if (!(bc & (1u << k))) lf = lv * dt * im;
+      }
+      Lx[k][i] = lxn;
+      Lxd[k][i] = lv;
+      Lf[k][i] = lf;
+    }
+  }
+  block_sum_to(Ldt, a.part_dtn);
+}
+
+// ---------------------------------------------------------------------------
+// ka_force: transpose of k_force (stress integration and FB hourglass force).
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock) ka_force(AdjDev a, double hgcoef) {
+  const int E = a.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  double Lhg_coef = 0.0;
+  if (e < E) {
+    int nd[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
+    double X[3][8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { X[0][c] = a.x0[nd[c]]; X[1][c] = a.y0[nd[c]]; X[2][c] = a.z0[nd[c]]; }
+    double LX[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) LX[k][c] = 0.0;
+    const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+    const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
+    // ---- stress part: f = s8 * B ----
+    {
+      constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
+                                {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
+      constexpr int nf[8][3] = {{0, 1, 4}, {0, 1, 2}, {0, 2, 3}, {0, 3, 4},
+                                {1, 4, 5}, {1, 2, 5}, {2, 3, 5}, {3, 4, 5}};
+      V3 N[6];
+#pragma unroll
+      for (int f = 0; f < 6; ++f) {
+        const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
+        const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
+        N[f] = vcross(d1, d2);
+      }
+      double Ls8 = 0.0;
+      V3 LN[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        const V3 lf = v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]);
+        V3 B = N[nf[n][0]]; vadd(B, N[nf[n][1]]); vadd(B, N[nf[n][2]]);
+        V3 LB = v3(s8 * lf.x, s8 * lf.y, s8 * lf.z);
+        if (n == 0 && !(MODE & 1)) {
+          // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice and no areaZ
+          B.y += N[4].y;
+          B.z -= N[4].z;
+          Ls8 += vdot(lf, B);
+          LN[0].x += LB.x; LN[1].x += LB.x; LN[4].x += LB.x;
+          LN[0].y += LB.y; LN[1].y += LB.y; LN[4].y += 2.0 * LB.y;
+          LN[0].z += LB.z; LN[1].z += LB.z;
+        } else {
+          Ls8 += vdot(lf, B);
+          vadd(LN[nf[n][0]], LB); vadd(LN[nf[n][1]], LB); vadd(LN[nf[n][2]], LB);
+        }
+      }
+      const double Lpq = -0.125 * Ls8;
+      a.lp[e] += Lpq;
+      a.lq[e] += Lpq;
+#pragma unroll
+      for (int f = 0; f < 6; ++f) {
+        const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
+        const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
+        const V3 L1 = vcross(d2, LN[f]), L2 = vcross(LN[f], d1);
+        LX[0][fd[f][0]] += L1.x; LX[1][fd[f][0]] += L1.y; LX[2][fd[f][0]] += L1.z;
+        LX[0][fd[f][1]] -= L1.x; LX[1][fd[f][1]] -= L1.y; LX[2][fd[f][1]] -= L1.z;
+        LX[0][fd[f][2]] += L2.x; LX[1][fd[f][2]] += L2.y; LX[2][fd[f][2]] += L2.z;
+        LX[0][fd[f][3]] -= L2.x; LX[1][fd[f][3]] -= L2.y; LX[2][fd[f][3]] -= L2.z;
+      }
+    }
+    // ---- FB hourglass part ----
+    const double v = a.v0[e];
+    const double determ = a.volo[e] * v;
+    if (hgcoef > 0.0) {
+      double w1[3], hm[3][4];
+      walsh7(X[0], w1, hm[0]);
+      walsh7(X[1], w1, hm[1]);
+      walsh7(X[2], w1, hm[2]);
+      constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
+      constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
+      // edge ids of (q1q2, q0q1, q0q4, q3q4, q2q5, q3q5) for each voluDer call
+      constexpr int pe[8][6] = {{5, 3, 4, 8, 7, 9}, {3, 0, 2, 9, 6, 11}, {0, 1, 7, 11, 4, 10},
+                                {1, 5, 6, 10, 2, 8}, {10, 11, 7, 1, 4, 0}, {11, 9, 2, 0, 6, 3},
+                                {9, 8, 4, 3, 7, 5}, {8, 10, 6, 5, 2, 1}};
+      constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
+      double dv[3][8];
+      {
+        double ex[12], ey[12], ez[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          ex[k] = X[0][ea[k]] + X[0][eb[k]];
+          ey[k] = X[1][ea[k]] + X[1][eb[k]];
+          ez[k] = X[2][ea[k]] + X[2][eb[k]];
+        }
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
+          const int slot = (MODE & 2) ? owner[n] : n;
+          dv[0][slot] = fma(ey[p12], ez[p01], fma(-ey[p01], ez[p12], fma(ey[p04], ez[p34],
+                        fma(-ey[p34], ez[p04], fma(-ey[p25], ez[p35], ey[p35] * ez[p25])))));
+          dv[1][slot] = fma(-ex[p12], ez[p01], fma(ex[p01], ez[p12], fma(-ex[p04], ez[p34],
+                        fma(ex[p34], ez[p04], fma(ex[p25], ez[p35], -(ex[p35] * ez[p25]))))));
+          dv[2][slot] = fma(-ey[p12], ex[p01], fma(ey[p01], ex[p12], fma(-ey[p04], ex[p34],
+                        fma(ey[p34], ex[p04], fma(ey[p25], ex[p35], -(ey[p35] * ex[p25]))))));
+        }
+      }
+      const double vi12 = 1.0 / (12.0 * determ);
+      double hms[3][4];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) hms[k][m] = vi12 * hm[k][m];
+      double hg[8][4], Lhg[8][4];
+#pragma unroll
+      for (int n = 0; n < 8; ++n)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          hg[n][m] = fma(-dv[2][n], hms[2][m], fma(-dv[1][n], hms[1][m], fma(-dv[0][n], hms[0][m], gamma_nm(n, m))));
+          Lhg[n][m] = 0.0;
+        }
+      const double ss = a.ss0[e], mass = a.elemMass[e];
+      const double r = rcbrt(determ);
+      const double c0 = -hgcoef * 0.01;
+      const double coef = ((c0 * ss) * mass) * r;
+      double Lcoef = 0.0;
+      const double* Vp[3] = {a.xd0, a.yd0, a.zd0};
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double vv[8], lf[8];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) { vv[c] = Vp[k][nd[c]]; lf[c] = Lf[k][nd[c]]; }
+        double S[4], h[4], Lh[4];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          double s = hg[0][m] * vv[0];
+#pragma unroll
+          for (int n = 1; n < 8; ++n) s = fma(hg[n][m], vv[n], s);
+          S[m] = s;
+          h[m] = coef * s;
+          double lh = 0.0;
+#pragma unroll
+          for (int n = 0; n < 8; ++n) {
+            lh = fma(lf[n], hg[n][m], lh);
+            Lhg[n][m] = fma(lf[n], h[m], Lhg[n][m]);
+          }
+          Lh[m] = lh;
+          Lcoef = fma(lh, S[m], Lcoef);
+        }
+        double LV[8];
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          double l = 0.0;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            const double LS = coef * Lh[m];
+            Lhg[n][m] = fma(LS, vv[n], Lhg[n][m]);
+            l = fma(LS, hg[n][m], l);
+          }
+          LV[n] = l;
+        }
+#pragma unroll
+        for (int c = 0; c < 8; ++c) a.cV[(k * 8 + c) * E + e] = LV[c];
+      }
+      // coef = c0*ss*mass*determ^(-1/3)
+      a.lss[e] += Lcoef * c0 * mass * r;
+      Lhg_coef = Lcoef * (-0.01) * ss * mass * r;
+      double Ldeterm = Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r / determ;
+      // hg = gamma - sum_k dv_k hms_k
+      double Ldv[3][8], Lhms[3][4];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          double s = 0.0;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) s = fma(Lhg[n][m], hms[k][m], s);
+          Ldv[k][n] = -s;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m) {
+          double s = 0.0;
+#pragma unroll
+          for (int n = 0; n < 8; ++n) s = fma(Lhg[n][m], dv[k][n], s);
+          Lhms[k][m] = -s;
+        }
+      }
+      double Lvi12 = 0.0;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) Lvi12 = fma(Lhms[k][m], hm[k][m], Lvi12);
+      Ldeterm += -Lvi12 * vi12 / determ;
+      a.lv[e] += Ldeterm * a.volo[e];
+      // hm_k[m] = sum_n gamma[n][m] X_k[n]
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          double s = 0.0;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) s = fma(gamma_nm(n, m), vi12 * Lhms[k][m], s);
+          LX[k][n] += s;
+        }
+      // voluDer transposes onto the edge sums, then onto the nodes
+      double Lex[12], Ley[12], Lez[12];
+#pragma unroll
+      for (int j = 0; j < 12; ++j) { Lex[j] = 0.0; Ley[j] = 0.0; Lez[j] = 0.0; }
+      {
+        double ex[12], ey[12], ez[12];
+#pragma unroll
+        for (int k = 0; k < 12; ++k) {
+          ex[k] = X[0][ea[k]] + X[0][eb[k]];
+          ey[k] = X[1][ea[k]] + X[1][eb[k]];
+          ez[k] = X[2][ea[k]] + X[2][eb[k]];
+        }
+#pragma unroll
+        for (int n = 0; n < 8; ++n) {
+          const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
+          const int slot = (MODE & 2) ? owner[n] : n;
+          const double gx = Ldv[0][slot], gy = Ldv[1][slot], gz = Ldv[2][slot];
+          // dvx = ey12 ez01 - ey01 ez12 + ey04 ez34 - ey34 ez04 - ey25 ez35 + ey35 ez25
+          Ley[p12] += gx * ez[p01]; Lez[p01] += gx * ey[p12];
+          Ley[p01] -= gx * ez[p12]; Lez[p12] -= gx * ey[p01];
+          Ley[p04] += gx * ez[p34]; Lez[p34] += gx * ey[p04];
+          Ley[p34] -= gx * ez[p04]; Lez[p04] -= gx * ey[p34];
+          Ley[p25] -= gx * ez[p35]; Lez[p35] -= gx * ey[p25];
+          Ley[p35] += gx * ez[p25]; Lez[p25] += gx * ey[p35];
+          // dvy = -ex12 ez01 + ex01 ez12 - ex04 ez34 + ex34 ez04 + ex25 ez35 - ex35 ez25
+          Lex[p12] -= gy * ez[p01]; Lez[p01] -= gy * ex[p12];
+          Lex[p01] += gy * ez[p12]; Lez[p12] += gy * ex[p01];
+          Lex[p04] -= gy * ez[p34]; Lez[p34] -= gy * ex[p04];
+          Lex[p34] += gy * ez[p04]; Lez[p04] += gy * ex[p34];
+          Lex[p25] += gy * ez[p35]; Lez[p35] += gy * ex[p25];
+          Lex[p35] -= gy * ez[p25]; Lez[p25] -= gy * ex[p35];
+          // dvz = -ey12 ex01 + ey01 ex12 - ey04 ex34 + ey34 ex04 + ey25 ex35 - ey35 ex25
+          Ley[p12] -= gz * ex[p01]; Lex[p01] -= gz * ey[p12];
+          Ley[p01] += gz * ex[p12]; Lex[p12] += gz * ey[p01];
+          Ley[p04] -= gz * ex[p34]; Lex[p34] -= gz * ey[p04];
+          Ley[p34] += gz * ex[p04]; Lex[p04] += gz * ey[p34];
+          Ley[p25] += gz * ex[p35]; Lex[p35] += gz * ey[p25];
+          Ley[p35] -= gz * ex[p25]; Lex[p25] -= gz * ey[p35];
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 12; ++j) {
+        LX[0][ea[j]] += Lex[j]; LX[0][eb[j]] += Lex[j];
+        LX[1][ea[j]] += Ley[j]; LX[1][eb[j]] += Ley[j];
+        LX[2][ea[j]] += Lez[j]; LX[2][eb[j]] += Lez[j];
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) a.cV[(k * 8 + c) * E + e] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
+  }
+  block_sum_to(Lhg_coef, a.part_hg);
+}
+
+// Sums `n` partials in a fixed order (one block).
+__global__ void __launch_bounds__(kAdjBlock) ka_sum(const double* part, int n, double* out) {
+  double s = 0.0;
+  for (int j = threadIdx.x; j < n; j += blockDim.x) s += part[j];
+  __shared__ double sh[kAdjBlock];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int w = kAdjBlock / 2; w > 0; w >>= 1) {
+    if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = sh[0];
+}
+
+// Smallest element index whose dt candidate equals the minimum: the element
+// the reference's strict-less-than scan keeps (src/domain.jl:3003-3008).
+__global__ void __launch_bounds__(kAdjBlock) ka_argmin(const double* cand, int E, unsigned long long minbits,
+                                                        int* out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < E && (unsigned long long)__double_as_longlong(cand[i]) == minbits) atomicMin(out, i);
+}
+
+// Loss seed and value: L = sum_e w_e e + sum_n 0.5 w_n |u|^2 with
+// w_e = mask*elemMass, w_n = mask*nodalMass (masks from the reference mesh).
+__global__ void __launch_bounds__(kAdjBlock) ka_loss_elem(const double* we, const double* e, int E, double* le,
+                                                           double* part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (i < E) {
+    s = we[i] * e[i];
+    if (le) le[i] = we[i];
+  }
+  block_sum_to(s, part);
+}
+
+__global__ void __launch_bounds__(kAdjBlock) ka_loss_node(const double* wn, const double* xd, const double* yd,
+                                                           const double* zd, int N, double* lxd, double* lyd,
+                                                           double* lzd, double* part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  double s = 0.0;
+  if (i < N) {
+    const double w = wn[i], u = xd[i], v = yd[i], z = zd[i];
+    s = 0.5 * w * fma(u, u, fma(v, v, z * z));
+    if (lxd) { lxd[i] = w * u; lyd[i] = w * v; lzd[i] = w * z; }
+  }
+  block_sum_to(s, part);
+}
+
+}  // namespace lulesh

@@ -13,13 +13,13 @@
 #include "lulesh_kernels.h"
 #include "lulesh_setup.h"
 #include "lulesh_arena.h"
+#include "lulesh_handle.h"
 #include "lulesh_device.cuh"
 
 using namespace lulesh;
 
 namespace {
 
-constexpr int kNumKernels = 5;
 const char* const kKernelNames[kNumKernels] = {"k_time_increment", "k_force", "k_node",
                                                "k_kinematics", "k_material"};
 constexpr int kGraphCycles = 16;   // cycles per captured graph
@@ -27,35 +27,7 @@ constexpr int kTimingCycles = 256; // cycles of kernel events held before a read
 constexpr int kPollLaunches = 4;   // graph launches between host polls
 constexpr int kPollCyclesTimed = 64;  // timed (graph-less) cycles between host polls
 
-struct HostScalars {
-  double s[LULESH_S_COUNT];
-};
-
 }  // namespace
-
-struct lulesh_domain {
-  lulesh_params params;
-  int64_t E = 0, N = 0;
-  double sc[LULESH_S_COUNT];  // Domain scalars (LULESH_S_*), cycle stored as double
-  int32_t status = 0, site = 0;
-  DevDomain dd{};
-  void* arena = nullptr;
-  cudaStream_t stream = nullptr;
-  DevState* hst = nullptr;  // pinned mirror of the device state
-  cudaGraphExec_t graph = nullptr;
-  int64_t graph_key = -1;
-  // host copies of what only the host uses
-  std::vector<int> symmX, symmY, symmZ;
-  std::vector<int64_t> regNumList, regElemlist, regCSR, regReps, regSorted, regElemSize;
-  // timing: a ring of kTimingCycles cycles x (kNumKernels+1) events, read
-  // back when full or when the caller asks, so timed runs never stall per cycle
-  bool timing = false;
-  std::vector<cudaEvent_t> ring;
-  int ring_used = 0;
-  Tuning tuning;
-  double kernel_ms[kNumKernels] = {};
-  int64_t cycle_i() const { return (int64_t)sc[LULESH_S_CYCLE]; }
-};
 
 static int cuda_fail(cudaError_t e) {
   if (e == cudaSuccess) return LULESH_OK;
@@ -64,7 +36,7 @@ static int cuda_fail(cudaError_t e) {
 }
 #define CK(call) do { int rc_ = cuda_fail(call); if (rc_) return rc_; } while (0)
 
-static Params make_params(const lulesh_domain* d) {
+Params lulesh::make_params(const lulesh_domain* d) {
   Params p;
   p.u_cut = d->sc[LULESH_S_U_CUT];
   p.hgcoef = d->sc[LULESH_S_HGCOEF];
@@ -93,7 +65,7 @@ static Params make_params(const lulesh_domain* d) {
 }
 
 // Maps kernel status bits to (status, site) in the reference's check order.
-static void decode_status(unsigned bits, int32_t* status, int32_t* site) {
+void lulesh::decode_status(unsigned bits, int32_t* status, int32_t* site) {
   *status = LULESH_OK;
   *site = LULESH_SITE_NONE;
   if (!bits) return;
@@ -106,7 +78,7 @@ static void decode_status(unsigned bits, int32_t* status, int32_t* site) {
   if (bits & ST_UPDATE) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_UPDATE; return; }
 }
 
-static void state_to_device_mirror(lulesh_domain* d) {
+void lulesh::state_to_device_mirror(lulesh_domain* d) {
   DevState* s = d->hst;
   s->time = d->sc[LULESH_S_TIME];
   s->deltatime = d->sc[LULESH_S_DELTATIME];
@@ -121,7 +93,7 @@ static void state_to_device_mirror(lulesh_domain* d) {
   s->first = 1;
 }
 
-static void state_from_device_mirror(lulesh_domain* d) {
+void lulesh::state_from_device_mirror(lulesh_domain* d) {
   DevState* s = d->hst;
   d->sc[LULESH_S_TIME] = s->time;
   d->sc[LULESH_S_DELTATIME] = s->deltatime;

@@ -28,6 +28,35 @@ enum : uint32_t {
   ST_UPDATE = 1u << 6,      // new v <= 0, src/domain.jl:2926
 };
 
+// Which value a monotonic-Q limiter returned (src/domain.jl:2357-2376).
+enum : int { PHI_MEAN = 0, PHI_M = 1, PHI_P = 2, PHI_ZERO = 3, PHI_MAX = 4 };
+
+// Branch record of one element's step, written by the taping forward kernels
+// and read by the adjoint so it differentiates exactly the branches taken.
+enum : unsigned long long {
+  TF_PHI_SHIFT = 0,            // 3 bits per direction (xi, eta, zeta): PHI_*
+  TF_QZERO = 1ull << 9,        // vdov > 0: ql = qq = 0
+  TF_DXCLAMP0 = 1ull << 10,    // delv_d * delx_d > 0 clamped to 0 (d = 0, 1, 2: bits 10-12)
+  TF_VNEW_MIN = 1ull << 13,    // vnewc clamped to eosvmin
+  TF_VNEW_MAX = 1ull << 14,    // vnewc clamped to eosvmax
+  TF_HALF_EQ_COMP = 1ull << 15,  // compHalfStep = compression (vnewc <= eosvmin)
+  TF_VMAX_HIT = 1ull << 16,    // vnewc >= eosvmax: pressures 0, p_old/compressions 0
+  TF_E1_MIN = 1ull << 17,      // first energy clamped to emin
+  TF_PH_CUT = 1ull << 18,      // half-step pressure: |p| < p_cut -> 0
+  TF_PH_MIN = 1ull << 19,      // half-step pressure clamped to pmin
+  TF_COMPRESS = 1ull << 20,    // delvc <= 0: q terms active
+  TF_S1_TINY = 1ull << 21,     // half-step sound speed took the TINY branch
+  TF_E2_CUT = 1ull << 22, TF_E2_MIN = 1ull << 23,
+  TF_PN1_CUT = 1ull << 24, TF_PN1_MIN = 1ull << 25,
+  TF_S2_TINY = 1ull << 26,
+  TF_E3_CUT = 1ull << 27, TF_E3_MIN = 1ull << 28,
+  TF_PN2_CUT = 1ull << 29, TF_PN2_MIN = 1ull << 30,
+  TF_SS_TINY = 1ull << 31,
+  TF_Q_CUT = 1ull << 32,       // final q: |q| < q_cut -> 0
+  TF_V_SNAP = 1ull << 33,      // |vnew - 1| < v_cut: v = 1
+  TF_FACE_SHIFT = 40,          // 3 bits: face whose area set the characteristic length
+};
+
 // Per-problem parameters passed by value to every kernel.
 struct Params {
   double u_cut, hgcoef, qstop, monoq_max_slope, monoq_limiter_mult, e_cut, p_cut, q_cut, v_cut;
@@ -82,6 +111,11 @@ struct DevDomain {
   const int* nodeInst;
   const double* instHg;
   int ninst;
+  // adjoint taping (null unless recording): branch flags and each element's
+  // Courant and hydro dt candidates (+inf where vdov == 0)
+  unsigned long long* tapeFlags;
+  double* tapeDtc;
+  double* tapeDth;
 };
 
 }  // namespace lulesh

@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(kMaxNodeBlock) k_node(DevDomain d, Params prm)
 // ---------------------------------------------------------------------------
 // k_kinematics
 // ---------------------------------------------------------------------------
-template <bool AUX, bool ENS>
+template <bool AUX, bool ENS, bool TAPE>
 __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -286,30 +286,31 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
         triple(d43[0] + d57[0], d64[0], d70[0], d43[1] + d57[1], d64[1], d70[1], d43[2] + d57[2], d64[2], d70[2]) +
         triple(d14[0] + d25[0], d61[0], d50[0], d14[1] + d25[1], d61[1], d50[1], d14[2] + d25[2], d61[2], d50[2]);
     volume = v12 * (1.0 / 12.0);
-    // areaFace (src/domain.jl:1874-1891) for the six faces; f, g from the
-    // face diagonals.
-    auto face = [&](const double* a, const double* b, double sf, double sg) {
-      double f[3], g[3];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) { f[k] = fma(sf, b[k], a[k]); g[k] = fma(sg, b[k], a[k]); }
-      const double ff = fma(f[0], f[0], fma(f[1], f[1], f[2] * f[2]));
-      const double gg = fma(g[0], g[0], fma(g[1], g[1], g[2] * g[2]));
-      const double fg = fma(f[0], g[0], fma(f[1], g[1], f[2] * g[2]));
-      const double area = fma(ff, gg, -(fg * fg));
-      charLength = fmax(area, charLength);
+    // areaFace (src/domain.jl:1874-1891): with f, g = a -/+ b for the face
+    // diagonals a, b, |f|^2|g|^2 - (f.g)^2 = |f x g|^2 = 4 |a x b|^2; the 4
+    // is folded into arealg below.
+    int fidx = 0;
+    auto face = [&](const double* a, const double* b, int f) {
+      double cx, cy, cz;
+      cross(a[0], a[1], a[2], b[0], b[1], b[2], cx, cy, cz);
+      const double area4 = fma(cx, cx, fma(cy, cy, cz * cz));
+      if (TAPE && area4 > charLength) fidx = f;
+      charLength = fmax(area4, charLength);
     };
-    face(d20, d31, -1.0, 1.0);   // nodes 1,2,3,4
-    face(d64, d57, 1.0, -1.0);   // 5,6,7,8
-    face(d50, d14, 1.0, -1.0);   // 1,2,6,5
-    face(d61, d25, 1.0, -1.0);   // 2,3,7,6
-    face(d72, d63, -1.0, 1.0);   // 3,4,8,7
-    face(d43, d70, -1.0, 1.0);   // 4,1,5,8
+    face(d20, d31, 0);   // nodes 1,2,3,4
+    face(d64, d57, 1);   // 5,6,7,8
+    face(d50, d14, 2);   // 1,2,6,5
+    face(d61, d25, 3);   // 2,3,7,6
+    face(d72, d63, 4);   // 3,4,8,7
+    face(d43, d70, 5);   // 4,1,5,8
+    if (TAPE) d.tapeFlags[e] = (unsigned long long)fidx << TF_FACE_SHIFT;
   }
   const double vnew = volume * LDG(&d.inv_volo[e]);
   if (le_zero(vnew)) atomicOr(&st->status, ST_KINEMATICS);
   d.vnew[e] = vnew;
   d.delv[e] = vnew - LDG(&d.v[e]);
-  d.arealg[e] = (4.0 * volume) * rsqrt(charLength);
+  // 4*volume/sqrt(max area) with area = 4*area4
+  d.arealg[e] = (2.0 * volume) * rsqrt(charLength);
 
   // Velocity gradient trace at the half-step position (src/domain.jl:2128-2158)
   double wx[3], wy[3], wz[3];
@@ -389,18 +390,20 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
 // k_material
 // ---------------------------------------------------------------------------
 
-// One limiter direction, src/domain.jl:2330-2376.
-__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm) {
+// One limiter direction, src/domain.jl:2330-2376. `src` reports which value
+// the result is (PHI_*), for the adjoint's tape.
+__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm, int& src) {
   const double norm = 1.0 / (self + 1.e-36);
   dm *= norm;
   dp *= norm;
   double phi = 0.5 * (dm + dp);
+  src = PHI_MEAN;
   dm *= prm.monoq_limiter_mult;
   dp *= prm.monoq_limiter_mult;
-  if (dm < phi) phi = dm;
-  if (dp < phi) phi = dp;
-  if (phi < 0.0) phi = 0.0;
-  if (phi > prm.monoq_max_slope) phi = prm.monoq_max_slope;
+  if (dm < phi) { phi = dm; src = PHI_M; }
+  if (dp < phi) { phi = dp; src = PHI_P; }
+  if (phi < 0.0) { phi = 0.0; src = PHI_ZERO; }
+  if (phi > prm.monoq_max_slope) { phi = prm.monoq_max_slope; src = PHI_MAX; }
   return phi;
 }
 
@@ -480,7 +483,7 @@ __device__ __forceinline__ void warp_min2_by_instance(unsigned long long a, unsi
   }
 }
 
-template <int MODE, bool AUX, bool ENS>
+template <int MODE, bool AUX, bool ENS, bool TAPE>
 __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params prm) {
   const int E = d.E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -491,22 +494,25 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
   const bool live = (i < E) && !step_off(st);
   if (live) {
     unsigned int err = 0u;
+    unsigned long long fl = 0ull;  // branch record (TAPE only)
     // ---- calcMonotonicQRegionForElems, src/domain.jl:2322-2513 ----
     const unsigned mask = LDG(&d.elemBC[i]);
     const double dvxi = LDG(&d.delv_xi[i]), dveta = LDG(&d.delv_eta[i]), dvzeta = LDG(&d.delv_zeta[i]);
     bool bad = false;
+    int src0, src1, src2;
     // xi-plus: the reference indexes delv_xi[lxip[i]] without +1 (:2349)
     const int ixp = (MODE & 4) ? LDG(&d.lxip[i]) : LDG(&d.lxip[i]) - 1;
     double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
     double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
-    const double phixi = monoq_phi(dvxi, dm, dp, prm);
+    const double phixi = monoq_phi(dvxi, dm, dp, prm, src0);
     dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);
-    const double phieta = monoq_phi(dveta, dm, dp, prm);
+    const double phieta = monoq_phi(dveta, dm, dp, prm, src1);
     dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, E, bad);
-    const double phizeta = monoq_phi(dvzeta, dm, dp, prm);
+    const double phizeta = monoq_phi(dvzeta, dm, dp, prm, src2);
     if (bad) err |= ST_BAD_BC;
+    if (TAPE) fl |= (unsigned long long)(src0 | (src1 << 3) | (src2 << 6));
 
     const double vdov = LDG(&d.vdov[i]);
     const double vnew = LDG(&d.vnew[i]);
@@ -515,13 +521,14 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     if (gt_zero(vdov)) {
       qlin = 0.0;
       qquad = 0.0;
+      if (TAPE) fl |= TF_QZERO;
     } else {
       double dxxi = dvxi * LDG(&d.delx_xi[i]);
       double dxeta = dveta * LDG(&d.delx_eta[i]);
       double dxzeta = dvzeta * LDG(&d.delx_zeta[i]);
-      if (gt_zero(dxxi)) dxxi = 0.0;
-      if (gt_zero(dxeta)) dxeta = 0.0;
-      if (gt_zero(dxzeta)) dxzeta = 0.0;
+      if (gt_zero(dxxi)) { dxxi = 0.0; if (TAPE) fl |= TF_DXCLAMP0; }
+      if (gt_zero(dxeta)) { dxeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 1; }
+      if (gt_zero(dxzeta)) { dxzeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 2; }
       const double rho = LDG(&d.elemMass[i]) / (volo * vnew);
       qlin = (-prm.qlc_monoq * rho) *
              fma(dxxi, 1.0 - phixi, fma(dxeta, 1.0 - phieta, dxzeta * (1.0 - phizeta)));
@@ -537,8 +544,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     // ---- applyMaterialPropertiesForElems, src/domain.jl:2860-2910 ----
     double vnewc = vnew;
-    if (prm.eosvmin != 0.0 && vnewc < prm.eosvmin) vnewc = prm.eosvmin;
-    if (prm.eosvmax != 0.0 && vnewc > prm.eosvmax) vnewc = prm.eosvmax;
+    if (prm.eosvmin != 0.0 && vnewc < prm.eosvmin) { vnewc = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
+    if (prm.eosvmax != 0.0 && vnewc > prm.eosvmax) { vnewc = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
     {
       double vc = LDG(&d.v[i]);
       if (prm.eosvmin != 0.0 && vc < prm.eosvmin) vc = prm.eosvmin;
@@ -555,51 +562,60 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     double compression = 1.0 / vnewc - 1.0;
     const double vchalf = fma(delvc, -0.5, vnewc);
     double compHalfStep = 1.0 / vchalf - 1.0;
-    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) compHalfStep = compression;
-    if (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) { p_old = 0.0; compression = 0.0; compHalfStep = 0.0; }
+    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) { compHalfStep = compression; if (TAPE) fl |= TF_HALF_EQ_COMP; }
+    if (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) {
+      p_old = 0.0; compression = 0.0; compHalfStep = 0.0;
+      if (TAPE) fl |= TF_VMAX_HIT;
+    }
     const double c1s = 2.0 / 3.0;
     const double inv_rho0 = 1.0 / prm.refdens;
     const bool vmax_hit = vnewc >= prm.eosvmax;
-    // calcPressureForElems (src/domain.jl:2585-2614) for one element
-    auto pressure = [&](double enew, double bvc) -> double {
+    // calcPressureForElems (src/domain.jl:2585-2614) for one element; the
+    // cut / pmin outcomes go to the tape bits given
+    auto pressure = [&](double enew, double bvc, unsigned long long cut_bit, unsigned long long min_bit) -> double {
       double pn = bvc * enew;
-      if (abs_lt(pn, prm.p_cut)) pn = 0.0;
+      if (abs_lt(pn, prm.p_cut)) { pn = 0.0; if (TAPE) fl |= cut_bit; }
       if (vmax_hit) pn = 0.0;
-      if (pn < prm.pmin) pn = prm.pmin;
+      if (pn < prm.pmin) { pn = prm.pmin; if (TAPE) fl |= min_bit; }
       return pn;
+    };
+    auto tiny_sqrt = [&](double ssc, unsigned long long bit) -> double {
+      if (ssc <= 0.111111e-36) { if (TAPE) fl |= bit; return 0.333333e-18; }
+      return sqrt(ssc);
     };
     const double pq_old = p_old + q_old;
     double e_new = fma(-0.5 * delvc, pq_old, e_old);
-    if (e_new < prm.emin) e_new = prm.emin;
+    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
     const double bvc_half = c1s * (compHalfStep + 1.0);
-    const double pHalfStep = pressure(e_new, bvc_half);
+    const double pHalfStep = pressure(e_new, bvc_half, TF_PH_CUT, TF_PH_MIN);
     const double vhalf = 1.0 / (1.0 + compHalfStep);
     const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
+    if (TAPE && compress) fl |= TF_COMPRESS;
     double q_new = 0.0;
     if (compress) {
       const double ssc = fma(c1s, e_new, ((vhalf * vhalf) * bvc_half) * pHalfStep) * inv_rho0;
-      q_new = fma(ssc_sqrt(ssc), qlin, qquad);
+      q_new = fma(tiny_sqrt(ssc, TF_S1_TINY), qlin, qquad);
     }
     e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
-    if (abs_lt(e_new, prm.e_cut)) e_new = 0.0;
-    if (e_new < prm.emin) e_new = prm.emin;
+    if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E2_CUT; }
+    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
     const double bvc = c1s * (compression + 1.0);
-    double p_new = pressure(e_new, bvc);
+    double p_new = pressure(e_new, bvc, TF_PN1_CUT, TF_PN1_MIN);
     const double vv_bvc = (vnewc * vnewc) * bvc;
     double q_tilde = 0.0;
     if (compress) {
       const double ssc = fma(c1s, e_new, vv_bvc * p_new) * inv_rho0;
-      q_tilde = fma(ssc_sqrt(ssc), qlin, qquad);
+      q_tilde = fma(tiny_sqrt(ssc, TF_S2_TINY), qlin, qquad);
     }
     e_new = e_new - ((fma(7.0, pq_old, -8.0 * (pHalfStep + q_new)) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
-    if (abs_lt(e_new, prm.e_cut)) e_new = 0.0;
-    if (e_new < prm.emin) e_new = prm.emin;
-    p_new = pressure(e_new, bvc);
+    if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E3_CUT; }
+    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
+    p_new = pressure(e_new, bvc, TF_PN2_CUT, TF_PN2_MIN);
     // the last q evaluation and the sound speed share one expression
-    const double ss_new = ssc_sqrt(fma(c1s, e_new, vv_bvc * p_new) * inv_rho0);
+    const double ss_new = tiny_sqrt(fma(c1s, e_new, vv_bvc * p_new) * inv_rho0, TF_SS_TINY);
     if (compress) {
       q_new = fma(ss_new, qlin, qquad);
-      if (abs_lt(q_new, prm.q_cut)) q_new = 0.0;
+      if (abs_lt(q_new, prm.q_cut)) { q_new = 0.0; if (TAPE) fl |= TF_Q_CUT; }
     }
     d.p[i] = p_new;
     d.e[i] = e_new;
@@ -608,19 +624,25 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     // ---- updateVolumesForElems, src/domain.jl:2912-2930 ----
     double tmpV = vnew;
-    if (abs_lt(tmpV - 1.0, prm.v_cut)) tmpV = 1.0;
+    if (abs_lt(tmpV - 1.0, prm.v_cut)) { tmpV = 1.0; if (TAPE) fl |= TF_V_SNAP; }
     d.v[i] = tmpV;
     if (le_zero(tmpV)) err |= ST_UPDATE;
 
     // ---- Courant and hydro constraints, src/domain.jl:2964-3054 ----
+    double dtc = __longlong_as_double((long long)kInfBits), dth = dtc;
     if (vdov != 0.0) {
       const double arealg = LDG(&d.arealg[i]);
       double dtf = ss_new * ss_new;
       if (vdov < 0.0) dtf = fma(((64.0 * prm.qqc) * prm.qqc) * (arealg * arealg), vdov * vdov, dtf);
-      const double dtc = arealg * rsqrt(dtf);
-      const double dth = prm.dvovmax / (fabs(vdov) + 1.e-20);
+      dtc = arealg * rsqrt(dtf);
+      dth = prm.dvovmax / (fabs(vdov) + 1.e-20);
       courant = (unsigned long long)__double_as_longlong(dtc);
       hydro = (unsigned long long)__double_as_longlong(dth);
+    }
+    if (TAPE) {
+      d.tapeFlags[i] |= fl;  // k_kinematics stored the face bits of this cycle
+      d.tapeDtc[i] = dtc;
+      d.tapeDth[i] = dth;
     }
     if (err) atomicOr(&st->status, err);
   }
@@ -686,9 +708,10 @@ void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& 
 void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
   const int bs = t.kin;
   const int grid = (d.E + bs - 1) / bs;
-  if (d.elemInst) k_kinematics<false, true><<<grid, bs, 0, s>>>(d, prm);
-  else if (aux) k_kinematics<true, false><<<grid, bs, 0, s>>>(d, prm);
-  else k_kinematics<false, false><<<grid, bs, 0, s>>>(d, prm);
+  if (d.elemInst) k_kinematics<false, true, false><<<grid, bs, 0, s>>>(d, prm);
+  else if (d.tapeFlags) k_kinematics<false, false, true><<<grid, bs, 0, s>>>(d, prm);
+  else if (aux) k_kinematics<true, false, false><<<grid, bs, 0, s>>>(d, prm);
+  else k_kinematics<false, false, false><<<grid, bs, 0, s>>>(d, prm);
 }
 
 void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
@@ -696,14 +719,17 @@ void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuni
   const int grid = (d.E + bs - 1) / bs;
   const bool fix = (d.mode & 4) != 0;
   if (d.elemInst) {
-    if (fix) k_material<4, false, true><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<0, false, true><<<grid, bs, 0, s>>>(d, prm);
+    if (fix) k_material<4, false, true, false><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<0, false, true, false><<<grid, bs, 0, s>>>(d, prm);
+  } else if (d.tapeFlags) {
+    if (fix) k_material<4, false, false, true><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<0, false, false, true><<<grid, bs, 0, s>>>(d, prm);
   } else if (fix) {
-    if (aux) k_material<4, true, false><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<4, false, false><<<grid, bs, 0, s>>>(d, prm);
+    if (aux) k_material<4, true, false, false><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<4, false, false, false><<<grid, bs, 0, s>>>(d, prm);
   } else {
-    if (aux) k_material<0, true, false><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<0, false, false><<<grid, bs, 0, s>>>(d, prm);
+    if (aux) k_material<0, true, false, false><<<grid, bs, 0, s>>>(d, prm);
+    else k_material<0, false, false, false><<<grid, bs, 0, s>>>(d, prm);
   }
 }
 

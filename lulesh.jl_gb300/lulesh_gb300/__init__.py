@@ -20,7 +20,8 @@ import numpy as np
 __all__ = [
     "LuleshProblem", "Domain", "timeIncrement", "lagrangeLeapFrog", "run",
     "verifyAndWriteFinalOutput", "LuleshError", "load_library", "library_path",
-    "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2",
+    "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2", "Ensemble", "sedov_instances",
+    "Adjoint", "STATE_FIELDS",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -107,6 +108,13 @@ class Tuning(ctypes.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class AdjResult(ctypes.Structure):
+    """lulesh_adj_result."""
+    _fields_ = [("loss", ctypes.c_double), ("grad_hgcoef", ctypes.c_double),
+                ("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
+                ("cycles", ctypes.c_int64), ("checkpoints", ctypes.c_int32), ("status", ctypes.c_int32)]
+
+
 _LIB = None
 
 
@@ -165,6 +173,13 @@ def load_library():
         "lulesh_ens_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
         "lulesh_ens_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
         "lulesh_ens_autotune": (ctypes.c_int, [P, i32, ctypes.POINTER(Tuning)]),
+        "lulesh_adj_create": (ctypes.c_int, [P, dbl, i32, ctypes.POINTER(P)]),
+        "lulesh_adj_destroy": (ctypes.c_int, [P]),
+        "lulesh_adj_set_seed": (ctypes.c_int, [P, i32, P, i64]),
+        "lulesh_adj_clear_seeds": (ctypes.c_int, [P]),
+        "lulesh_adj_loss": (ctypes.c_int, [P, ctypes.POINTER(dbl)]),
+        "lulesh_adj_gradient": (ctypes.c_int, [P, i64, ctypes.POINTER(AdjResult)]),
+        "lulesh_adj_get_gradient": (ctypes.c_int, [P, i32, P, i64]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -472,3 +487,71 @@ class Ensemble:
         t = Tuning()
         _check(self._L.lulesh_ens_autotune(self._h, int(cycles), ctypes.byref(t)), "autotune")
         return t.as_dict()
+
+
+# The state a cycle maps to the next one (node then element fields).
+STATE_FIELDS = ("x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss")
+
+
+class Adjoint:
+    """Reverse-mode gradient of a run of a Domain (lulesh_adj_* of the C ABI).
+
+    The reference differentiates `lagrangeLeapFrog` with Enzyme
+    (examples/benchmark.jl:48-52, 85-86: `autodiff(lagrangeLeapFrog,
+    Duplicated(domain, shadow))`); this is a hand-written adjoint of whole runs.
+    The default objective after the run is the energy within `radius` of the
+    origin (element internal energy times mass, plus nodal kinetic energy,
+    masked by the initial mesh); `set_seed` replaces it with linear weights on
+    state fields. `gradient(n)` advances the domain by up to n cycles and
+    returns the objective; `grad(name)` is then the gradient w.r.t. that
+    field's value before the run and `result.grad_hgcoef` w.r.t. hgcoef.
+    """
+
+    def __init__(self, domain, radius=0.3, checkpoint_every=20):
+        L = load_library()
+        h = ctypes.c_void_p()
+        _check(L.lulesh_adj_create(domain.handle, float(radius), int(checkpoint_every), ctypes.byref(h)),
+               "adjoint")
+        self._L, self._h, self.domain = L, h, domain
+        self.result = None
+
+    def close(self):
+        if self._h:
+            self._L.lulesh_adj_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_seed(self, name, weights):
+        fid, _ = FIELDS[name]
+        w = np.ascontiguousarray(weights, dtype=np.float64)
+        _check(self._L.lulesh_adj_set_seed(self._h, fid, w.ctypes.data_as(ctypes.c_void_p), w.size),
+               f"seed {name}")
+
+    def clear_seeds(self):
+        _check(self._L.lulesh_adj_clear_seeds(self._h), "clear seeds")
+
+    def loss(self):
+        x = ctypes.c_double()
+        _check(self._L.lulesh_adj_loss(self._h, ctypes.byref(x)), "loss")
+        return x.value
+
+    def gradient(self, num_cycles):
+        r = AdjResult()
+        rc = self._L.lulesh_adj_gradient(self._h, int(num_cycles), ctypes.byref(r))
+        if rc:
+            _raise_step(self.domain, rc)
+        self.result = r
+        return r.loss
+
+    def grad(self, name):
+        fid, _ = FIELDS[name]
+        n = self.domain.numNode if fid >= 32 else self.domain.numElem
+        out = np.empty(n)
+        _check(self._L.lulesh_adj_get_gradient(self._h, fid, out.ctypes.data_as(ctypes.c_void_p), n),
+               f"gradient {name}")
+        return out

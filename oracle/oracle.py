@@ -163,3 +163,101 @@ class OracleDomain:
         out = (ctypes.c_double * 3)()
         self.L.ora_symmetry(self.h, out)
         return tuple(out)
+
+
+def load_dual():
+    """The dual-number (forward-mode) build of the oracle."""
+    if "dual" in _libs:
+        return _libs["dual"]
+    path = os.path.join(BUILD, "liblulesh_oracle_dual.so")
+    if not os.path.exists(path):
+        build()
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    D = ctypes.POINTER(ctypes.c_double)
+    L.ord_create.restype = P
+    L.ord_create.argtypes = [ctypes.c_int] * 5 + [ctypes.c_ulonglong]
+    L.ord_destroy.argtypes = [P]
+    L.ord_destroy.restype = None
+    for f in ["ord_num_elem", "ord_num_node", "ord_cycle"]:
+        getattr(L, f).argtypes = [P]
+        getattr(L, f).restype = ctypes.c_longlong
+    L.ord_set_cycle.argtypes = [P, ctypes.c_longlong]
+    L.ord_set_cycle.restype = None
+    L.ord_set_field.argtypes = [P, ctypes.c_char_p, D, D, ctypes.c_longlong]
+    L.ord_get_field.argtypes = [P, ctypes.c_char_p, D, D, ctypes.c_longlong]
+    L.ord_set_scalar.argtypes = [P, ctypes.c_char_p, ctypes.c_double, ctypes.c_double]
+    L.ord_get_scalar.argtypes = [P, ctypes.c_char_p, D, D]
+    for f in ["ord_time_increment", "ord_lagrange_leapfrog"]:
+        getattr(L, f).argtypes = [P]
+        getattr(L, f).restype = ctypes.c_int
+    L.ord_cycles.argtypes = [P, ctypes.c_longlong]
+    L.ord_cycles.restype = ctypes.c_int
+    _libs["dual"] = L
+    return L
+
+
+def _dptr(a):
+    return None if a is None else a.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+
+
+class DualDomain:
+    """An oracle problem over dual numbers: every value carries one tangent,
+    so running cycles gives the exact Jacobian-vector product of the run."""
+
+    def __init__(self, nx, nr=11, balance=1, cost=1, mode=FAITHFUL, seed=0):
+        self.L = load_dual()
+        self.h = self.L.ord_create(int(nx), int(nr), int(balance), int(cost), int(mode), int(seed))
+        if not self.h:
+            raise ValueError("bad oracle parameters")
+        self.ne = int(self.L.ord_num_elem(self.h))
+        self.nn = int(self.L.ord_num_node(self.h))
+
+    def close(self):
+        if self.h:
+            self.L.ord_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _len(self, name):
+        node = name in ("x", "y", "z", "xd", "yd", "zd", "xdd", "ydd", "zdd", "fx", "fy", "fz", "nodalMass")
+        return self.nn if node else self.ne
+
+    def set_field(self, name, values=None, tangents=None):
+        n = self._len(name)
+        v = None if values is None else np.ascontiguousarray(values, dtype=np.float64)
+        t = None if tangents is None else np.ascontiguousarray(tangents, dtype=np.float64)
+        if self.L.ord_set_field(self.h, name.encode(), _dptr(v), _dptr(t), n) != 0:
+            raise KeyError(name)
+
+    def field(self, name):
+        """(values, tangents) of a field."""
+        n = self._len(name)
+        v = np.empty(n)
+        t = np.empty(n)
+        if self.L.ord_get_field(self.h, name.encode(), _dptr(v), _dptr(t), n) != 0:
+            raise KeyError(name)
+        return v, t
+
+    def get(self, name):
+        if name == "cycle":
+            return int(self.L.ord_cycle(self.h)), 0.0
+        v, t = ctypes.c_double(), ctypes.c_double()
+        if self.L.ord_get_scalar(self.h, name.encode(), ctypes.byref(v), ctypes.byref(t)) != 0:
+            raise KeyError(name)
+        return v.value, t.value
+
+    def set(self, name, value, tangent=0.0):
+        if name == "cycle":
+            self.L.ord_set_cycle(self.h, int(value))
+            return
+        if self.L.ord_set_scalar(self.h, name.encode(), float(value), float(tangent)) != 0:
+            raise KeyError(name)
+
+    def cycles(self, n):
+        return self.L.ord_cycles(self.h, int(n))

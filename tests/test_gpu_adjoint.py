@@ -1,0 +1,211 @@
+"""The reverse-mode adjoint (lulesh_adj_*) against the dual-number oracle and
+against central finite differences of the GPU run itself.
+
+Checks:
+  * block dot products: for every (output field, input field) pair of one
+    cycle, <w, J v> from the dual oracle equals <J^T w, v> from the adjoint
+    (relative to sum |w||Jv|, bar 1e-8); plus the hgcoef column;
+  * a 30-cycle run with checkpoints every 7 cycles (a partial last segment):
+    the energy objective's gradient w.r.t. e and hgcoef against the dual
+    oracle, same bar;
+  * gradients independent of the checkpoint interval, the domain left at the
+    final state of a plain run, loss equal to the objective of that state;
+  * central finite differences (step 1e-6 relative) of the GPU run on a few
+    directions.
+The derivative is that of the branches the run takes; the inputs are chosen so
+that no cut-off sits at its threshold (a positive background energy).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STATE = ["x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"]
+SCAL = ["time", "deltatime", "dtcourant", "dthydro"]
+
+
+def snapshot(g):
+    return {f: g.field(f) for f in STATE}, {s: getattr(g, s) for s in SCAL + ["cycle", "hgcoef"]}
+
+
+def restore(g, snap):
+    fields, scal = snap
+    for f, v in fields.items():
+        g.set_field(f, v)
+    for s, v in scal.items():
+        setattr(g, s, v)
+
+
+def dual_from(oracle_mod, snap, nx, mode):
+    fields, scal = snap
+    d = oracle_mod.DualDomain(nx, mode=mode)
+    for f, v in fields.items():
+        d.set_field(f, v, np.zeros_like(v))
+    for s in SCAL + ["hgcoef"]:
+        d.set(s, scal[s], 0.0)
+    d.set("cycle", scal["cycle"])
+    return d
+
+
+def developed(L, nx, mode, cycles, seed):
+    """A GPU domain with a positive background energy, run `cycles` cycles."""
+    g = L.Domain(L.LuleshProblem(nx=nx, mode=mode))
+    rng = np.random.default_rng(seed)
+    g.e = g.e + 1e4 * (1.0 + rng.random(g.numElem))
+    if cycles:
+        L.run(g, cycles)
+    return g
+
+
+def energy_weights(nx, radius, elem_mass, nodal_mass):
+    h = 1.125 / nx
+    c = (np.arange(nx) + 0.5) * h
+    zc, yc, xc = np.meshgrid(c, c, c, indexing="ij")
+    we = np.where((xc ** 2 + yc ** 2 + zc ** 2).ravel() < radius ** 2, elem_mass, 0.0)
+    p = np.arange(nx + 1) * h
+    zn, yn, xn = np.meshgrid(p, p, p, indexing="ij")
+    wn = np.where((xn ** 2 + yn ** 2 + zn ** 2).ravel() < radius ** 2, nodal_mass, 0.0)
+    return we, wn
+
+
+def close(a, b, scale, tol):
+    return abs(a - b) <= tol * max(scale, 1e-300)
+
+
+@pytest.mark.parametrize("mode", [0, 7])
+def test_one_cycle_block_dot_products(gpu_lib, oracle_mod, mode):
+    L = gpu_lib
+    nx = 6
+    g = developed(L, nx, mode, 5, 0xA1)
+    snap = snapshot(g)
+    rng = np.random.default_rng(0xA2)
+    fields = snap[0]
+    w = {f: rng.standard_normal(fields[f].size) for f in STATE}
+    scale = {f: np.mean(np.abs(fields[f])) + 1e-3 for f in STATE}
+    v = {f: rng.standard_normal(fields[f].size) * scale[f] for f in STATE}
+    v_hg = 0.3
+    # dual oracle: one run per input direction gives every output's tangent
+    jv = {}
+    for fi in STATE + ["hgcoef"]:
+        d = dual_from(oracle_mod, snap, nx, mode)
+        if fi == "hgcoef":
+            d.set("hgcoef", snap[1]["hgcoef"], v_hg)
+        else:
+            d.set_field(fi, fields[fi], v[fi])
+        assert d.cycles(1) == 0
+        jv[fi] = {fo: d.field(fo)[1] for fo in STATE}
+    adj = L.Adjoint(g, checkpoint_every=1)
+    bad = []
+    for fo in STATE:
+        restore(g, snap)
+        adj.clear_seeds()
+        adj.set_seed(fo, w[fo])
+        adj.gradient(1)
+        assert adj.result.cycles == 1
+        for fi in STATE + ["hgcoef"]:
+            a = float(np.dot(w[fo], jv[fi][fo]))
+            a_scale = float(np.dot(np.abs(w[fo]), np.abs(jv[fi][fo])))
+            if fi == "hgcoef":
+                b = adj.result.grad_hgcoef * v_hg
+                b_scale = abs(b)
+            else:
+                gi = adj.grad(fi)
+                b = float(np.dot(gi, v[fi]))
+                b_scale = float(np.dot(np.abs(gi), np.abs(v[fi])))
+            if not close(a, b, max(a_scale, b_scale), 1e-8):
+                bad.append((fo, fi, a, b, max(a_scale, b_scale)))
+    adj.close()
+    assert not bad, bad
+
+
+@pytest.mark.parametrize("mode", [0, 7])
+def test_run_gradient_matches_dual_oracle(gpu_lib, oracle_mod, mode):
+    L = gpu_lib
+    nx, cycles, radius = 8, 30, 0.3
+    g = developed(L, nx, mode, 0, 0xB1)
+    snap = snapshot(g)
+    rng = np.random.default_rng(0xB2)
+    de = rng.standard_normal(g.numElem) * snap[0]["e"]
+    dhg = 0.2
+    adj = L.Adjoint(g, radius=radius, checkpoint_every=7)
+    loss = adj.gradient(cycles)
+    assert adj.result.cycles == cycles and adj.result.checkpoints == 5
+    ge, ghg = adj.grad("e"), adj.result.grad_hgcoef
+    d = dual_from(oracle_mod, snap, nx, mode)
+    d.set_field("e", snap[0]["e"], de)
+    d.set("hgcoef", snap[1]["hgcoef"], dhg)
+    assert d.cycles(cycles) == 0
+    we, wn = energy_weights(nx, radius, d.field("elemMass")[0], d.field("nodalMass")[0])
+    e, te = d.field("e")
+    ref_loss = float(np.dot(we, e))
+    jvp = float(np.dot(we, te))
+    jscale = float(np.dot(np.abs(we), np.abs(te)))
+    for c in ("xd", "yd", "zd"):
+        u, tu = d.field(c)
+        ref_loss += 0.5 * float(np.dot(wn, u * u))
+        jvp += float(np.dot(wn, u * tu))
+        jscale += float(np.dot(np.abs(wn), np.abs(u * tu)))
+    assert loss == pytest.approx(ref_loss, rel=1e-10)
+    vjp = float(np.dot(ge, de)) + ghg * dhg
+    assert close(jvp, vjp, jscale, 1e-8), (jvp, vjp, jscale)
+    adj.close()
+
+
+def test_checkpoint_interval_and_final_state(gpu_lib):
+    L = gpu_lib
+    nx, cycles = 8, 23
+    g = developed(L, nx, 0, 0, 0xC1)
+    snap = snapshot(g)
+    ref = L.Domain(L.LuleshProblem(nx=nx))
+    restore(ref, snap)
+    for _ in range(cycles):
+        L.timeIncrement(ref)
+        L.lagrangeLeapFrog(ref)
+    grads = []
+    for k in (1, 5, 23, 40):
+        restore(g, snap)
+        adj = L.Adjoint(g, checkpoint_every=k)
+        loss = adj.gradient(cycles)
+        grads.append((loss, adj.result.grad_hgcoef, {f: adj.grad(f) for f in STATE}))
+        for f in STATE:
+            assert np.array_equal(g.field(f), ref.field(f)), (k, f)
+        for s in SCAL + ["cycle"]:
+            assert getattr(g, s) == getattr(ref, s), (k, s)
+        assert loss == adj.loss()
+        adj.close()
+    for other in grads[1:]:
+        assert other[0] == grads[0][0] and other[1] == grads[0][1]
+        for f in STATE:
+            assert np.array_equal(other[2][f], grads[0][2][f]), f
+
+
+def test_gradient_matches_central_fd(gpu_lib):
+    L = gpu_lib
+    nx, cycles, h = 12, 40, 1e-6
+    g = L.Domain(L.LuleshProblem(nx=nx))
+    rng = np.random.default_rng(0xC5)
+    e0 = g.e
+    e0[1:] = rng.uniform(0.0, 1e-3, g.numElem - 1) + 1e-2
+    g.e = e0
+    snap = snapshot(g)
+    adj = L.Adjoint(g, radius=0.3, checkpoint_every=10)
+    adj.gradient(cycles)
+    ge, ghg = adj.grad("e"), adj.result.grad_hgcoef
+    hg0 = snap[1]["hgcoef"]
+
+    def loss_at(e, hg):
+        restore(g, snap)
+        g.e = e
+        g.hgcoef = hg
+        L.run(g, cycles)
+        assert g.cycle == cycles
+        return adj.loss()
+
+    drng = np.random.default_rng(0xF0)
+    for k in range(4):
+        de = drng.standard_normal(g.numElem) * e0
+        dhg = (0.5 if k == 3 else 0.0) * hg0
+        fd = (loss_at(e0 + h * de, hg0 + h * dhg) - loss_at(e0 - h * de, hg0 - h * dhg)) / (2 * h)
+        an = float(np.dot(ge, de)) + ghg * dhg
+        assert an == pytest.approx(fd, rel=2e-6, abs=1e-9 * abs(adj.result.loss)), (k, an, fd)
+    adj.close()
