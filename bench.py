@@ -20,6 +20,8 @@ import sys
 import threading
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 for _p in (os.path.join(ROOT, "lulesh.jl_gb300"), os.path.join(ROOT, "oracle")):
     if _p not in sys.path:
@@ -240,6 +242,85 @@ def ensemble_leg(L, torch, dev, n, cycles):
             "tuning": tuning}
 
 
+def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
+    """Config C5: gradient of the energy within r < 0.3 of the origin after
+    `cycles` cycles of an nx^3 Sedov problem (origin energy the default, the
+    others U[0, 1e-3] from seed 0xC5) w.r.t. the initial e field and hgcoef,
+    with checkpoints every `every` cycles. Reports its cost against the
+    forward run of the same cycles and its agreement with central finite
+    differences of the GPU run on `dirs` directions (seed 0xF0, step 1e-6
+    relative: d_i = N(0,1) * e0_i, and N(0,1) * hgcoef)."""
+    g = L.Domain(L.LuleshProblem(nx=nx, nr=11, device=dev))
+    rng = np.random.default_rng(0xC5)
+    e0 = g.field("e")
+    e0[1:] = rng.uniform(0.0, 1e-3, g.numElem - 1)
+    g.set_field("e", e0)
+    snap = ({f: g.field(f) for f in STATE_FIELDS},
+            {s: getattr(g, s) for s in ("time", "deltatime", "dtcourant", "dthydro", "cycle", "hgcoef")})
+
+    def restore(e=None, hg=None):
+        for f, v in snap[0].items():
+            g.set_field(f, v)
+        for k, v in snap[1].items():
+            setattr(g, k, v)
+        if e is not None:
+            g.set_field("e", e)
+        if hg is not None:
+            g.hgcoef = hg
+
+    adj = L.Adjoint(g, radius=0.3, checkpoint_every=every)
+    restore()
+    L.run(g, cycles)  # warm-up (graph capture)
+    fwd = []
+    for _ in range(3):
+        restore()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        L.run(g, cycles)
+        torch.cuda.synchronize(dev)
+        fwd.append(time.perf_counter() - t0)
+    fwd_s = min(fwd)
+    restore()
+    adj.gradient(cycles)  # warm-up (checkpoint buffers)
+    times = []
+    for _ in range(2):
+        restore()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        loss = adj.gradient(cycles)
+        torch.cuda.synchronize(dev)
+        times.append(time.perf_counter() - t0)
+    adj_s = min(times)
+    res = adj.result
+    ge, ghg = adj.grad("e"), res.grad_hgcoef
+    hg0 = snap[1]["hgcoef"]
+
+    def loss_at(e, hg):
+        restore(e, hg)
+        L.run(g, cycles)
+        return adj.loss()
+
+    drng = np.random.default_rng(0xF0)
+    h = 1e-6
+    errs = []
+    for _ in range(dirs):
+        de = drng.standard_normal(g.numElem) * e0
+        dhg = drng.standard_normal() * hg0
+        fd = (loss_at(e0 + h * de, hg0 + h * dhg) - loss_at(e0 - h * de, hg0 - h * dhg)) / (2 * h)
+        an = float(np.dot(ge, de)) + ghg * dhg
+        errs.append(abs(an - fd) / max(abs(fd), 1e-12 * abs(loss)))
+    adj.close()
+    g.close()
+    return {"config": f"Sedov {nx}^3, {cycles} cycles, energy within r < 0.3, d/d(e0, hgcoef), "
+                      f"checkpoints every {every} cycles, FP64",
+            "nx": nx, "cycles": int(res.cycles), "checkpoints": int(res.checkpoints),
+            "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
+            "adjoint_sweep_ms": {"checkpointed_forward": res.forward_ms, "reverse": res.reverse_ms},
+            "loss": loss, "grad_hgcoef": ghg, "grad_e_origin": float(ge[0]),
+            "fd": {"directions": dirs, "step": h, "max_rel_err": max(errs),
+                   "median_rel_err": float(np.median(errs))}}
+
+
 def run_ours(args):
     world, rank, local = _dist()
     import torch
@@ -337,6 +418,12 @@ def run_ours(args):
         g.close()
         ensemble = ensemble_leg(L, torch, dev, args.ens_instances, args.ens_cycles)
 
+    adjoint = None
+    if not args.no_adjoint:
+        if ensemble is None:
+            g.close()
+        adjoint = adjoint_leg(L, torch, dev, args.adj_nx, args.adj_cycles, args.adj_every, args.adj_dirs)
+
     cpu = None
     if world == 1 and not args.no_cpu:
         rate, used, n, dt = cpu_oracle_rate(args.nx, args.cpu_seconds)
@@ -357,7 +444,7 @@ def run_ours(args):
             "kernel_ms_per_cycle": {k: v / cycles for k, v in ktimes.items()},
             "dominant_kernel": dominant,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
-            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble}
+            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint}
     print(json.dumps(line), flush=True)
     g.close()
     return 0
@@ -377,6 +464,11 @@ def main():
     ap.add_argument("--no-ensemble", action="store_true", help="skip the batched-ensemble leg")
     ap.add_argument("--ens-instances", type=int, default=256)
     ap.add_argument("--ens-cycles", type=int, default=300)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--adj-nx", type=int, default=48)
+    ap.add_argument("--adj-cycles", type=int, default=200)
+    ap.add_argument("--adj-every", type=int, default=20)
+    ap.add_argument("--adj-dirs", type=int, default=16)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be at least 3")

@@ -10,8 +10,11 @@
 //      kinematics outputs, accelerations, branch flags, dt candidates), then
 //      transpose the cycles in reverse with the ka_* kernels. The dt control
 //      (timeIncrement!, the Courant and hydro minima) is transposed on the
-//      host from the recorded scalars: the minima pass their adjoint to the
+//      device from the recorded scalars: the minima pass their adjoint to the
 //      element that attained them.
+// The forward sweep runs as lulesh_run does (CUDA graphs, dt on the device);
+// the recompute and the transpose of a segment are queued without any host
+// synchronisation.
 // The handle is left at its final state. Every derivative is that of the
 // branches the forward run took.
 #include <cuda_runtime.h>
@@ -58,14 +61,6 @@ struct CycleTape {
   double *dtc, *dth;
 };
 
-struct ScalarRec {
-  double time_prev, dt_prev, dtc_in, dth_in;
-  long long cycle_prev;
-  double dt, time;
-  bool active_c, active_h;
-  int argmin_c, argmin_h;
-};
-
 struct Scalars5 {
   double time, dt, dtc, dth;
   long long cycle;
@@ -88,15 +83,18 @@ struct lulesh_adjoint {
   std::vector<CycleTape> tape;   // K cycles
   std::vector<StateBuf> ckpts;   // segment start states
   std::vector<Scalars5> ckpt_scalars;
+  std::vector<int> seg_len;      // cycles of each segment
+  DevState* ckpt_st = nullptr;   // device: step state at each checkpoint
+  int ckpt_st_cap = 0;
   StateBuf final_state{};
   double *we = nullptr, *wn = nullptr;  // objective weights
   int *nbStart = nullptr, *nbList = nullptr;
   double *fx_s = nullptr, *fy_s = nullptr, *fz_s = nullptr;  // force scratch of taped cycles
   AdjDev ad{};
-  double* scal = nullptr;  // device: sums of partials
-  int* argmin = nullptr;
+  double* scal = nullptr;       // device: sums of partials (objective)
+  CycleRec* rec = nullptr;      // device: K cycle records of the current segment
+  AdjScal* dsc = nullptr;       // device: carried scalar adjoints
   std::map<int32_t, double*> seeds;  // linear-objective weights per state field
-  std::vector<ScalarRec> rec;
 };
 
 static int dmalloc(lulesh_adjoint* a, void** p, size_t bytes) {
@@ -117,19 +115,22 @@ static int alloc_state(lulesh_adjoint* a, StateBuf& s) {
   return LULESH_OK;
 }
 
-static int copy_state_from_domain(lulesh_adjoint* a, StateBuf& s) {
-  for (int k = 0; k < kStateFields; ++k)
-    ACK(cudaMemcpyAsync(s.f[k], *state_ptr(a->dom->dd, k), (k < 6 ? a->N : a->E) * sizeof(double),
-                        cudaMemcpyDeviceToDevice, a->dom->stream));
-  return LULESH_OK;
+static StateSet domain_set(lulesh_adjoint* a) {
+  StateSet t;
+  for (int k = 0; k < kStateFields; ++k) t.f[k] = *state_ptr(a->dom->dd, k);
+  return t;
 }
-
-static int copy_state_to_domain(lulesh_adjoint* a, const StateBuf& s) {
-  for (int k = 0; k < kStateFields; ++k)
-    ACK(cudaMemcpyAsync(*state_ptr(a->dom->dd, k), s.f[k], (k < 6 ? a->N : a->E) * sizeof(double),
-                        cudaMemcpyDeviceToDevice, a->dom->stream));
-  return LULESH_OK;
+static StateSet buf_set(const StateBuf& b) {
+  StateSet t;
+  for (int k = 0; k < kStateFields; ++k) t.f[k] = b.f[k];
+  return t;
 }
+static void copy_state(lulesh_adjoint* a, const StateSet& src, const StateSet& dst) {
+  const int n = std::max(a->E, a->N);
+  ka_copy_state<<<(n + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, a->dom->stream>>>(src, dst, a->E, a->N);
+}
+static void copy_state_from_domain(lulesh_adjoint* a, StateBuf& s) { copy_state(a, domain_set(a), buf_set(s)); }
+static void copy_state_to_domain(lulesh_adjoint* a, const StateBuf& s) { copy_state(a, buf_set(s), domain_set(a)); }
 
 static Scalars5 get_scalars(const lulesh_domain* d) {
   return Scalars5{d->sc[LULESH_S_TIME], d->sc[LULESH_S_DELTATIME], d->sc[LULESH_S_DTCOURANT],
@@ -143,112 +144,30 @@ static void set_scalars(lulesh_domain* d, const Scalars5& s) {
   d->sc[LULESH_S_CYCLE] = (double)s.cycle;
 }
 
-// One cycle driven from the host (timeIncrement! on the host, the step on the
-// device) exactly as lulesh_time_increment + lulesh_lagrange_leapfrog; with a
-// tape, the kinematics outputs, accelerations, flags and dt candidates of the
-// cycle go to it and the arg-min elements are found.
-static int forward_cycle(lulesh_adjoint* a, const CycleTape* tp, ScalarRec* r) {
+// One taped cycle, queued on the stream: timeIncrement! on the device
+// (recorded), the step kernels with the cycle's kinematics outputs,
+// accelerations, branch flags and dt candidates going to the tape, then the
+// arg-min elements of the Courant and hydro minima.
+static void tape_cycle(lulesh_adjoint* a, const CycleTape& tp, CycleRec* rec) {
   lulesh_domain* d = a->dom;
   const Params prm = make_params(d);
   cudaStream_t s = d->stream;
-  ScalarRec rec{};
-  rec.time_prev = d->sc[LULESH_S_TIME];
-  rec.dt_prev = d->sc[LULESH_S_DELTATIME];
-  rec.dtc_in = d->sc[LULESH_S_DTCOURANT];
-  rec.dth_in = d->sc[LULESH_S_DTHYDRO];
-  rec.cycle_prev = (long long)d->sc[LULESH_S_CYCLE];
-  {
-    double time = rec.time_prev, dt = rec.dt_prev;
-    long long cycle = rec.cycle_prev;
-    time_increment(time, dt, cycle, rec.dtc_in, rec.dth_in, prm);
-    d->sc[LULESH_S_TIME] = time;
-    d->sc[LULESH_S_DELTATIME] = dt;
-    d->sc[LULESH_S_CYCLE] = (double)cycle;
-    rec.dt = dt;
-    rec.time = time;
-  }
-  state_to_device_mirror(d);
-  ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
+  ka_tape_begin<<<1, 1, 0, s>>>(d->dd.st, rec, prm);
   DevDomain td = d->dd;
-  bool aux = d->params.keep_aux != 0;
-  if (tp) {
-    td.vnew = tp->vnew; td.delv = tp->delv; td.arealg = tp->arealg; td.vdov = tp->vdov;
-    td.delv_xi = tp->dv[0]; td.delv_eta = tp->dv[1]; td.delv_zeta = tp->dv[2];
-    td.delx_xi = tp->dx[0]; td.delx_eta = tp->dx[1]; td.delx_zeta = tp->dx[2];
-    td.xdd = tp->ax; td.ydd = tp->ay; td.zdd = tp->az;
-    td.fx = a->fx_s; td.fy = a->fy_s; td.fz = a->fz_s;
-    td.tapeFlags = tp->flags; td.tapeDtc = tp->dtc; td.tapeDth = tp->dth;
-    aux = true;  // the node kernel stores the accelerations
-  }
+  td.vnew = tp.vnew; td.delv = tp.delv; td.arealg = tp.arealg; td.vdov = tp.vdov;
+  td.delv_xi = tp.dv[0]; td.delv_eta = tp.dv[1]; td.delv_zeta = tp.dv[2];
+  td.delx_xi = tp.dx[0]; td.delx_eta = tp.dx[1]; td.delx_zeta = tp.dx[2];
+  td.xdd = tp.ax; td.ydd = tp.ay; td.zdd = tp.az;
+  td.fx = a->fx_s; td.fy = a->fy_s; td.fz = a->fz_s;
+  td.tapeFlags = tp.flags; td.tapeDtc = tp.dtc; td.tapeDth = tp.dth;
   launch_force(td, prm, d->tuning, s);
-  launch_node(td, prm, aux, d->tuning, s);
+  launch_node(td, prm, true, d->tuning, s);  // aux: the node kernel stores the accelerations
   launch_kinematics(td, prm, false, d->tuning, s);
   launch_material(td, prm, false, d->tuning, s);
-  ACK(cudaGetLastError());
-  ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
-  ACK(cudaStreamSynchronize(s));
-  const unsigned long long accc = d->hst->acc_courant, acch = d->hst->acc_hydro;
-  state_from_device_mirror(d);
-  if (d->status) return d->status;
-  rec.active_c = accc != kInfBits;
-  rec.active_h = acch != kInfBits;
-  rec.argmin_c = rec.argmin_h = -1;
-  if (tp) {
-    const int grid = (a->E + kAdjBlock - 1) / kAdjBlock;
-    int init[2] = {INT_MAX, INT_MAX};
-    ACK(cudaMemcpyAsync(a->argmin, init, sizeof(init), cudaMemcpyHostToDevice, s));
-    if (rec.active_c) ka_argmin<<<grid, kAdjBlock, 0, s>>>(tp->dtc, a->E, accc, a->argmin);
-    if (rec.active_h) ka_argmin<<<grid, kAdjBlock, 0, s>>>(tp->dth, a->E, acch, a->argmin + 1);
-    int got[2];
-    ACK(cudaMemcpyAsync(got, a->argmin, sizeof(got), cudaMemcpyDeviceToHost, s));
-    ACK(cudaStreamSynchronize(s));
-    rec.argmin_c = rec.active_c ? got[0] : -1;
-    rec.argmin_h = rec.active_h ? got[1] : -1;
-  }
-  if (r) *r = rec;
-  return LULESH_OK;
-}
-
-// Transpose of timeIncrement! (src/domain.jl:920-961) for the recorded
-// inputs: Ldt is the adjoint of the new deltatime; adds to the adjoints of
-// the previous time, deltatime, dtcourant and dthydro along the branch taken.
-static void time_increment_reverse(const ScalarRec& r, const Params& prm, double Ldt, double& Ltime,
-                                   double& Ldt_prev, double& Ldtc, double& Ldth) {
-  double targetdt = prm.stoptime - r.time_prev;
-  double dt_pre = r.dt_prev;
-  int which = 0, rb = 0;
-  bool mb = false;
-  const bool adaptive = prm.dtfixed <= 0.0 && r.cycle_prev != 0;
-  if (adaptive) {
-    const double olddt = r.dt_prev;
-    double gnewdt = (double)INFINITY;
-    if (r.dtc_in < gnewdt) { gnewdt = r.dtc_in / 2.0; which = 1; }
-    if (r.dth_in < gnewdt) { gnewdt = r.dth_in * 2.0 / 3.0; which = 2; }
-    double newdt = gnewdt;
-    const double ratio = newdt / olddt;
-    if (ratio >= 1.0) {
-      if (ratio < prm.deltatimemultlb) { newdt = olddt; rb = 1; }
-      else if (ratio > prm.deltatimemultub) { newdt = olddt * prm.deltatimemultub; rb = 2; }
-    }
-    if (!(newdt != newdt) && prm.dtmax < newdt) { newdt = prm.dtmax; mb = true; }
-    dt_pre = newdt;
-  }
-  bool t1 = false;
-  if (dt_pre < targetdt && targetdt < 4.0 * dt_pre / 3.0) { targetdt = 2.0 * dt_pre / 3.0; t1 = true; }
-  const bool t2 = targetdt < dt_pre;
-  double Lpre = 0.0;
-  if (t2) {
-    if (t1) Lpre += (2.0 / 3.0) * Ldt;
-    else Ltime += -Ldt;  // dt = stoptime - time
-  } else {
-    Lpre += Ldt;
-  }
-  if (!adaptive) { Ldt_prev += Lpre; return; }
-  if (mb) return;
-  if (rb == 1) { Ldt_prev += Lpre; return; }
-  if (rb == 2) { Ldt_prev += prm.deltatimemultub * Lpre; return; }
-  if (which == 1) Ldtc += 0.5 * Lpre;
-  else if (which == 2) Ldth += (2.0 / 3.0) * Lpre;
+  ka_tape_end<<<1, 1, 0, s>>>(d->dd.st, rec);
+  const int ge = (a->E + kAdjBlock - 1) / kAdjBlock;
+  ka_argmin<<<ge, kAdjBlock, 0, s>>>(tp.dtc, a->E, d->dd.st, 0, &rec->argmin_c);
+  ka_argmin<<<ge, kAdjBlock, 0, s>>>(tp.dth, a->E, d->dd.st, 1, &rec->argmin_h);
 }
 
 static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const StateBuf& s1, const CycleTape& t) {
@@ -262,39 +181,34 @@ static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const Stat
   ad.flags = t.flags;
 }
 
-// Transpose of one recorded cycle: the adjoint state goes from the cycle's
-// end to its start; returns the kernels' adjoint of dt and of hgcoef.
-static int reverse_cycle(lulesh_adjoint* a, const ScalarRec& r, int argmin_c, double lam_c, int argmin_h,
-                         double lam_h, double* Ldt_k, double* Lhg_k) {
+// Transpose of one recorded cycle, queued on the stream: the adjoint state
+// goes from the cycle's end to its start, and the carried scalar adjoints
+// through timeIncrement!.
+static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec) {
   lulesh_domain* d = a->dom;
   cudaStream_t s = d->stream;
   const Params prm = make_params(d);
   const int ge = (a->E + kAdjBlock - 1) / kAdjBlock, gn = (a->N + kAdjBlock - 1) / kAdjBlock;
   const int mode = d->dd.mode;
-  if (mode & 4) ka_material<4><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, argmin_c, lam_c, argmin_h, lam_h);
-  else ka_material<0><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, argmin_c, lam_c, argmin_h, lam_h);
+  if (mode & 4) ka_material<4><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, rec, a->dsc);
+  else ka_material<0><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, rec, a->dsc);
   ka_nb_gather<<<ge, kAdjBlock, 0, s>>>(a->ad);
-  ka_kinematics<<<ge, kAdjBlock, 0, s>>>(a->ad, r.dt);
+  ka_kinematics<<<ge, kAdjBlock, 0, s>>>(a->ad, rec);
   ka_gather_corners<<<gn, kAdjBlock, 0, s>>>(a->ad);
-  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, r.dt);
+  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, rec);
   const double hg = d->sc[LULESH_S_HGCOEF];
+#define LULESH_KA_FORCE(M)                                   \
+  ka_hourglass<M><<<ge, kAdjBlock, 0, s>>>(a->ad, hg);       \
+  ka_force_geo<M><<<ge, kAdjBlock, 0, s>>>(a->ad)
   switch (mode & 3) {
-    case 0: ka_force<0><<<ge, kAdjBlock, 0, s>>>(a->ad, hg); break;
-    case 1: ka_force<1><<<ge, kAdjBlock, 0, s>>>(a->ad, hg); break;
-    case 2: ka_force<2><<<ge, kAdjBlock, 0, s>>>(a->ad, hg); break;
-    default: ka_force<3><<<ge, kAdjBlock, 0, s>>>(a->ad, hg); break;
+    case 0: LULESH_KA_FORCE(0); break;
+    case 1: LULESH_KA_FORCE(1); break;
+    case 2: LULESH_KA_FORCE(2); break;
+    default: LULESH_KA_FORCE(3); break;
   }
+#undef LULESH_KA_FORCE
   ka_gather_corners<<<gn, kAdjBlock, 0, s>>>(a->ad);
-  ka_sum<<<1, kAdjBlock, 0, s>>>(a->ad.part_dt, ge, a->scal);
-  ka_sum<<<1, kAdjBlock, 0, s>>>(a->ad.part_dtn, gn, a->scal + 1);
-  ka_sum<<<1, kAdjBlock, 0, s>>>(a->ad.part_hg, ge, a->scal + 2);
-  ACK(cudaGetLastError());
-  double h[3];
-  ACK(cudaMemcpyAsync(h, a->scal, sizeof(h), cudaMemcpyDeviceToHost, s));
-  ACK(cudaStreamSynchronize(s));
-  *Ldt_k = h[0] + h[1];
-  *Lhg_k = h[2];
-  return LULESH_OK;
+  ka_cycle_close<<<1, kAdjBlock, 0, s>>>(a->ad, ge, gn, rec, a->dsc, prm);
 }
 
 static double* adj_field(lulesh_adjoint* a, int32_t f) {
@@ -402,9 +316,10 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
       (rc = dalloc(a, &ad.lss, E)) || (rc = dalloc(a, &ad.lv, E)) || (rc = dalloc(a, &ad.lvnew, E)) ||
       (rc = dalloc(a, &ad.ldelv, E)) || (rc = dalloc(a, &ad.larealg, E)) || (rc = dalloc(a, &ad.lvdov, E)) ||
       (rc = dalloc(a, &ad.lnb, 6 * (size_t)E)) || (rc = dalloc(a, &ad.cX, 24 * (size_t)E)) ||
-      (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
+      (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
+      (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
       (rc = dalloc(a, &ad.part_dtn, gn)) || (rc = dalloc(a, &ad.part_hg, ge)) || (rc = dalloc(a, &a->scal, 4)) ||
-      (rc = dalloc(a, &a->argmin, 2)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
+      (rc = dalloc(a, &a->rec, K)) || (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
       (rc = dalloc(a, &a->fx_s, N)) || (rc = dalloc(a, &a->fy_s, N)) || (rc = dalloc(a, &a->fz_s, N)))
     return fail(rc);
   for (int k = 0; k < 3; ++k)
@@ -536,67 +451,78 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   const int K = a->K;
   lulesh_adj_result out{};
   int rc;
-  // ---- forward sweep with checkpoints (stops early at stoptime, as the
-  // examples/benchmark.jl loop does) ----
+  // ---- forward sweep with checkpoints: lulesh_run per segment, which stops
+  // early at stoptime as the examples/benchmark.jl loop does ----
   auto t0 = std::chrono::steady_clock::now();
   int64_t done = 0;
   int nseg = 0;
-  auto running = [&]() { return done < num_cycles && d->sc[LULESH_S_TIME] < d->sc[LULESH_S_STOPTIME]; };
-  while (running()) {
+  a->seg_len.clear();
+  while (done < num_cycles && d->sc[LULESH_S_TIME] < d->sc[LULESH_S_STOPTIME]) {
     if ((int)a->ckpts.size() == nseg) {
       a->ckpts.emplace_back();
       if ((rc = alloc_state(a, a->ckpts.back()))) { a->ckpts.pop_back(); return rc; }
     }
     if ((int)a->ckpt_scalars.size() == nseg) a->ckpt_scalars.emplace_back();
-    if ((rc = copy_state_from_domain(a, a->ckpts[nseg]))) return rc;
+    copy_state_from_domain(a, a->ckpts[nseg]);
     a->ckpt_scalars[nseg] = get_scalars(d);
-    ++nseg;
-    for (int j = 0; j < K && running(); ++j, ++done)
-      if ((rc = forward_cycle(a, nullptr, nullptr))) { out.status = rc; if (res) *res = out; return rc; }
+    const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
+    const int64_t want = std::min<int64_t>(K, num_cycles - done);
+    rc = lulesh_run(d, c0 + want, nullptr);
+    const int64_t n = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
+    if (n > 0) { a->seg_len.push_back((int)n); ++nseg; done += n; }
+    if (rc) { out.status = rc; out.cycles = done; if (res) *res = out; return rc; }
+    if (n < want) break;
   }
+  auto t1 = std::chrono::steady_clock::now();
   out.cycles = done;
   out.checkpoints = nseg;
-  ACK(cudaStreamSynchronize(s));
-  auto t1 = std::chrono::steady_clock::now();
-  if ((rc = objective(a, true, &out.loss))) return rc;
-  if ((rc = copy_state_from_domain(a, a->final_state))) return rc;
+  // step state at each checkpoint, as lulesh_run uploads it
+  if (a->ckpt_st_cap < nseg) {
+    DevState* p = nullptr;
+    if ((rc = dalloc(a, &p, nseg))) return rc;
+    a->ckpt_st = p;
+    a->ckpt_st_cap = nseg;
+  }
+  {
+    std::vector<DevState> hs(nseg);
+    const Scalars5 now = get_scalars(d);
+    for (int k = 0; k < nseg; ++k) {
+      set_scalars(d, a->ckpt_scalars[k]);
+      state_to_device_mirror(d);
+      hs[k] = *d->hst;
+    }
+    set_scalars(d, now);
+    if (nseg) ACK(cudaMemcpyAsync(a->ckpt_st, hs.data(), nseg * sizeof(DevState), cudaMemcpyHostToDevice, s));
+    if ((rc = objective(a, true, &out.loss))) return rc;  // synchronises the stream (hs stays valid)
+  }
+  copy_state_from_domain(a, a->final_state);
   const Scalars5 final_sc = get_scalars(d);
   // ---- reverse sweep ----
-  const Params prm = make_params(d);
-  double Ltime = 0.0, Ldt = 0.0, Ldtc = 0.0, Ldth = 0.0, Lhg = 0.0;
-  a->rec.resize(K);
+  ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
   for (int k = nseg - 1; k >= 0; --k) {
-    if ((rc = copy_state_to_domain(a, a->ckpts[k]))) return rc;
-    set_scalars(d, a->ckpt_scalars[k]);
-    const int n = (int)std::min<int64_t>(K, done - (int64_t)k * K);
+    const int n = a->seg_len[k];
+    copy_state_to_domain(a, a->ckpts[k]);
+    ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
     for (int j = 0; j < n; ++j) {
-      if ((rc = copy_state_from_domain(a, a->slots[j]))) return rc;
-      if ((rc = forward_cycle(a, &a->tape[j], &a->rec[j]))) return rc;
+      copy_state_from_domain(a, a->slots[j]);
+      tape_cycle(a, a->tape[j], a->rec + j);
     }
-    if ((rc = copy_state_from_domain(a, a->slots[n]))) return rc;
+    copy_state_from_domain(a, a->slots[n]);
     for (int j = n - 1; j >= 0; --j) {
-      const ScalarRec& r = a->rec[j];
-      // the cycle's Courant/hydro minima feed the element that attained them
-      const double lam_c = r.active_c ? Ldtc : 0.0, lam_h = r.active_h ? Ldth : 0.0;
-      double Ldtc_prev = r.active_c ? 0.0 : Ldtc, Ldth_prev = r.active_h ? 0.0 : Ldth;
       set_cycle_pointers(a, a->slots[j], a->slots[j + 1], a->tape[j]);
-      double Ldt_k = 0.0, Lhg_k = 0.0;
-      if ((rc = reverse_cycle(a, r, r.argmin_c, lam_c, r.argmin_h, lam_h, &Ldt_k, &Lhg_k))) return rc;
-      Lhg += Lhg_k;
-      // time_n = time_{n-1} + dt_n, then timeIncrement!'s transpose
-      double Ldt_tot = Ldt + Ldt_k + Ltime;
-      double Ldt_prev = 0.0;
-      time_increment_reverse(r, prm, Ldt_tot, Ltime, Ldt_prev, Ldtc_prev, Ldth_prev);
-      Ldt = Ldt_prev;
-      Ldtc = Ldtc_prev;
-      Ldth = Ldth_prev;
+      reverse_cycle(a, a->rec + j);
     }
+    ACK(cudaGetLastError());
   }
-  if ((rc = copy_state_to_domain(a, a->final_state))) return rc;
-  set_scalars(d, final_sc);
+  copy_state_to_domain(a, a->final_state);
+  AdjScal hsc;
+  ACK(cudaMemcpyAsync(&hsc, a->dsc, sizeof(AdjScal), cudaMemcpyDeviceToHost, s));
   ACK(cudaStreamSynchronize(s));
+  set_scalars(d, final_sc);
+  state_to_device_mirror(d);
+  ACK(cudaMemcpy(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice));
   auto t2 = std::chrono::steady_clock::now();
-  out.grad_hgcoef = Lhg;
+  out.grad_hgcoef = hsc.Lhg;
   out.forward_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   out.reverse_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
   out.status = LULESH_OK;

@@ -13,11 +13,31 @@
 // neighbour list: no atomics, so gradients are bitwise reproducible.
 #pragma once
 
+#include <climits>
+
 #include "lulesh_device.cuh"
 
 namespace lulesh {
 
 constexpr int kAdjBlock = 128;
+
+// Scalars of one recorded cycle: timeIncrement!'s inputs and output, and the
+// elements that attained the Courant and hydro minima (INT_MAX: none).
+struct CycleRec {
+  double time_prev, dt_prev, dtc_in, dth_in, dt;
+  long long cycle_prev;
+  int active_c, active_h, argmin_c, argmin_h;
+};
+
+// Adjoints of the Domain scalars carried from cycle to cycle.
+struct AdjScal {
+  double Ltime, Ldt, Ldtc, Ldth, Lhg;
+};
+
+// The 11 state fields (x y z xd yd zd e p q v ss) of one stored state.
+struct StateSet {
+  double* f[11];
+};
 
 struct AdjDev {
   int E, N;
@@ -48,6 +68,7 @@ struct AdjDev {
   double* lnb;                                // [6][E]: limiter neighbour slots
   double *cX, *cV;                            // [3][8][E] corner buffers
   double *part_dt, *part_dtn, *part_hg;       // per-block partial sums (kinematics, node, force)
+  double *sLdv, *sLhm;                        // [3][8][E], [3][4][E]: hourglass -> geometry
 };
 
 // Deterministic block sum (fixed tree order); thread 0 writes the block's sum.
@@ -100,11 +121,15 @@ __device__ __forceinline__ int limiter_index(unsigned mask, unsigned bits, unsig
 // Courant and hydro candidates).
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, int argmin_c, double lam_c,
-                                                          int argmin_h, double lam_h) {
+__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, const CycleRec* rec,
+                                                          const AdjScal* sc) {
   const int E = a.E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= E) return;
+  // the cycle's Courant/hydro minima pass their adjoint to the element that
+  // attained them
+  const int argmin_c = rec->argmin_c, argmin_h = rec->argmin_h;
+  const double lam_c = rec->active_c ? sc->Ldtc : 0.0, lam_h = rec->active_h ? sc->Ldth : 0.0;
   const unsigned long long fl = a.flags[i];
   const double ptiny = 1.e-36;
   const unsigned mask = a.elemBC[i];
@@ -349,9 +374,10 @@ __global__ void __launch_bounds__(kAdjBlock) ka_nb_gather(AdjDev a) {
 // ka_kinematics: transpose of k_kinematics (volume, characteristic length,
 // velocity-gradient trace, monotonic-Q gradients), into the corner buffers.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, double dt) {
+__global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const CycleRec* rec) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  const double dt = rec->dt;
   double Ldt = 0.0;
   if (e < E) {
     int nd[8];
@@ -533,8 +559,9 @@ __global__ void __launch_bounds__(kAdjBlock) ka_gather_corners(AdjDev a) {
 // ka_node: transpose of k_node (position and velocity update with the
 // velocity snap, acceleration = force / mass with the symmetry BCs).
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, double dt) {
+__global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, const CycleRec* rec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const double dt = rec->dt;
   double Ldt = 0.0;
   if (i < a.N) {
     const unsigned bc = a.nodeBC[i];
@@ -567,10 +594,56 @@ __global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, double dt) {
 }
 
 // ---------------------------------------------------------------------------
-// ka_force: transpose of k_force (stress integration and FB hourglass force).
+// Transpose of k_force, in two kernels: ka_hourglass (the FB hourglass force
+// onto the velocities, ss, v, hgcoef and the two geometric factors) and
+// ka_force_geo (the stress force and those geometric factors onto the
+// positions).
 // ---------------------------------------------------------------------------
+
+// Transpose of the hourglass mode transform: out[n] = sum_m gamma[n][m] t[m]
+// (12 adds).
+__device__ __forceinline__ void walsh_modes_t(const double t[4], double out[8]) {
+  const double cm = t[2] - t[3], cp = t[2] + t[3];
+  const double s = t[0] + t[1], d = t[0] - t[1];
+  out[0] = s + cm; out[1] = d - cm; out[2] = cm - s; out[3] = -d - cm;
+  out[4] = cp - s; out[5] = -d - cp; out[6] = s + cp; out[7] = d - cp;
+}
+
+// The 8 volume derivatives (times 12) of one coordinate pair, in the forward
+// kernel's slot order: dv_x uses (ey, ez), dv_y (ex, ez), dv_z (ey, ex) with
+// the sign pattern of each.
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_force(AdjDev a, double hgcoef) {
+__device__ __forceinline__ void volu_der(const double ex[12], const double ey[12], const double ez[12],
+                                         double dv[3][8]) {
+  constexpr int pe[8][6] = {{5, 3, 4, 8, 7, 9}, {3, 0, 2, 9, 6, 11}, {0, 1, 7, 11, 4, 10},
+                            {1, 5, 6, 10, 2, 8}, {10, 11, 7, 1, 4, 0}, {11, 9, 2, 0, 6, 3},
+                            {9, 8, 4, 3, 7, 5}, {8, 10, 6, 5, 2, 1}};
+  constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
+    const int slot = (MODE & 2) ? owner[n] : n;
+    dv[0][slot] = fma(ey[p12], ez[p01], fma(-ey[p01], ez[p12], fma(ey[p04], ez[p34],
+                  fma(-ey[p34], ez[p04], fma(-ey[p25], ez[p35], ey[p35] * ez[p25])))));
+    dv[1][slot] = fma(-ex[p12], ez[p01], fma(ex[p01], ez[p12], fma(-ex[p04], ez[p34],
+                  fma(ex[p34], ez[p04], fma(ex[p25], ez[p35], -(ex[p35] * ez[p25]))))));
+    dv[2][slot] = fma(-ey[p12], ex[p01], fma(ey[p01], ex[p12], fma(-ey[p04], ex[p34],
+                  fma(ey[p34], ex[p04], fma(ey[p25], ex[p35], -(ey[p35] * ex[p25]))))));
+  }
+}
+
+// Hourglass transpose. With hg[n][m] = gamma[n][m] - sum_j dv_j[n] hms_j[m]
+// (hms = the modes over 12*determ), S_k = hg^T V_k, T_k = hg^T lf_k (lf the
+// force adjoints) and coef the hourglass coefficient, the forward force is
+// F_k = coef hg S_k and its transpose needs only
+//   dL/dV_k   = coef hg T_k,
+//   dL/ddv_j  = -coef sum_k (lf_k (S_k . hms_j) + V_k (T_k . hms_j)),
+//   dL/dhms_j = -coef sum_k (S_k (lf_k . dv_j) + T_k (V_k . dv_j)),
+//   dL/dcoef  = sum_k S_k . T_k,
+// where hg^T u = Gamma(u) - sum_j hms_j (dv_j . u): 3x3 dot-product tables
+// replace the 8x4 matrices hg and dL/dhg.
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoef) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   double Lhg_coef = 0.0;
@@ -578,276 +651,421 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force(AdjDev a, double hgcoef) {
     int nd[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
-    double X[3][8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) { X[0][c] = a.x0[nd[c]]; X[1][c] = a.y0[nd[c]]; X[2][c] = a.z0[nd[c]]; }
-    double LX[3][8];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) LX[k][c] = 0.0;
-    const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
-    const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
-    // ---- stress part: f = s8 * B ----
-    {
-      constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
-                                {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
-      constexpr int nf[8][3] = {{0, 1, 4}, {0, 1, 2}, {0, 2, 3}, {0, 3, 4},
-                                {1, 4, 5}, {1, 2, 5}, {2, 3, 5}, {3, 4, 5}};
-      V3 N[6];
-#pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
-        const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
-        N[f] = vcross(d1, d2);
-      }
-      double Ls8 = 0.0;
-      V3 LN[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
-#pragma unroll
-      for (int n = 0; n < 8; ++n) {
-        const V3 lf = v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]);
-        V3 B = N[nf[n][0]]; vadd(B, N[nf[n][1]]); vadd(B, N[nf[n][2]]);
-        V3 LB = v3(s8 * lf.x, s8 * lf.y, s8 * lf.z);
-        if (n == 0 && !(MODE & 1)) {
-          // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice and no areaZ
-          B.y += N[4].y;
-          B.z -= N[4].z;
-          Ls8 += vdot(lf, B);
-          LN[0].x += LB.x; LN[1].x += LB.x; LN[4].x += LB.x;
-          LN[0].y += LB.y; LN[1].y += LB.y; LN[4].y += 2.0 * LB.y;
-          LN[0].z += LB.z; LN[1].z += LB.z;
-        } else {
-          Ls8 += vdot(lf, B);
-          vadd(LN[nf[n][0]], LB); vadd(LN[nf[n][1]], LB); vadd(LN[nf[n][2]], LB);
-        }
-      }
-      const double Lpq = -0.125 * Ls8;
-      a.lp[e] += Lpq;
-      a.lq[e] += Lpq;
-#pragma unroll
-      for (int f = 0; f < 6; ++f) {
-        const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
-        const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
-        const V3 L1 = vcross(d2, LN[f]), L2 = vcross(LN[f], d1);
-        LX[0][fd[f][0]] += L1.x; LX[1][fd[f][0]] += L1.y; LX[2][fd[f][0]] += L1.z;
-        LX[0][fd[f][1]] -= L1.x; LX[1][fd[f][1]] -= L1.y; LX[2][fd[f][1]] -= L1.z;
-        LX[0][fd[f][2]] += L2.x; LX[1][fd[f][2]] += L2.y; LX[2][fd[f][2]] += L2.z;
-        LX[0][fd[f][3]] -= L2.x; LX[1][fd[f][3]] -= L2.y; LX[2][fd[f][3]] -= L2.z;
-      }
-    }
-    // ---- FB hourglass part ----
-    const double v = a.v0[e];
-    const double determ = a.volo[e] * v;
-    if (hgcoef > 0.0) {
-      double w1[3], hm[3][4];
-      walsh7(X[0], w1, hm[0]);
-      walsh7(X[1], w1, hm[1]);
-      walsh7(X[2], w1, hm[2]);
-      constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
-      constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
-      // edge ids of (q1q2, q0q1, q0q4, q3q4, q2q5, q3q5) for each voluDer call
-      constexpr int pe[8][6] = {{5, 3, 4, 8, 7, 9}, {3, 0, 2, 9, 6, 11}, {0, 1, 7, 11, 4, 10},
-                                {1, 5, 6, 10, 2, 8}, {10, 11, 7, 1, 4, 0}, {11, 9, 2, 0, 6, 3},
-                                {9, 8, 4, 3, 7, 5}, {8, 10, 6, 5, 2, 1}};
-      constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
-      double dv[3][8];
-      {
-        double ex[12], ey[12], ez[12];
-#pragma unroll
-        for (int k = 0; k < 12; ++k) {
-          ex[k] = X[0][ea[k]] + X[0][eb[k]];
-          ey[k] = X[1][ea[k]] + X[1][eb[k]];
-          ez[k] = X[2][ea[k]] + X[2][eb[k]];
-        }
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
-          const int slot = (MODE & 2) ? owner[n] : n;
-          dv[0][slot] = fma(ey[p12], ez[p01], fma(-ey[p01], ez[p12], fma(ey[p04], ez[p34],
-                        fma(-ey[p34], ez[p04], fma(-ey[p25], ez[p35], ey[p35] * ez[p25])))));
-          dv[1][slot] = fma(-ex[p12], ez[p01], fma(ex[p01], ez[p12], fma(-ex[p04], ez[p34],
-                        fma(ex[p34], ez[p04], fma(ex[p25], ez[p35], -(ex[p35] * ez[p25]))))));
-          dv[2][slot] = fma(-ey[p12], ex[p01], fma(ey[p01], ex[p12], fma(-ey[p04], ex[p34],
-                        fma(ey[p34], ex[p04], fma(ey[p25], ex[p35], -(ey[p35] * ex[p25]))))));
-        }
-      }
-      const double vi12 = 1.0 / (12.0 * determ);
-      double hms[3][4];
+    if (!(hgcoef > 0.0)) {
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int m = 0; m < 4; ++m) hms[k][m] = vi12 * hm[k][m];
-      double hg[8][4], Lhg[8][4];
+        for (int c = 0; c < 8; ++c) { a.cV[(k * 8 + c) * E + e] = 0.0; a.sLdv[(k * 8 + c) * E + e] = 0.0; }
 #pragma unroll
-      for (int n = 0; n < 8; ++n)
+      for (int k = 0; k < 12; ++k) a.sLhm[k * E + e] = 0.0;
+    } else {
+      const double* Xp[3] = {a.x0, a.y0, a.z0};
+      const double* Vp[3] = {a.xd0, a.yd0, a.zd0};
+      const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+      double hms[3][4], dv[3][8];
+      {
+        double X[3][8];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          hg[n][m] = fma(-dv[2][n], hms[2][m], fma(-dv[1][n], hms[1][m], fma(-dv[0][n], hms[0][m], gamma_nm(n, m))));
-          Lhg[n][m] = 0.0;
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) X[k][c] = Xp[k][nd[c]];
+        double w1[3];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) walsh7(X[k], w1, hms[k]);
+        constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
+        constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
+        double ex[12], ey[12], ez[12];
+#pragma unroll
+        for (int j = 0; j < 12; ++j) {
+          ex[j] = X[0][ea[j]] + X[0][eb[j]];
+          ey[j] = X[1][ea[j]] + X[1][eb[j]];
+          ez[j] = X[2][ea[j]] + X[2][eb[j]];
         }
+        volu_der<MODE>(ex, ey, ez, dv);
+      }
+      const double determ = a.volo[e] * a.v0[e];
+      const double vi12 = 1.0 / (12.0 * determ);
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) hms[j][m] *= vi12;
       const double ss = a.ss0[e], mass = a.elemMass[e];
       const double r = rcbrt(determ);
       const double c0 = -hgcoef * 0.01;
       const double coef = ((c0 * ss) * mass) * r;
+      // S_k, D[k][j] = V_k . dv_j and T_k, C[k][j] = lf_k . dv_j
+      double S[3][4], T[3][4], D[3][3], C[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        double u[8], w2[4], w1[3];
+#pragma unroll
+        for (int c = 0; c < 8; ++c) u[c] = Vp[k][nd[c]];
+        walsh7(u, w1, w2);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double s = dv[j][0] * u[0];
+#pragma unroll
+          for (int c = 1; c < 8; ++c) s = fma(dv[j][c], u[c], s);
+          D[k][j] = s;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          S[k][m] = fma(-hms[2][m], D[k][2], fma(-hms[1][m], D[k][1], fma(-hms[0][m], D[k][0], w2[m])));
+#pragma unroll
+        for (int c = 0; c < 8; ++c) u[c] = Lf[k][nd[c]];
+        walsh7(u, w1, w2);
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          double s = dv[j][0] * u[0];
+#pragma unroll
+          for (int c = 1; c < 8; ++c) s = fma(dv[j][c], u[c], s);
+          C[k][j] = s;
+        }
+#pragma unroll
+        for (int m = 0; m < 4; ++m)
+          T[k][m] = fma(-hms[2][m], C[k][2], fma(-hms[1][m], C[k][1], fma(-hms[0][m], C[k][0], w2[m])));
+      }
       double Lcoef = 0.0;
-      const double* Vp[3] = {a.xd0, a.yd0, a.zd0};
 #pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        double vv[8], lf[8];
+      for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) { vv[c] = Vp[k][nd[c]]; lf[c] = Lf[k][nd[c]]; }
-        double S[4], h[4], Lh[4];
+        for (int m = 0; m < 4; ++m) Lcoef = fma(S[k][m], T[k][m], Lcoef);
+      // A[k][j] = S_k . hms_j, B[k][j] = T_k . hms_j
+      double A[3][3], B[3][3];
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          double s = hg[0][m] * vv[0];
+      for (int k = 0; k < 3; ++k)
 #pragma unroll
-          for (int n = 1; n < 8; ++n) s = fma(hg[n][m], vv[n], s);
-          S[m] = s;
-          h[m] = coef * s;
-          double lh = 0.0;
-#pragma unroll
-          for (int n = 0; n < 8; ++n) {
-            lh = fma(lf[n], hg[n][m], lh);
-            Lhg[n][m] = fma(lf[n], h[m], Lhg[n][m]);
-          }
-          Lh[m] = lh;
-          Lcoef = fma(lh, S[m], Lcoef);
+        for (int j = 0; j < 3; ++j) {
+          A[k][j] = fma(S[k][0], hms[j][0], fma(S[k][1], hms[j][1], fma(S[k][2], hms[j][2], S[k][3] * hms[j][3])));
+          B[k][j] = fma(T[k][0], hms[j][0], fma(T[k][1], hms[j][1], fma(T[k][2], hms[j][2], T[k][3] * hms[j][3])));
         }
-        double LV[8];
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          double l = 0.0;
-#pragma unroll
-          for (int m = 0; m < 4; ++m) {
-            const double LS = coef * Lh[m];
-            Lhg[n][m] = fma(LS, vv[n], Lhg[n][m]);
-            l = fma(LS, hg[n][m], l);
-          }
-          LV[n] = l;
-        }
-#pragma unroll
-        for (int c = 0; c < 8; ++c) a.cV[(k * 8 + c) * E + e] = LV[c];
-      }
-      // coef = c0*ss*mass*determ^(-1/3)
-      a.lss[e] += Lcoef * c0 * mass * r;
-      Lhg_coef = Lcoef * (-0.01) * ss * mass * r;
-      double Ldeterm = Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r / determ;
-      // hg = gamma - sum_k dv_k hms_k
-      double Ldv[3][8], Lhms[3][4];
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          double s = 0.0;
-#pragma unroll
-          for (int m = 0; m < 4; ++m) s = fma(Lhg[n][m], hms[k][m], s);
-          Ldv[k][n] = -s;
-        }
-#pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          double s = 0.0;
-#pragma unroll
-          for (int n = 0; n < 8; ++n) s = fma(Lhg[n][m], dv[k][n], s);
-          Lhms[k][m] = -s;
-        }
-      }
+      // dL/dhm_j = vi12 dL/dhms_j; dL/dvi12 = sum_j dL/dhms_j . hm_j = sum_j dL/dhms_j . hms_j / vi12
       double Lvi12 = 0.0;
 #pragma unroll
-      for (int k = 0; k < 3; ++k)
+      for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int m = 0; m < 4; ++m) Lvi12 = fma(Lhms[k][m], hm[k][m], Lvi12);
-      Ldeterm += -Lvi12 * vi12 / determ;
-      a.lv[e] += Ldeterm * a.volo[e];
-      // hm_k[m] = sum_n gamma[n][m] X_k[n]
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          double s = 0.0;
-#pragma unroll
-          for (int m = 0; m < 4; ++m) s = fma(gamma_nm(n, m), vi12 * Lhms[k][m], s);
-          LX[k][n] += s;
+        for (int m = 0; m < 4; ++m) {
+          const double Lhms = -coef * fma(S[0][m], C[0][j], fma(S[1][m], C[1][j], fma(S[2][m], C[2][j],
+                              fma(T[0][m], D[0][j], fma(T[1][m], D[1][j], T[2][m] * D[2][j])))));
+          Lvi12 = fma(Lhms, hms[j][m], Lvi12);
+          a.sLhm[(j * 4 + m) * E + e] = vi12 * Lhms;
         }
-      // voluDer transposes onto the edge sums, then onto the nodes
-      double Lex[12], Ley[12], Lez[12];
+      // dL/dV_k = coef (Gamma^T T_k - sum_j dv_j B[k][j])
 #pragma unroll
-      for (int j = 0; j < 12; ++j) { Lex[j] = 0.0; Ley[j] = 0.0; Lez[j] = 0.0; }
+      for (int k = 0; k < 3; ++k) {
+        double q[8];
+        walsh_modes_t(T[k], q);
+#pragma unroll
+        for (int c = 0; c < 8; ++c)
+          a.cV[(k * 8 + c) * E + e] =
+              coef * fma(-dv[2][c], B[k][2], fma(-dv[1][c], B[k][1], fma(-dv[0][c], B[k][0], q[c])));
+      }
+      // dL/ddv_j = -coef sum_k (lf_k A[k][j] + V_k B[k][j])
       {
-        double ex[12], ey[12], ez[12];
+        double Ldv[3][8];
 #pragma unroll
-        for (int k = 0; k < 12; ++k) {
-          ex[k] = X[0][ea[k]] + X[0][eb[k]];
-          ey[k] = X[1][ea[k]] + X[1][eb[k]];
-          ez[k] = X[2][ea[k]] + X[2][eb[k]];
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) Ldv[j][c] = 0.0;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) {
+            const double lf = Lf[k][nd[c]], vv = Vp[k][nd[c]];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) Ldv[j][c] = fma(lf, A[k][j], fma(vv, B[k][j], Ldv[j][c]));
+          }
         }
 #pragma unroll
-        for (int n = 0; n < 8; ++n) {
-          const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
-          const int slot = (MODE & 2) ? owner[n] : n;
-          const double gx = Ldv[0][slot], gy = Ldv[1][slot], gz = Ldv[2][slot];
-          // dvx = ey12 ez01 - ey01 ez12 + ey04 ez34 - ey34 ez04 - ey25 ez35 + ey35 ez25
-          Ley[p12] += gx * ez[p01]; Lez[p01] += gx * ey[p12];
-          Ley[p01] -= gx * ez[p12]; Lez[p12] -= gx * ey[p01];
-          Ley[p04] += gx * ez[p34]; Lez[p34] += gx * ey[p04];
-          Ley[p34] -= gx * ez[p04]; Lez[p04] -= gx * ey[p34];
-          Ley[p25] -= gx * ez[p35]; Lez[p35] -= gx * ey[p25];
-          Ley[p35] += gx * ez[p25]; Lez[p25] += gx * ey[p35];
-          // dvy = -ex12 ez01 + ex01 ez12 - ex04 ez34 + ex34 ez04 + ex25 ez35 - ex35 ez25
-          Lex[p12] -= gy * ez[p01]; Lez[p01] -= gy * ex[p12];
-          Lex[p01] += gy * ez[p12]; Lez[p12] += gy * ex[p01];
-          Lex[p04] -= gy * ez[p34]; Lez[p34] -= gy * ex[p04];
-          Lex[p34] += gy * ez[p04]; Lez[p04] += gy * ex[p34];
-          Lex[p25] += gy * ez[p35]; Lez[p35] += gy * ex[p25];
-          Lex[p35] -= gy * ez[p25]; Lez[p25] -= gy * ex[p35];
-          // dvz = -ey12 ex01 + ey01 ex12 - ey04 ex34 + ey34 ex04 + ey25 ex35 - ey35 ex25
-          Ley[p12] -= gz * ex[p01]; Lex[p01] -= gz * ey[p12];
-          Ley[p01] += gz * ex[p12]; Lex[p12] += gz * ey[p01];
-          Ley[p04] -= gz * ex[p34]; Lex[p34] -= gz * ey[p04];
-          Ley[p34] += gz * ex[p04]; Lex[p04] += gz * ey[p34];
-          Ley[p25] += gz * ex[p35]; Lex[p35] += gz * ey[p25];
-          Ley[p35] -= gz * ex[p25]; Lex[p25] -= gz * ey[p35];
-        }
+        for (int j = 0; j < 3; ++j)
+#pragma unroll
+          for (int c = 0; c < 8; ++c) a.sLdv[(j * 8 + c) * E + e] = -coef * Ldv[j][c];
       }
-#pragma unroll
-      for (int j = 0; j < 12; ++j) {
-        LX[0][ea[j]] += Lex[j]; LX[0][eb[j]] += Lex[j];
-        LX[1][ea[j]] += Ley[j]; LX[1][eb[j]] += Ley[j];
-        LX[2][ea[j]] += Lez[j]; LX[2][eb[j]] += Lez[j];
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 3; ++k)
-#pragma unroll
-        for (int c = 0; c < 8; ++c) a.cV[(k * 8 + c) * E + e] = 0.0;
+      // coef = c0 ss mass determ^(-1/3), vi12 = 1/(12 determ), determ = volo v
+      a.lss[e] += Lcoef * c0 * mass * r;
+      Lhg_coef = Lcoef * (-0.01) * ss * mass * r;
+      const double Ldeterm = Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r / determ - Lvi12 / determ;
+      a.lv[e] += Ldeterm * a.volo[e];
     }
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
   }
   block_sum_to(Lhg_coef, a.part_hg);
 }
 
-// Sums `n` partials in a fixed order (one block).
-__global__ void __launch_bounds__(kAdjBlock) ka_sum(const double* part, int n, double* out) {
+// Position transpose of k_force: the stress force (face-diagonal cross
+// products, with the reference's face-5 normal quirk unless corrected), the
+// hourglass modes (Gamma^T of dL/dhm) and the volume derivatives (through
+// the 12 edge sums), written to the position corner buffer.
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
+  const int E = a.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  int nd[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
+  double X[3][8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) { X[0][c] = a.x0[nd[c]]; X[1][c] = a.y0[nd[c]]; X[2][c] = a.z0[nd[c]]; }
+  double LX[3][8];
+  // hourglass modes hm_k = Gamma(X_k)
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    double t[4], q[8];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) t[m] = a.sLhm[(k * 4 + m) * E + e];
+    walsh_modes_t(t, q);
+#pragma unroll
+    for (int c = 0; c < 8; ++c) LX[k][c] = q[c];
+  }
+  // volume derivatives through the edge sums
+  {
+    constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
+    constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
+    constexpr int pe[8][6] = {{5, 3, 4, 8, 7, 9}, {3, 0, 2, 9, 6, 11}, {0, 1, 7, 11, 4, 10},
+                              {1, 5, 6, 10, 2, 8}, {10, 11, 7, 1, 4, 0}, {11, 9, 2, 0, 6, 3},
+                              {9, 8, 4, 3, 7, 5}, {8, 10, 6, 5, 2, 1}};
+    constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
+    double ex[12], ey[12], ez[12], Lex[12], Ley[12], Lez[12];
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+      ex[j] = X[0][ea[j]] + X[0][eb[j]];
+      ey[j] = X[1][ea[j]] + X[1][eb[j]];
+      ez[j] = X[2][ea[j]] + X[2][eb[j]];
+      Lex[j] = 0.0; Ley[j] = 0.0; Lez[j] = 0.0;
+    }
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
+      const int slot = (MODE & 2) ? owner[n] : n;
+      const double gx = a.sLdv[(0 * 8 + slot) * E + e], gy = a.sLdv[(1 * 8 + slot) * E + e],
+                   gz = a.sLdv[(2 * 8 + slot) * E + e];
+      // dvx = ey12 ez01 - ey01 ez12 + ey04 ez34 - ey34 ez04 - ey25 ez35 + ey35 ez25
+      Ley[p12] = fma(gx, ez[p01], Ley[p12]); Lez[p01] = fma(gx, ey[p12], Lez[p01]);
+      Ley[p01] = fma(-gx, ez[p12], Ley[p01]); Lez[p12] = fma(-gx, ey[p01], Lez[p12]);
+      Ley[p04] = fma(gx, ez[p34], Ley[p04]); Lez[p34] = fma(gx, ey[p04], Lez[p34]);
+      Ley[p34] = fma(-gx, ez[p04], Ley[p34]); Lez[p04] = fma(-gx, ey[p34], Lez[p04]);
+      Ley[p25] = fma(-gx, ez[p35], Ley[p25]); Lez[p35] = fma(-gx, ey[p25], Lez[p35]);
+      Ley[p35] = fma(gx, ez[p25], Ley[p35]); Lez[p25] = fma(gx, ey[p35], Lez[p25]);
+      // dvy = -ex12 ez01 + ex01 ez12 - ex04 ez34 + ex34 ez04 + ex25 ez35 - ex35 ez25
+      Lex[p12] = fma(-gy, ez[p01], Lex[p12]); Lez[p01] = fma(-gy, ex[p12], Lez[p01]);
+      Lex[p01] = fma(gy, ez[p12], Lex[p01]); Lez[p12] = fma(gy, ex[p01], Lez[p12]);
+      Lex[p04] = fma(-gy, ez[p34], Lex[p04]); Lez[p34] = fma(-gy, ex[p04], Lez[p34]);
+      Lex[p34] = fma(gy, ez[p04], Lex[p34]); Lez[p04] = fma(gy, ex[p34], Lez[p04]);
+      Lex[p25] = fma(gy, ez[p35], Lex[p25]); Lez[p35] = fma(gy, ex[p25], Lez[p35]);
+      Lex[p35] = fma(-gy, ez[p25], Lex[p35]); Lez[p25] = fma(-gy, ex[p35], Lez[p25]);
+      // dvz = -ey12 ex01 + ey01 ex12 - ey04 ex34 + ey34 ex04 + ey25 ex35 - ey35 ex25
+      Ley[p12] = fma(-gz, ex[p01], Ley[p12]); Lex[p01] = fma(-gz, ey[p12], Lex[p01]);
+      Ley[p01] = fma(gz, ex[p12], Ley[p01]); Lex[p12] = fma(gz, ey[p01], Lex[p12]);
+      Ley[p04] = fma(-gz, ex[p34], Ley[p04]); Lex[p34] = fma(-gz, ey[p04], Lex[p34]);
+      Ley[p34] = fma(gz, ex[p04], Ley[p34]); Lex[p04] = fma(gz, ey[p34], Lex[p04]);
+      Ley[p25] = fma(gz, ex[p35], Ley[p25]); Lex[p35] = fma(gz, ey[p25], Lex[p35]);
+      Ley[p35] = fma(-gz, ex[p25], Ley[p35]); Lex[p25] = fma(-gz, ey[p35], Lex[p25]);
+    }
+#pragma unroll
+    for (int j = 0; j < 12; ++j) {
+      LX[0][ea[j]] += Lex[j]; LX[0][eb[j]] += Lex[j];
+      LX[1][ea[j]] += Ley[j]; LX[1][eb[j]] += Ley[j];
+      LX[2][ea[j]] += Lez[j]; LX[2][eb[j]] += Lez[j];
+    }
+  }
+  // stress part: f = s8 * B with B the sum of the node's three face cross products
+  {
+    const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+    const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
+    constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
+                              {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
+    constexpr int nf[8][3] = {{0, 1, 4}, {0, 1, 2}, {0, 2, 3}, {0, 3, 4},
+                              {1, 4, 5}, {1, 2, 5}, {2, 3, 5}, {3, 4, 5}};
+    V3 N[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
+      const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
+      N[f] = vcross(d1, d2);
+    }
+    double Ls8 = 0.0;
+    V3 LN[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+      const V3 lf = v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]);
+      V3 B = N[nf[n][0]]; vadd(B, N[nf[n][1]]); vadd(B, N[nf[n][2]]);
+      const V3 LB = v3(s8 * lf.x, s8 * lf.y, s8 * lf.z);
+      if (n == 0 && !(MODE & 1)) {
+        // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice and no areaZ
+        B.y += N[4].y;
+        B.z -= N[4].z;
+        Ls8 += vdot(lf, B);
+        LN[0].x += LB.x; LN[1].x += LB.x; LN[4].x += LB.x;
+        LN[0].y += LB.y; LN[1].y += LB.y; LN[4].y += 2.0 * LB.y;
+        LN[0].z += LB.z; LN[1].z += LB.z;
+      } else {
+        Ls8 += vdot(lf, B);
+        vadd(LN[nf[n][0]], LB); vadd(LN[nf[n][1]], LB); vadd(LN[nf[n][2]], LB);
+      }
+    }
+    const double Lpq = -0.125 * Ls8;
+    a.lp[e] += Lpq;
+    a.lq[e] += Lpq;
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
+      const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
+      const V3 L1 = vcross(d2, LN[f]), L2 = vcross(LN[f], d1);
+      LX[0][fd[f][0]] += L1.x; LX[1][fd[f][0]] += L1.y; LX[2][fd[f][0]] += L1.z;
+      LX[0][fd[f][1]] -= L1.x; LX[1][fd[f][1]] -= L1.y; LX[2][fd[f][1]] -= L1.z;
+      LX[0][fd[f][2]] += L2.x; LX[1][fd[f][2]] += L2.y; LX[2][fd[f][2]] += L2.z;
+      LX[0][fd[f][3]] -= L2.x; LX[1][fd[f][3]] -= L2.y; LX[2][fd[f][3]] -= L2.z;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
+}
+
+// Sum of `n` partials in a fixed order by one block; every thread gets it.
+__device__ double block_fixed_sum(const double* part, int n) {
+  __shared__ double sh[kAdjBlock];
   double s = 0.0;
   for (int j = threadIdx.x; j < n; j += blockDim.x) s += part[j];
-  __shared__ double sh[kAdjBlock];
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int w = kAdjBlock / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
     __syncthreads();
   }
-  if (threadIdx.x == 0) *out = sh[0];
+  const double r = sh[0];
+  __syncthreads();
+  return r;
 }
 
-// Smallest element index whose dt candidate equals the minimum: the element
-// the reference's strict-less-than scan keeps (src/domain.jl:3003-3008).
-__global__ void __launch_bounds__(kAdjBlock) ka_argmin(const double* cand, int E, unsigned long long minbits,
+// Sums `n` partials in a fixed order (one block).
+__global__ void __launch_bounds__(kAdjBlock) ka_sum(const double* part, int n, double* out) {
+  const double s = block_fixed_sum(part, n);
+  if (threadIdx.x == 0) *out = s;
+}
+
+// Transpose of timeIncrement! (src/domain.jl:920-961) for the recorded
+// inputs: Ldt is the adjoint of the new deltatime; adds to the adjoints of
+// the previous time, deltatime, dtcourant and dthydro along the branch taken.
+__host__ __device__ inline void time_increment_reverse(const CycleRec& r, const Params& prm, double Ldt,
+                                                       double& Ltime, double& Ldt_prev, double& Ldtc,
+                                                       double& Ldth) {
+  double targetdt = prm.stoptime - r.time_prev;
+  double dt_pre = r.dt_prev;
+  int which = 0, rb = 0;
+  bool mb = false;
+  const bool adaptive = prm.dtfixed <= 0.0 && r.cycle_prev != 0;
+  if (adaptive) {
+    const double olddt = r.dt_prev;
+    double gnewdt = (double)INFINITY;
+    if (r.dtc_in < gnewdt) { gnewdt = r.dtc_in / 2.0; which = 1; }
+    if (r.dth_in < gnewdt) { gnewdt = r.dth_in * 2.0 / 3.0; which = 2; }
+    double newdt = gnewdt;
+    const double ratio = newdt / olddt;
+    if (ratio >= 1.0) {
+      if (ratio < prm.deltatimemultlb) { newdt = olddt; rb = 1; }
+      else if (ratio > prm.deltatimemultub) { newdt = olddt * prm.deltatimemultub; rb = 2; }
+    }
+    if (!(newdt != newdt) && (prm.dtmax != prm.dtmax || prm.dtmax < newdt)) { newdt = prm.dtmax; mb = true; }
+    dt_pre = newdt;
+  }
+  bool t1 = false;
+  if (dt_pre < targetdt && targetdt < 4.0 * dt_pre / 3.0) { targetdt = 2.0 * dt_pre / 3.0; t1 = true; }
+  const bool t2 = targetdt < dt_pre;
+  double Lpre = 0.0;
+  if (t2) {
+    if (t1) Lpre += (2.0 / 3.0) * Ldt;
+    else Ltime += -Ldt;  // dt = stoptime - time
+  } else {
+    Lpre += Ldt;
+  }
+  if (!adaptive) { Ldt_prev += Lpre; return; }
+  if (mb) return;
+  if (rb == 1) { Ldt_prev += Lpre; return; }
+  if (rb == 2) { Ldt_prev += prm.deltatimemultub * Lpre; return; }
+  if (which == 1) Ldtc += 0.5 * Lpre;
+  else if (which == 2) Ldth += (2.0 / 3.0) * Lpre;
+}
+
+// Closes the transpose of one cycle (one block): sums the kernels' partial
+// adjoints of dt and hgcoef in a fixed order, then transposes time += dt and
+// timeIncrement! on the carried scalar adjoints.
+__global__ void __launch_bounds__(kAdjBlock) ka_cycle_close(AdjDev a, int ge, int gn, const CycleRec* rec,
+                                                             AdjScal* sc, Params prm) {
+  const double s_kin = block_fixed_sum(a.part_dt, ge);
+  const double s_node = block_fixed_sum(a.part_dtn, gn);
+  const double s_hg = block_fixed_sum(a.part_hg, ge);
+  if (threadIdx.x != 0) return;
+  const CycleRec r = *rec;
+  AdjScal v = *sc;
+  v.Lhg += s_hg;
+  // a minimum the cycle did not reach leaves the scalar as it was
+  double Ldtc_prev = r.active_c ? 0.0 : v.Ldtc, Ldth_prev = r.active_h ? 0.0 : v.Ldth;
+  // time_n = time_{n-1} + dt_n
+  const double Ldt_tot = v.Ldt + (s_kin + s_node) + v.Ltime;
+  double Ldt_prev = 0.0;
+  time_increment_reverse(r, prm, Ldt_tot, v.Ltime, Ldt_prev, Ldtc_prev, Ldth_prev);
+  v.Ldt = Ldt_prev;
+  v.Ldtc = Ldtc_prev;
+  v.Ldth = Ldth_prev;
+  *sc = v;
+}
+
+// Start of a taped cycle (one thread): folds the previous cycle's minima,
+// records timeIncrement!'s inputs, advances time and records the new dt.
+__global__ void ka_tape_begin(DevState* st, CycleRec* rec, Params prm) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (st->acc_courant != kInfBits) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
+  if (st->acc_hydro != kInfBits) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
+  st->acc_courant = kInfBits;
+  st->acc_hydro = kInfBits;
+  CycleRec r;
+  r.time_prev = st->time;
+  r.dt_prev = st->deltatime;
+  r.dtc_in = st->dtcourant;
+  r.dth_in = st->dthydro;
+  r.cycle_prev = st->cycle;
+  double time = st->time, dt = st->deltatime;
+  long long cycle = st->cycle;
+  time_increment(time, dt, cycle, st->dtcourant, st->dthydro, prm);
+  st->time = time;
+  st->deltatime = dt;
+  st->cycle = cycle;
+  r.dt = dt;
+  r.active_c = r.active_h = 0;
+  r.argmin_c = r.argmin_h = INT_MAX;
+  *rec = r;
+}
+
+// End of a taped cycle (one thread): which minima the cycle reached.
+__global__ void ka_tape_end(const DevState* st, CycleRec* rec) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  rec->active_c = st->acc_courant != kInfBits;
+  rec->active_h = st->acc_hydro != kInfBits;
+}
+
+// Smallest element index whose dt candidate equals the cycle's minimum: the
+// element the reference's strict-less-than scan keeps (src/domain.jl:3003-3008).
+__global__ void __launch_bounds__(kAdjBlock) ka_argmin(const double* cand, int E, const DevState* st, int which,
                                                         int* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < E && (unsigned long long)__double_as_longlong(cand[i]) == minbits) atomicMin(out, i);
+  const unsigned long long minbits = which ? st->acc_hydro : st->acc_courant;
+  if (minbits == kInfBits || i >= E) return;
+  if ((unsigned long long)__double_as_longlong(cand[i]) == minbits) atomicMin(out, i);
+}
+
+// Copies the 11 state fields (node fields n < N, element fields n < E).
+__global__ void __launch_bounds__(kAdjBlock) ka_copy_state(StateSet src, StateSet dst, int E, int N) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < N) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) dst.f[k][i] = src.f[k][i];
+  }
+  if (i < E) {
+#pragma unroll
+    for (int k = 6; k < 11; ++k) dst.f[k][i] = src.f[k][i];
+  }
 }
 
 // Loss seed and value: L = sum_e w_e e + sum_n 0.5 w_n |u|^2 with

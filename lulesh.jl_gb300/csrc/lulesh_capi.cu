@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -89,7 +90,7 @@ void lulesh::state_to_device_mirror(lulesh_domain* d) {
   s->acc_hydro = kInfBits;
   s->status = 0u;
   s->done = 0;
-  s->iters_left = 0;
+  s->num_iters = LLONG_MAX;  // no cycle limit unless a run sets one
   s->first = 1;
 }
 
@@ -198,8 +199,7 @@ static int ensure_ring(lulesh_domain* d) {
 
 // Launches one cycle's kernels; with timing on, brackets each kernel with
 // events from the ring (reading the ring back first when it is full).
-static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_increment,
-                       long long num_iters, bool timed) {
+static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_increment, bool timed) {
   const bool aux = d->params.keep_aux != 0;
   cudaStream_t s = d->stream;
   cudaEvent_t* ev = nullptr;
@@ -211,7 +211,7 @@ static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_incre
     d->ring_used += 1;
   }
   if (ev) cudaEventRecord(ev[0], s);
-  if (with_time_increment) launch_time_increment(d->dd.st, 1, prm, num_iters, s);
+  if (with_time_increment) launch_time_increment(d->dd.st, 1, prm, s);
   if (ev) cudaEventRecord(ev[1], s);
   launch_force(d->dd, prm, d->tuning, s);
   if (ev) cudaEventRecord(ev[2], s);
@@ -376,7 +376,7 @@ int lulesh_lagrange_leapfrog(lulesh_domain* d) {
   state_to_device_mirror(d);
   int rc;
   if ((rc = h2d(d->dd.st, d->hst, 1, d->stream))) return rc;
-  if ((rc = launch_step(d, prm, false, 0, d->timing))) return rc;
+  if ((rc = launch_step(d, prm, false, d->timing))) return rc;
   if ((rc = d2h(d->hst, d->dd.st, 1, d->stream))) return rc;
   CK(cudaStreamSynchronize(d->stream));
   if (d->timing && (rc = collect_times(d))) return rc;
@@ -389,6 +389,7 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
   CK(cudaSetDevice(d->params.device));
   const Params prm = make_params(d);
   state_to_device_mirror(d);
+  d->hst->num_iters = num_iters;
   int rc;
   cudaStream_t s = d->stream;
   if ((rc = h2d(d->dd.st, d->hst, 1, s))) return rc;
@@ -399,7 +400,7 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
     // per-kernel events and no graph; the host polls the done flag every
     // kPollCyclesTimed cycles
     for (int64_t k = 0; k < budget; ++k) {
-      if ((rc = launch_step(d, prm, true, num_iters, true))) return rc;
+      if ((rc = launch_step(d, prm, true, true))) return rc;
       if ((k + 1) % kPollCyclesTimed == 0) {
         if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
         CK(cudaStreamSynchronize(s));
@@ -408,18 +409,18 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
     }
     if ((rc = collect_times(d))) return rc;
   } else {
-    // one graph = kGraphCycles cycles; rebuilt when the parameters change
-    const int64_t key = num_iters;
-    if (!d->graph || d->graph_key != key) {
+    // one graph = kGraphCycles cycles; rebuilt when a parameter it bakes in
+    // changes (the run limit is read from the device state)
+    if (!d->graph) {
       drop_graph(d);
       cudaGraph_t g;
       CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      for (int c = 0; c < kGraphCycles; ++c) launch_step(d, prm, true, num_iters, false);
+      for (int c = 0; c < kGraphCycles; ++c) launch_step(d, prm, true, false);
       CK(cudaStreamEndCapture(s, &g));
       cudaError_t e = cudaGraphInstantiate(&d->graph, g, 0);
       cudaGraphDestroy(g);
       CK(e);
-      d->graph_key = key;
+      d->graph_key = 0;
     }
     int64_t launched = 0;
     for (;;) {
@@ -460,8 +461,12 @@ int lulesh_get_scalar(const lulesh_domain* d, int32_t id, double* v) {
 int lulesh_set_scalar(lulesh_domain* d, int32_t id, double v) {
   if (!d || id < 0 || id >= LULESH_S_COUNT) return LULESH_ERR_ARGUMENT;
   if (id == LULESH_S_CYCLE && (v < 0 || v != std::floor(v))) return LULESH_ERR_ARGUMENT;
+  const bool state = id == LULESH_S_TIME || id == LULESH_S_DELTATIME || id == LULESH_S_DTCOURANT ||
+                     id == LULESH_S_DTHYDRO || id == LULESH_S_CYCLE;
+  // the other scalars are kernel parameters baked into the captured graph;
+  // the step state is uploaded at the start of every call
+  if (!state && !(d->sc[id] == v)) drop_graph(d);
   d->sc[id] = v;
-  drop_graph(d);  // parameters are baked into the captured graph
   return LULESH_OK;
 }
 

@@ -130,8 +130,8 @@ static void drop_graph(lulesh_ensemble* s) {
   s->graph_key = -1;
 }
 
-static void launch_cycle(lulesh_ensemble* s, long long num_iters) {
-  launch_time_increment(s->dd.st, s->n, s->prm, num_iters, s->stream);
+static void launch_cycle(lulesh_ensemble* s) {
+  launch_time_increment(s->dd.st, s->n, s->prm, s->stream);
   launch_force(s->dd, s->prm, s->tuning, s->stream);
   launch_node(s->dd, s->prm, false, s->tuning, s->stream);
   launch_kinematics(s->dd, s->prm, false, s->tuning, s->stream);
@@ -241,6 +241,7 @@ int lulesh_ens_create(const lulesh_instance* instances, int32_t n, int32_t mode,
     std::memset(&st, 0, sizeof(st));
     st.time = 0.0; st.deltatime = m.deltatime; st.dtcourant = 1e20; st.dthydro = 1e20; st.cycle = 0;
     st.acc_courant = kInfBits; st.acc_hydro = kInfBits; st.status = 0; st.done = 0; st.first = 1;
+    st.num_iters = LLONG_MAX;
   };
   {
     const int workers = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -316,19 +317,21 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
     if (d.acc_hydro != kInfBits) { std::memcpy(&d.dthydro, &d.acc_hydro, 8); d.acc_hydro = kInfBits; }
     if (d.status == 0u) d.done = 0;
     d.first = 1;
+    d.num_iters = num_iters;
     budget = std::max<int64_t>(budget, num_iters - d.cycle);
   }
   ECK(cudaMemcpyAsync(s->dd.st, s->hst, sizeof(DevState) * s->n, cudaMemcpyHostToDevice, st));
-  if (!s->graph || s->graph_key != num_iters) {
+  // the run limit lives in the device state, so one graph serves every call
+  if (!s->graph) {
     drop_graph(s);
     cudaGraph_t g;
     ECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int c = 0; c < kGraphCycles; ++c) launch_cycle(s, num_iters);
+    for (int c = 0; c < kGraphCycles; ++c) launch_cycle(s);
     ECK(cudaStreamEndCapture(st, &g));
     cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
     cudaGraphDestroy(g);
     ECK(e);
-    s->graph_key = num_iters;
+    s->graph_key = 0;
   }
   int64_t launched = 0;
   for (;;) {

@@ -73,7 +73,7 @@ struct DevState {
   unsigned long long acc_courant, acc_hydro;
   unsigned int status;
   int done;             // device run loop: 1 once stoptime/num_iters/error is reached
-  long long iters_left;  // device run loop: cycles still allowed
+  long long num_iters;   // device run loop: stop once cycle >= num_iters (after the first)
   long long first;       // device run loop: 1 before the first cycle of a run call
 };
 

@@ -653,7 +653,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 // ---------------------------------------------------------------------------
 // k_time_increment (device run loop): one thread per problem
 // ---------------------------------------------------------------------------
-__device__ void advance_time(DevState* st, const Params& prm, long long num_iters) {
+__device__ void advance_time(DevState* st, const Params& prm) {
   if (st->done) return;
   if (st->status) { st->done = 1; return; }
   // fold the previous step's minima (src/domain.jl:3012-3014, 3050-3052)
@@ -662,7 +662,7 @@ __device__ void advance_time(DevState* st, const Params& prm, long long num_iter
   st->acc_courant = kInfBits;
   st->acc_hydro = kInfBits;
   // examples/benchmark.jl:82-98: while time < stoptime ... break if cycle >= num_iters
-  if (!(st->time < prm.stoptime) || (!st->first && st->cycle >= num_iters)) { st->done = 1; return; }
+  if (!(st->time < prm.stoptime) || (!st->first && st->cycle >= st->num_iters)) { st->done = 1; return; }
   st->first = 0;
   double time = st->time, dt = st->deltatime;
   long long cycle = st->cycle;
@@ -672,9 +672,9 @@ __device__ void advance_time(DevState* st, const Params& prm, long long num_iter
   st->cycle = cycle;
 }
 
-__global__ void k_time_increment(DevState* st, int n, Params prm, long long num_iters) {
+__global__ void k_time_increment(DevState* st, int n, Params prm) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) advance_time(st + k, prm, num_iters);
+  if (k < n) advance_time(st + k, prm);
 }
 
 // ---------------------------------------------------------------------------
@@ -733,8 +733,8 @@ void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuni
   }
 }
 
-void launch_time_increment(DevState* st, int n, const Params& prm, long long num_iters, cudaStream_t s) {
-  k_time_increment<<<(n + 127) / 128, 128, 0, s>>>(st, n, prm, num_iters);
+void launch_time_increment(DevState* st, int n, const Params& prm, cudaStream_t s) {
+  k_time_increment<<<(n + 127) / 128, 128, 0, s>>>(st, n, prm);
 }
 
 }  // namespace lulesh

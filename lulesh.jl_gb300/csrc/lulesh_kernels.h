@@ -26,7 +26,7 @@ void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaSt
 void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
 void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
 void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
-void launch_time_increment(DevState* st, int n, const Params& prm, long long num_iters, cudaStream_t s);
+void launch_time_increment(DevState* st, int n, const Params& prm, cudaStream_t s);
 
 // Picks block sizes for the four step kernels by timing them on the live
 // problem (lulesh_tune.cu); the state advances, so callers save and restore it.

@@ -38,7 +38,7 @@ cudaError_t autotune_blocks(const DevDomain& d, const Params& prm, bool aux, int
       *slot = cand[j];
       float total = 0.f;
       for (int c = 0; c <= cycles && err == cudaSuccess; ++c) {  // cycle 0 warms up
-        launch_time_increment(d.st, ninst, prm, LLONG_MAX, s);
+        launch_time_increment(d.st, ninst, prm, s);
         for (int q = 0; q < 4; ++q) {
           if (q == k) cudaEventRecord(e0, s);
           launch_phase(q, d, prm, aux, t, s);

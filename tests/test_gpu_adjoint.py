@@ -209,3 +209,42 @@ def test_gradient_matches_central_fd(gpu_lib):
         an = float(np.dot(ge, de)) + ghg * dhg
         assert an == pytest.approx(fd, rel=2e-6, abs=1e-9 * abs(adj.result.loss)), (k, an, fd)
     adj.close()
+
+
+def test_c5_gradient_matches_dual_oracle_full_size(gpu_lib, oracle_mod):
+    """The 48^3, 200-cycle gradient (checkpoints every 20) of the energy
+    within r < 0.3 w.r.t. e0 and hgcoef, origin energy the default and the
+    others U[0, 1e-3] (seed 0xC5), against the dual-number oracle's exact JVP
+    along one direction (seed 0xF0)."""
+    L = gpu_lib
+    nx, cycles, radius = 48, 200, 0.3
+    g = L.Domain(L.LuleshProblem(nx=nx))
+    rng = np.random.default_rng(0xC5)
+    e0 = g.e
+    e0[1:] = rng.uniform(0.0, 1e-3, g.numElem - 1)
+    g.e = e0
+    snap = snapshot(g)
+    adj = L.Adjoint(g, radius=radius, checkpoint_every=20)
+    loss = adj.gradient(cycles)
+    assert adj.result.cycles == cycles and adj.result.checkpoints == 10
+    ge, ghg = adj.grad("e"), adj.result.grad_hgcoef
+    adj.close()
+    drng = np.random.default_rng(0xF0)
+    de = drng.standard_normal(g.numElem) * e0
+    dhg = drng.standard_normal() * snap[1]["hgcoef"]
+    d = dual_from(oracle_mod, snap, nx, 0)
+    d.set_field("e", e0, de)
+    d.set("hgcoef", snap[1]["hgcoef"], dhg)
+    assert d.cycles(cycles) == 0
+    we, wn = energy_weights(nx, radius, d.field("elemMass")[0], d.field("nodalMass")[0])
+    e, te = d.field("e")
+    ref_loss, jvp = float(np.dot(we, e)), float(np.dot(we, te))
+    jscale = float(np.dot(np.abs(we), np.abs(te)))
+    for c in ("xd", "yd", "zd"):
+        u, tu = d.field(c)
+        ref_loss += 0.5 * float(np.dot(wn, u * u))
+        jvp += float(np.dot(wn, u * tu))
+        jscale += float(np.dot(np.abs(wn), np.abs(u * tu)))
+    assert loss == pytest.approx(ref_loss, rel=1e-9)
+    vjp = float(np.dot(ge, de)) + ghg * dhg
+    assert close(jvp, vjp, jscale, 1e-8), (jvp, vjp, jscale)
