@@ -59,6 +59,7 @@ struct CycleTape {
   double *vnew, *delv, *arealg, *vdov, *dv[3], *dx[3];
   unsigned long long* flags;
   double *dtc, *dth;
+  double* geo;  // [48][E] force-kernel tape
 };
 
 struct Scalars5 {
@@ -159,7 +160,7 @@ static void tape_cycle(lulesh_adjoint* a, const CycleTape& tp, CycleRec* rec) {
   td.delx_xi = tp.dx[0]; td.delx_eta = tp.dx[1]; td.delx_zeta = tp.dx[2];
   td.xdd = tp.ax; td.ydd = tp.ay; td.zdd = tp.az;
   td.fx = a->fx_s; td.fy = a->fy_s; td.fz = a->fz_s;
-  td.tapeFlags = tp.flags; td.tapeDtc = tp.dtc; td.tapeDth = tp.dth;
+  td.tapeFlags = tp.flags; td.tapeDtc = tp.dtc; td.tapeDth = tp.dth; td.tapeGeo = tp.geo;
   launch_force(td, prm, d->tuning, s);
   launch_node(td, prm, true, d->tuning, s);  // aux: the node kernel stores the accelerations
   launch_kinematics(td, prm, false, d->tuning, s);
@@ -179,6 +180,7 @@ static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const Stat
   ad.vnew = t.vnew; ad.delv = t.delv; ad.arealg = t.arealg; ad.vdov = t.vdov;
   for (int k = 0; k < 3; ++k) { ad.dvl[k] = t.dv[k]; ad.dxl[k] = t.dx[k]; }
   ad.flags = t.flags;
+  ad.geo = t.geo;
 }
 
 // Transpose of one recorded cycle, queued on the stream: the adjoint state
@@ -190,12 +192,11 @@ static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec) {
   const Params prm = make_params(d);
   const int ge = (a->E + kAdjBlock - 1) / kAdjBlock, gn = (a->N + kAdjBlock - 1) / kAdjBlock;
   const int mode = d->dd.mode;
-  if (mode & 4) ka_material<4><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, rec, a->dsc);
-  else ka_material<0><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, rec, a->dsc);
-  ka_nb_gather<<<ge, kAdjBlock, 0, s>>>(a->ad);
-  ka_kinematics<<<ge, kAdjBlock, 0, s>>>(a->ad, rec);
-  ka_gather_corners<<<gn, kAdjBlock, 0, s>>>(a->ad);
-  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, rec);
+  const double irho0 = 1.0 / prm.refdens;
+  if (mode & 4) ka_material<4><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, irho0, rec, a->dsc);
+  else ka_material<0><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, irho0, rec, a->dsc);
+  ka_kinematics<<<ge, kAdjBlock, 0, s>>>(a->ad, rec);  // also gathers the limiter's neighbour reads
+  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, rec);        // also gathers the kinematics corners
   const double hg = d->sc[LULESH_S_HGCOEF];
 #define LULESH_KA_FORCE(M)                                   \
   ka_hourglass<M><<<ge, kAdjBlock, 0, s>>>(a->ad, hg);       \
@@ -208,7 +209,7 @@ static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec) {
   }
 #undef LULESH_KA_FORCE
   ka_gather_corners<<<gn, kAdjBlock, 0, s>>>(a->ad);
-  ka_cycle_close<<<1, kAdjBlock, 0, s>>>(a->ad, ge, gn, rec, a->dsc, prm);
+  ka_cycle_close<<<1, kCloseBlock, 0, s>>>(a->ad, ge, gn, rec, a->dsc, prm);
 }
 
 static double* adj_field(lulesh_adjoint* a, int32_t f) {
@@ -301,7 +302,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
     if ((rc = dalloc(a, &t.ax, N)) || (rc = dalloc(a, &t.ay, N)) || (rc = dalloc(a, &t.az, N)) ||
         (rc = dalloc(a, &t.vnew, E)) || (rc = dalloc(a, &t.delv, E)) || (rc = dalloc(a, &t.arealg, E)) ||
         (rc = dalloc(a, &t.vdov, E)) || (rc = dalloc(a, &t.flags, E)) || (rc = dalloc(a, &t.dtc, E)) ||
-        (rc = dalloc(a, &t.dth, E)))
+        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 48 * (size_t)E)))
       return fail(rc);
     for (int k = 0; k < 3; ++k)
       if ((rc = dalloc(a, &t.dv[k], E)) || (rc = dalloc(a, &t.dx[k], E))) return fail(rc);

@@ -58,6 +58,7 @@ struct AdjDev {
   const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
   const double *dvl[3], *dxl[3];              // delv_{xi,eta,zeta}, delx_{xi,eta,zeta}
   const unsigned long long* flags;
+  const double* geo;                          // [48][E] force-kernel tape (dv, hms, S)
   // adjoints of the state (in place: S1 on entry, S0 on exit)
   double *lx, *ly, *lz, *lxd, *lyd, *lzd;     // N
   double *le, *lp, *lq, *lss, *lv;            // E
@@ -81,13 +82,6 @@ __device__ __forceinline__ void block_sum_to(double v, double* out) {
     __syncthreads();
   }
   if (threadIdx.x == 0) out[blockIdx.x] = sh[0];
-}
-
-// Walsh sign of node n in direction a (xi, eta, zeta) as walsh1 uses it.
-__device__ __forceinline__ double walsh_sign(int a, int n) {
-  if (a == 0) return ((n == 1) | (n == 2) | (n == 5) | (n == 6)) ? 1.0 : -1.0;
-  if (a == 1) return ((n == 2) | (n == 3) | (n == 6) | (n == 7)) ? 1.0 : -1.0;
-  return (n >= 4) ? 1.0 : -1.0;
 }
 
 struct V3 {
@@ -121,7 +115,7 @@ __device__ __forceinline__ int limiter_index(unsigned mask, unsigned bits, unsig
 // Courant and hydro candidates).
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, const CycleRec* rec,
+__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, double irho0, const CycleRec* rec,
                                                           const AdjScal* sc) {
   const int E = a.E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,14 +151,19 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
            : src == PHI_ZERO ? 0.0 : prm.monoq_max_slope;
     delx[d] = a.dxl[d][i];
   }
-  const double vdov = a.vdov[i], vnew = a.vnew[i], volo = a.volo[i], mass = a.elemMass[i];
+  const double vdov = a.vdov[i], vnew = a.vnew[i], mass = a.elemMass[i];
   const double delvc = a.delv[i], arealg = a.arealg[i];
+  const bool vmin_c = (fl & TF_VNEW_MIN) != 0, vmax_c = (fl & TF_VNEW_MAX) != 0;
+  const double vnewc = vmin_c ? prm.eosvmin : vmax_c ? prm.eosvmax : vnew;
+  // reciprocals shared by the recompute and the transpose
+  const double inv_vnewc = 1.0 / vnewc;
+  const double inv_vnew = (vnewc == vnew) ? inv_vnewc : 1.0 / vnew;
   const bool qzero = (fl & TF_QZERO) != 0;
   double dx[3] = {0.0, 0.0, 0.0}, rho = 0.0, qlin = 0.0, qquad = 0.0, s1sum = 0.0, s2sum = 0.0;
   if (!qzero) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) dx[d] = (fl & (TF_DXCLAMP0 << d)) ? 0.0 : self[d] * delx[d];
-    rho = mass / (volo * vnew);
+    rho = (mass * a.inv_volo[i]) * inv_vnew;
     s1sum = fma(dx[0], 1.0 - phi[0], fma(dx[1], 1.0 - phi[1], dx[2] * (1.0 - phi[2])));
     s2sum = fma(dx[0] * dx[0], fma(-phi[0], phi[0], 1.0),
                 fma(dx[1] * dx[1], fma(-phi[1], phi[1], 1.0), (dx[2] * dx[2]) * fma(-phi[2], phi[2], 1.0)));
@@ -172,27 +171,34 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
     qquad = (prm.qqc_monoq * rho) * s2sum;
   }
   // EOS forward (values only; branches from the tape)
-  const bool vmin_c = (fl & TF_VNEW_MIN) != 0, vmax_c = (fl & TF_VNEW_MAX) != 0;
-  const double vnewc = vmin_c ? prm.eosvmin : vmax_c ? prm.eosvmax : vnew;
   const bool vmax_hit = (fl & TF_VMAX_HIT) != 0, half_eq = (fl & TF_HALF_EQ_COMP) != 0;
   const double p_old = vmax_hit ? 0.0 : a.p0[i], q_old = a.q0[i], e_old = a.e0[i];
-  const double compression = vmax_hit ? 0.0 : 1.0 / vnewc - 1.0;
+  const double compression = vmax_hit ? 0.0 : inv_vnewc - 1.0;
   const double vchalf = fma(delvc, -0.5, vnewc);
-  const double chs = vmax_hit ? 0.0 : half_eq ? compression : 1.0 / vchalf - 1.0;
-  const double c1s = 2.0 / 3.0, irho0 = 1.0 / prm.refdens;
+  const double inv_vchalf = (vmax_hit || half_eq) ? 0.0 : 1.0 / vchalf;
+  const double chs = vmax_hit ? 0.0 : half_eq ? compression : inv_vchalf - 1.0;
+  const double c1s = 2.0 / 3.0;  // irho0 = 1 / refdens
   const double pq = p_old + q_old;
   const bool e1min = (fl & TF_E1_MIN) != 0;
   const double e1 = e1min ? prm.emin : fma(-0.5 * delvc, pq, e_old);
   const double bvc_h = c1s * (chs + 1.0);
   const bool pH_on = !vmax_hit && !(fl & (TF_PH_CUT | TF_PH_MIN));
   const double pH = pH_on ? bvc_h * e1 : (fl & TF_PH_MIN) ? prm.pmin : 0.0;
-  const double vhalf = 1.0 / (1.0 + chs);
+  // vhalf = 1 / (1 + compHalfStep), which is vchalf, vnewc or 1 by the branch taken
+  const double vhalf = vmax_hit ? 1.0 : half_eq ? vnewc : vchalf;
   const bool comp = (fl & TF_COMPRESS) != 0;
   const bool s1t = (fl & TF_S1_TINY) != 0, s2t = (fl & TF_S2_TINY) != 0, sst = (fl & TF_SS_TINY) != 0;
-  double ssc1 = 0.0, s1 = 0.0, qn1 = 0.0;
+  // each square root s = sqrt(c) comes with h = 0.5 / s = 0.5 rsqrt(c)
+  double ssc1 = 0.0, s1 = 0.0, h1 = 0.0, qn1 = 0.0;
   if (comp) {
     ssc1 = fma(c1s, e1, ((vhalf * vhalf) * bvc_h) * pH) * irho0;
-    s1 = s1t ? 0.333333e-18 : sqrt(ssc1);
+    if (s1t) {
+      s1 = 0.333333e-18;
+    } else {
+      const double r = rsqrt(ssc1);
+      s1 = ssc1 * r;
+      h1 = 0.5 * r;
+    }
     qn1 = fma(s1, qlin, qquad);
   }
   const bool e2fix = (fl & (TF_E2_CUT | TF_E2_MIN)) != 0;
@@ -202,10 +208,16 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   const bool pn1_on = !vmax_hit && !(fl & (TF_PN1_CUT | TF_PN1_MIN));
   const double pn1 = pn1_on ? bvc * e2 : (fl & TF_PN1_MIN) ? prm.pmin : 0.0;
   const double vv_bvc = (vnewc * vnewc) * bvc;
-  double ssc2 = 0.0, s2 = 0.0, qt = 0.0;
+  double ssc2 = 0.0, s2 = 0.0, h2 = 0.0, qt = 0.0;
   if (comp) {
     ssc2 = fma(c1s, e2, vv_bvc * pn1) * irho0;
-    s2 = s2t ? 0.333333e-18 : sqrt(ssc2);
+    if (s2t) {
+      s2 = 0.333333e-18;
+    } else {
+      const double r = rsqrt(ssc2);
+      s2 = ssc2 * r;
+      h2 = 0.5 * r;
+    }
     qt = fma(s2, qlin, qquad);
   }
   const double k3 = fma(7.0, pq, -8.0 * (pH + qn1)) + (pn1 + qt);
@@ -214,7 +226,12 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   const bool pn2_on = !vmax_hit && !(fl & (TF_PN2_CUT | TF_PN2_MIN));
   const double pn2 = pn2_on ? bvc * e3 : (fl & TF_PN2_MIN) ? prm.pmin : 0.0;
   const double ssc3 = fma(c1s, e3, vv_bvc * pn2) * irho0;
-  const double ss = sst ? 0.333333e-18 : sqrt(ssc3);
+  double ss = 0.333333e-18, hs = 0.0;
+  if (!sst) {
+    const double r = rsqrt(ssc3);
+    ss = ssc3 * r;
+    hs = 0.5 * r;
+  }
 
   // ---------------- reverse ----------------
   double Le3 = a.le[i], Lpn2 = a.lp[i], Lq = a.lq[i], Lss = a.lss[i], Lv1 = a.lv[i];
@@ -244,7 +261,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   double Lvv = 0.0, Lbvc = 0.0, Le2 = 0.0, Lpn1 = 0.0, Lpq = 0.0, LpH = 0.0, Lqn1 = 0.0, Lqt = 0.0;
   // ss = sqrt(ssc3)
   if (!sst) {
-    const double Lssc = Lss * 0.5 / ss * irho0;
+    const double Lssc = Lss * hs * irho0;
     Le3 += Lssc * c1s;
     Lvv += Lssc * pn2;
     Lpn2 += Lssc * vv_bvc;
@@ -259,7 +276,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   if (comp) {
     Lqlin += Lqt * s2; Lqquad += Lqt;
     if (!s2t) {
-      const double Lssc = Lqt * qlin * 0.5 / s2 * irho0;
+      const double Lssc = Lqt * qlin * h2 * irho0;
       Le2 += Lssc * c1s;
       Lvv += Lssc * pn1;
       Lpn1 += Lssc * vv_bvc;
@@ -280,7 +297,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   if (comp) {
     Lqlin += Lqn1 * s1; Lqquad += Lqn1;
     if (!s1t) {
-      const double Lssc = Lqn1 * qlin * 0.5 / s1 * irho0;
+      const double Lssc = Lqn1 * qlin * h1 * irho0;
       Le1 += Lssc * c1s;
       const double Lvhalf = Lssc * 2.0 * vhalf * bvc_h * pH;
       Lbvch += Lssc * (vhalf * vhalf) * pH;
@@ -302,11 +319,11 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   if (!vmax_hit) {
     if (half_eq) Lcomp += Lchs;
     else {
-      const double Lvch = -Lchs / (vchalf * vchalf);
+      const double Lvch = -Lchs * (inv_vchalf * inv_vchalf);
       Lvnewc += Lvch;
       Ldelvc += -0.5 * Lvch;
     }
-    Lvnewc += -Lcomp / (vnewc * vnewc);
+    Lvnewc += -Lcomp * (inv_vnewc * inv_vnewc);
   }
   if (!vmin_c && !vmax_c) Lvnew += Lvnewc;
   // qlin / qquad
@@ -321,7 +338,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
       Lphi[d] = Lqlin * (prm.qlc_monoq * rho) * dx[d] + Lqquad * (-prm.qqc_monoq * rho) * dx[d] * dx[d] * 2.0 * phi[d];
       if (!(fl & (TF_DXCLAMP0 << d))) { Lself[d] += Ldxd * delx[d]; Ldx[d] += Ldxd * self[d]; }
     }
-    Lvnew += -Lrho * rho / vnew;
+    Lvnew += -Lrho * rho * inv_vnew;
   }
   // limiter
 #pragma unroll
@@ -354,20 +371,15 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, c
   a.lv[i] = 0.0;
 }
 
-// Limiter neighbour transposes: every element adds the slots of the
-// elements that read its delv (inverse neighbour list, fixed order).
-__global__ void __launch_bounds__(kAdjBlock) ka_nb_gather(AdjDev a) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= a.E) return;
-  double s[3] = {a.ldv[0][k], a.ldv[1][k], a.ldv[2][k]};
-  for (int j = a.nbStart[k]; j < a.nbStart[k + 1]; ++j) {
-    const int ent = a.nbList[j];
-    const int slot = ent / a.E;
-    s[slot >> 1] += a.lnb[ent];
-  }
-  a.ldv[0][k] = s[0];
-  a.ldv[1][k] = s[1];
-  a.ldv[2][k] = s[2];
+// Transpose of walsh1: adds dL/dv of the 8 corner values for the adjoints
+// Lw of the three coefficients (through the body diagonals, 14 adds).
+__device__ __forceinline__ void walsh1_t(const double Lw[3], double L[8]) {
+  const double p = Lw[0] + Lw[2], q = Lw[2] - Lw[0];
+  const double La = p + Lw[1], Lb = p - Lw[1], Lc = q + Lw[1], Ld = q - Lw[1];
+  L[6] += La; L[0] -= La;
+  L[5] += Lb; L[3] -= Lb;
+  L[7] += Lc; L[1] -= Lc;
+  L[4] += Ld; L[2] -= Ld;
 }
 
 // ---------------------------------------------------------------------------
@@ -414,6 +426,17 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       const double vol = volo * vnew;
       const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
       double Lvol = 0.0, Lnorm64 = 0.0;
+      // limiter reads of this element's delv by its neighbours (inverse
+      // neighbour list, fixed order) join its own delv adjoints
+      double Ldvs[3] = {a.ldv[0][e], a.ldv[1][e], a.ldv[2][e]};
+      for (int j = a.nbStart[e]; j < a.nbStart[e + 1]; ++j) {
+        const int ent = a.nbList[j];
+        const int dir = (ent / E) >> 1;
+        const double v = a.lnb[ent];
+        if (dir == 0) Ldvs[0] += v;
+        else if (dir == 1) Ldvs[1] += v;
+        else Ldvs[2] += v;
+      }
       // direction d uses A = P x Q and velocity vector VW[d]
       const int Pi[3] = {1, 2, 0}, Qi[3] = {2, 0, 1};
 #pragma unroll
@@ -422,7 +445,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
         const V3 A = vcross(P, Q);
         const double s2 = fma(A.x, A.x, fma(A.y, A.y, fma(A.z, A.z, 256.0 * ptiny)));
         const double rs = rsqrt(s2);
-        const double Ldx = a.ldx[d][e], Ldv = a.ldv[d][e];
+        const double Ldx = a.ldx[d][e], Ldv = Ldvs[d];
         Lvol += Ldx * 16.0 * rs;
         const double Ls2 = Ldx * 16.0 * vol * (-0.5) * rs * rs * rs;
         V3 LA = v3(2.0 * A.x * Ls2, 2.0 * A.y * Ls2, 2.0 * A.z * Ls2);
@@ -473,14 +496,14 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       }
     }
     // Walsh transposes
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        const double s = walsh_sign(d, c);
-        LX[0][c] = fma(s, LW[d].x, LX[0][c]); LX[1][c] = fma(s, LW[d].y, LX[1][c]); LX[2][c] = fma(s, LW[d].z, LX[2][c]);
-        LV[0][c] = fma(s, LVW[d].x, LV[0][c]); LV[1][c] = fma(s, LVW[d].y, LV[1][c]); LV[2][c] = fma(s, LVW[d].z, LV[2][c]);
-      }
+    {
+      const double lwx[3] = {LW[0].x, LW[1].x, LW[2].x}, lwy[3] = {LW[0].y, LW[1].y, LW[2].y},
+                   lwz[3] = {LW[0].z, LW[1].z, LW[2].z};
+      walsh1_t(lwx, LX[0]); walsh1_t(lwy, LX[1]); walsh1_t(lwz, LX[2]);
+      const double lvx[3] = {LVW[0].x, LVW[1].x, LVW[2].x}, lvy[3] = {LVW[0].y, LVW[1].y, LVW[2].y},
+                   lvz[3] = {LVW[0].z, LVW[1].z, LVW[2].z};
+      walsh1_t(lvx, LV[0]); walsh1_t(lvy, LV[1]); walsh1_t(lvz, LV[2]);
+    }
     // ---- volume and characteristic length ----
     {
       auto dg = [&](int p, int q) { return v3(X[0][p] - X[0][q], X[1][p] - X[1][q], X[2][p] - X[2][q]); };
@@ -493,17 +516,22 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       const double v12 = vdot(U1, vcross(d63, d20)) + vdot(U2, vcross(d64, d70)) + vdot(U3, vcross(d61, d50));
       const double volume = v12 * (1.0 / 12.0);
       // characteristic length from the face the tape recorded
+      // (selected without indexing, so the diagonals stay in registers)
       const int f = (int)((a.flags[e] >> TF_FACE_SHIFT) & 7ull);
-      const V3 fa[6] = {d20, d64, d50, d61, d72, d43};
-      const V3 fb[6] = {d31, d57, d14, d25, d63, d70};
-      const V3 nf = vcross(fa[f], fb[f]);
+      V3 fa = d20, fb = d31;
+      if (f == 1) { fa = d64; fb = d57; }
+      else if (f == 2) { fa = d50; fb = d14; }
+      else if (f == 3) { fa = d61; fb = d25; }
+      else if (f == 4) { fa = d72; fb = d63; }
+      else if (f == 5) { fa = d43; fb = d70; }
+      const V3 nf = vcross(fa, fb);
       const double cl = vdot(nf, nf);
       const double rsc = rsqrt(cl);
       const double Lar = a.larealg[e];
       double Lvolume = Lar * 2.0 * rsc + Lvnew * a.inv_volo[e];
       const double Lcl = Lar * 2.0 * volume * (-0.5) * rsc * rsc * rsc;
       const V3 Ln = v3(2.0 * nf.x * Lcl, 2.0 * nf.y * Lcl, 2.0 * nf.z * Lcl);
-      const V3 Lfa = vcross(fb[f], Ln), Lfb = vcross(Ln, fa[f]);
+      const V3 Lfa = vcross(fb, Ln), Lfb = vcross(Ln, fa);
       const double Lv12 = Lvolume * (1.0 / 12.0);
       // gradients of the diagonals
       V3 L61 = v3(0, 0, 0), L70 = v3(0, 0, 0), L63 = v3(0, 0, 0), L20 = v3(0, 0, 0), L50 = v3(0, 0, 0), L64 = v3(0, 0, 0);
@@ -516,11 +544,12 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
         const V3 gU3 = vcross(d61, d50), gV3 = vcross(d50, U3), gW3 = vcross(U3, d61);
         vaxpy(L14, Lv12, gU3); vaxpy(L25, Lv12, gU3); vaxpy(L61, Lv12, gV3); vaxpy(L50, Lv12, gW3);
       }
-      V3* Lfa_t[6] = {&L20, &L64, &L50, &L61, &L72, &L43};
-      V3* Lfb_t[6] = {&L31, &L57, &L14, &L25, &L63, &L70};
-#pragma unroll
-      for (int q = 0; q < 6; ++q)
-        if (q == f) { vadd(*Lfa_t[q], Lfa); vadd(*Lfb_t[q], Lfb); }
+      if (f == 0) { vadd(L20, Lfa); vadd(L31, Lfb); }
+      else if (f == 1) { vadd(L64, Lfa); vadd(L57, Lfb); }
+      else if (f == 2) { vadd(L50, Lfa); vadd(L14, Lfb); }
+      else if (f == 3) { vadd(L61, Lfa); vadd(L25, Lfb); }
+      else if (f == 4) { vadd(L72, Lfa); vadd(L63, Lfb); }
+      else { vadd(L43, Lfa); vadd(L70, Lfb); }
       auto put = [&](const V3& L, int p, int q) {
         LX[0][p] += L.x; LX[1][p] += L.y; LX[2][p] += L.z;
         LX[0][q] -= L.x; LX[1][q] -= L.y; LX[2][q] -= L.z;
@@ -571,11 +600,22 @@ __global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, const CycleRec* r
     double* Lf[3] = {a.lfx, a.lfy, a.lfz};
     const double* xd1[3] = {a.xd1, a.yd1, a.zd1};
     const double* acc[3] = {a.ax, a.ay, a.az};
+    // the kinematics transpose's corner adjoints join the end-state adjoints
+    double gx[3] = {0.0, 0.0, 0.0}, gv[3] = {0.0, 0.0, 0.0};
+    {
+      const int s = a.nodeElemStart[i], t = a.nodeElemStart[i + 1];
+      const long long E8 = 8ll * a.E;
+      for (int j = s; j < t; ++j) {
+        const int c = a.cornerList[j];
+#pragma unroll
+        for (int k = 0; k < 3; ++k) { gx[k] += a.cX[k * E8 + c]; gv[k] += a.cV[k * E8 + c]; }
+      }
+    }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double lxn = Lx[k][i];
+      const double lxn = Lx[k][i] + gx[k];
       const double v1 = xd1[k][i];
-      double lv = Lxd[k][i] + lxn * dt;   // x1 = x0 + xd1*dt
+      double lv = (Lxd[k][i] + gv[k]) + lxn * dt;   // x1 = x0 + xd1*dt
       Ldt += lxn * v1;
       double lf = 0.0;
       if (v1 == 0.0) {
@@ -659,48 +699,34 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
 #pragma unroll
       for (int k = 0; k < 12; ++k) a.sLhm[k * E + e] = 0.0;
     } else {
-      const double* Xp[3] = {a.x0, a.y0, a.z0};
       const double* Vp[3] = {a.xd0, a.yd0, a.zd0};
       const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+      // the forward kernel's volume derivatives and scaled modes, from the tape
       double hms[3][4], dv[3][8];
-      {
-        double X[3][8];
-#pragma unroll
-        for (int k = 0; k < 3; ++k)
-#pragma unroll
-          for (int c = 0; c < 8; ++c) X[k][c] = Xp[k][nd[c]];
-        double w1[3];
-#pragma unroll
-        for (int k = 0; k < 3; ++k) walsh7(X[k], w1, hms[k]);
-        constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
-        constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
-        double ex[12], ey[12], ez[12];
-#pragma unroll
-        for (int j = 0; j < 12; ++j) {
-          ex[j] = X[0][ea[j]] + X[0][eb[j]];
-          ey[j] = X[1][ea[j]] + X[1][eb[j]];
-          ez[j] = X[2][ea[j]] + X[2][eb[j]];
-        }
-        volu_der<MODE>(ex, ey, ez, dv);
-      }
-      const double determ = a.volo[e] * a.v0[e];
-      const double vi12 = 1.0 / (12.0 * determ);
 #pragma unroll
       for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int m = 0; m < 4; ++m) hms[j][m] *= vi12;
+        for (int c = 0; c < 8; ++c) dv[j][c] = a.geo[(j * 8 + c) * E + e];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int m = 0; m < 4; ++m) hms[j][m] = a.geo[(24 + j * 4 + m) * E + e];
+      const double determ = a.volo[e] * a.v0[e];
+      const double inv_det = 1.0 / determ;
+      const double vi12 = inv_det * (1.0 / 12.0);
       const double ss = a.ss0[e], mass = a.elemMass[e];
       const double r = rcbrt(determ);
       const double c0 = -hgcoef * 0.01;
       const double coef = ((c0 * ss) * mass) * r;
-      // S_k, D[k][j] = V_k . dv_j and T_k, C[k][j] = lf_k . dv_j
+      // S_k (taped), D[k][j] = V_k . dv_j and T_k, C[k][j] = lf_k . dv_j
       double S[3][4], T[3][4], D[3][3], C[3][3];
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
         double u[8], w2[4], w1[3];
 #pragma unroll
+        for (int m = 0; m < 4; ++m) S[k][m] = a.geo[(36 + 4 * k + m) * E + e];
+#pragma unroll
         for (int c = 0; c < 8; ++c) u[c] = Vp[k][nd[c]];
-        walsh7(u, w1, w2);
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           double s = dv[j][0] * u[0];
@@ -708,9 +734,6 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
           for (int c = 1; c < 8; ++c) s = fma(dv[j][c], u[c], s);
           D[k][j] = s;
         }
-#pragma unroll
-        for (int m = 0; m < 4; ++m)
-          S[k][m] = fma(-hms[2][m], D[k][2], fma(-hms[1][m], D[k][1], fma(-hms[0][m], D[k][0], w2[m])));
 #pragma unroll
         for (int c = 0; c < 8; ++c) u[c] = Lf[k][nd[c]];
         walsh7(u, w1, w2);
@@ -748,7 +771,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
           const double Lhms = -coef * fma(S[0][m], C[0][j], fma(S[1][m], C[1][j], fma(S[2][m], C[2][j],
                               fma(T[0][m], D[0][j], fma(T[1][m], D[1][j], T[2][m] * D[2][j])))));
           Lvi12 = fma(Lhms, hms[j][m], Lvi12);
-          a.sLhm[(j * 4 + m) * E + e] = vi12 * Lhms;
+          a.sLhm[(j * 4 + m) * E + e] = vi12 * Lhms;  // hms = vi12 * hm
         }
       // dL/dV_k = coef (Gamma^T T_k - sum_j dv_j B[k][j])
 #pragma unroll
@@ -784,7 +807,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
       // coef = c0 ss mass determ^(-1/3), vi12 = 1/(12 determ), determ = volo v
       a.lss[e] += Lcoef * c0 * mass * r;
       Lhg_coef = Lcoef * (-0.01) * ss * mass * r;
-      const double Ldeterm = Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r / determ - Lvi12 / determ;
+      const double Ldeterm = (Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r - Lvi12) * inv_det;
       a.lv[e] += Ldeterm * a.volo[e];
     }
   }
@@ -883,25 +906,26 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
       const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
       N[f] = vcross(d1, d2);
     }
-    double Ls8 = 0.0;
-    V3 LN[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
+    // sum_n lf_n . B_n = sum_f N_f . LU_f with LU_f the sum of lf over the
+    // face's nodes (node 1's quirk included); the normals' adjoints are s8 LU_f
+    V3 LU[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
       const V3 lf = v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]);
-      V3 B = N[nf[n][0]]; vadd(B, N[nf[n][1]]); vadd(B, N[nf[n][2]]);
-      const V3 LB = v3(s8 * lf.x, s8 * lf.y, s8 * lf.z);
       if (n == 0 && !(MODE & 1)) {
         // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice and no areaZ
-        B.y += N[4].y;
-        B.z -= N[4].z;
-        Ls8 += vdot(lf, B);
-        LN[0].x += LB.x; LN[1].x += LB.x; LN[4].x += LB.x;
-        LN[0].y += LB.y; LN[1].y += LB.y; LN[4].y += 2.0 * LB.y;
-        LN[0].z += LB.z; LN[1].z += LB.z;
+        vadd(LU[0], lf); vadd(LU[1], lf);
+        LU[4].x += lf.x; LU[4].y = fma(2.0, lf.y, LU[4].y);
       } else {
-        Ls8 += vdot(lf, B);
-        vadd(LN[nf[n][0]], LB); vadd(LN[nf[n][1]], LB); vadd(LN[nf[n][2]], LB);
+        vadd(LU[nf[n][0]], lf); vadd(LU[nf[n][1]], lf); vadd(LU[nf[n][2]], lf);
       }
+    }
+    double Ls8 = 0.0;
+    V3 LN[6];
+#pragma unroll
+    for (int f = 0; f < 6; ++f) {
+      Ls8 += vdot(N[f], LU[f]);
+      LN[f] = v3(s8 * LU[f].x, s8 * LU[f].y, s8 * LU[f].z);
     }
     const double Lpq = -0.125 * Ls8;
     a.lp[e] += Lpq;
@@ -923,14 +947,16 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
     for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
 }
 
-// Sum of `n` partials in a fixed order by one block; every thread gets it.
+// Sum of `n` partials in a fixed order by one block of BS threads; every
+// thread gets it.
+template <int BS>
 __device__ double block_fixed_sum(const double* part, int n) {
-  __shared__ double sh[kAdjBlock];
+  __shared__ double sh[BS];
   double s = 0.0;
-  for (int j = threadIdx.x; j < n; j += blockDim.x) s += part[j];
+  for (int j = threadIdx.x; j < n; j += BS) s += part[j];
   sh[threadIdx.x] = s;
   __syncthreads();
-  for (int w = kAdjBlock / 2; w > 0; w >>= 1) {
+  for (int w = BS / 2; w > 0; w >>= 1) {
     if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
     __syncthreads();
   }
@@ -941,7 +967,7 @@ __device__ double block_fixed_sum(const double* part, int n) {
 
 // Sums `n` partials in a fixed order (one block).
 __global__ void __launch_bounds__(kAdjBlock) ka_sum(const double* part, int n, double* out) {
-  const double s = block_fixed_sum(part, n);
+  const double s = block_fixed_sum<kAdjBlock>(part, n);
   if (threadIdx.x == 0) *out = s;
 }
 
@@ -991,11 +1017,12 @@ __host__ __device__ inline void time_increment_reverse(const CycleRec& r, const 
 // Closes the transpose of one cycle (one block): sums the kernels' partial
 // adjoints of dt and hgcoef in a fixed order, then transposes time += dt and
 // timeIncrement! on the carried scalar adjoints.
-__global__ void __launch_bounds__(kAdjBlock) ka_cycle_close(AdjDev a, int ge, int gn, const CycleRec* rec,
-                                                             AdjScal* sc, Params prm) {
-  const double s_kin = block_fixed_sum(a.part_dt, ge);
-  const double s_node = block_fixed_sum(a.part_dtn, gn);
-  const double s_hg = block_fixed_sum(a.part_hg, ge);
+constexpr int kCloseBlock = 1024;
+__global__ void __launch_bounds__(kCloseBlock) ka_cycle_close(AdjDev a, int ge, int gn, const CycleRec* rec,
+                                                               AdjScal* sc, Params prm) {
+  const double s_kin = block_fixed_sum<kCloseBlock>(a.part_dt, ge);
+  const double s_node = block_fixed_sum<kCloseBlock>(a.part_dtn, gn);
+  const double s_hg = block_fixed_sum<kCloseBlock>(a.part_hg, ge);
   if (threadIdx.x != 0) return;
   const CycleRec r = *rec;
   AdjScal v = *sc;

@@ -116,6 +116,10 @@ struct DevDomain {
   unsigned long long* tapeFlags;
   double* tapeDtc;
   double* tapeDth;
+  // [48][E]: the force kernel's volume derivatives dv_j[n] (24, node order),
+  // hourglass modes over 12*determ (12) and mode sums S_k[m] of the
+  // velocities (12)
+  double* tapeGeo;
 };
 
 }  // namespace lulesh

@@ -29,7 +29,7 @@ __device__ __forceinline__ bool step_off(const DevState* st) {
 // ---------------------------------------------------------------------------
 // k_force
 // ---------------------------------------------------------------------------
-template <int MODE, bool ENS>
+template <int MODE, bool ENS, bool TAPE>
 __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -157,6 +157,20 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     const double vi12 = 1.0 / (12.0 * determ);
 #pragma unroll
     for (int m = 0; m < 4; ++m) { hmx[m] *= vi12; hmy[m] *= vi12; hmz[m] *= vi12; }
+    if (TAPE) {
+#pragma unroll
+      for (int n = 0; n < 8; ++n) {
+        d.tapeGeo[n * E + e] = dvx[n];
+        d.tapeGeo[(8 + n) * E + e] = dvy[n];
+        d.tapeGeo[(16 + n) * E + e] = dvz[n];
+      }
+#pragma unroll
+      for (int m = 0; m < 4; ++m) {
+        d.tapeGeo[(24 + m) * E + e] = hmx[m];
+        d.tapeGeo[(28 + m) * E + e] = hmy[m];
+        d.tapeGeo[(32 + m) * E + e] = hmz[m];
+      }
+    }
     double hg[8][4];
 #pragma unroll
     for (int n = 0; n < 8; ++n)
@@ -183,6 +197,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
         double s = hg[0][m] * vv[0];
 #pragma unroll
         for (int n = 1; n < 8; ++n) s = fma(hg[n][m], vv[n], s);
+        if (TAPE) d.tapeGeo[(36 + 4 * k + m) * E + e] = s;
         h[m] = coef * s;
       }
 #pragma unroll
@@ -686,8 +701,10 @@ void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaSt
   const int bs = t.force;
   const int grid = (d.E + bs - 1) / bs;
   const bool ens = d.elemInst != nullptr;
-#define LULESH_FORCE(M) \
-  (ens ? k_force<M, true><<<grid, bs, 0, s>>>(d, prm) : k_force<M, false><<<grid, bs, 0, s>>>(d, prm))
+#define LULESH_FORCE(M)                                                      \
+  (ens ? k_force<M, true, false><<<grid, bs, 0, s>>>(d, prm)                  \
+       : d.tapeGeo ? k_force<M, false, true><<<grid, bs, 0, s>>>(d, prm)      \
+                   : k_force<M, false, false><<<grid, bs, 0, s>>>(d, prm))
   switch (d.mode & 3) {
     case 0: LULESH_FORCE(0); break;
     case 1: LULESH_FORCE(1); break;
