@@ -60,6 +60,8 @@ struct CycleTape {
   unsigned long long* flags;
   double *dtc, *dth;
   double* geo;  // [48][E] force-kernel tape
+  double* kin;  // [45][E] kinematics-kernel tape
+  double* mat;  // [31][E] material-kernel tape
 };
 
 struct Scalars5 {
@@ -161,6 +163,7 @@ static void tape_cycle(lulesh_adjoint* a, const CycleTape& tp, CycleRec* rec) {
   td.xdd = tp.ax; td.ydd = tp.ay; td.zdd = tp.az;
   td.fx = a->fx_s; td.fy = a->fy_s; td.fz = a->fz_s;
   td.tapeFlags = tp.flags; td.tapeDtc = tp.dtc; td.tapeDth = tp.dth; td.tapeGeo = tp.geo;
+  td.tapeKin = tp.kin; td.tapeMat = tp.mat;
   launch_force(td, prm, d->tuning, s);
   launch_node(td, prm, true, d->tuning, s);  // aux: the node kernel stores the accelerations
   launch_kinematics(td, prm, false, d->tuning, s);
@@ -181,6 +184,8 @@ static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const Stat
   for (int k = 0; k < 3; ++k) { ad.dvl[k] = t.dv[k]; ad.dxl[k] = t.dx[k]; }
   ad.flags = t.flags;
   ad.geo = t.geo;
+  ad.kin = t.kin;
+  ad.mat = t.mat;
 }
 
 // Transpose of one recorded cycle, queued on the stream: the adjoint state
@@ -302,7 +307,8 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
     if ((rc = dalloc(a, &t.ax, N)) || (rc = dalloc(a, &t.ay, N)) || (rc = dalloc(a, &t.az, N)) ||
         (rc = dalloc(a, &t.vnew, E)) || (rc = dalloc(a, &t.delv, E)) || (rc = dalloc(a, &t.arealg, E)) ||
         (rc = dalloc(a, &t.vdov, E)) || (rc = dalloc(a, &t.flags, E)) || (rc = dalloc(a, &t.dtc, E)) ||
-        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 48 * (size_t)E)))
+        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 48 * (size_t)E)) ||
+        (rc = dalloc(a, &t.kin, 45 * (size_t)E)) || (rc = dalloc(a, &t.mat, 31 * (size_t)E)))
       return fail(rc);
     for (int k = 0; k < 3; ++k)
       if ((rc = dalloc(a, &t.dv[k], E)) || (rc = dalloc(a, &t.dx[k], E))) return fail(rc);

@@ -58,7 +58,9 @@ struct AdjDev {
   const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
   const double *dvl[3], *dxl[3];              // delv_{xi,eta,zeta}, delx_{xi,eta,zeta}
   const unsigned long long* flags;
-  const double* geo;                          // [48][E] force-kernel tape (dv, hms, S)
+  const double* geo;
+  const double* kin;                          // [45][E] kinematics-kernel tape
+  const double* mat;                          // [31][E] material-kernel tape                          // [48][E] force-kernel tape (dv, hms, S)
   // adjoints of the state (in place: S1 on entry, S0 on exit)
   double *lx, *ly, *lz, *lxd, *lyd, *lzd;     // N
   double *le, *lp, *lq, *lss, *lv;            // E
@@ -125,7 +127,6 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
   const int argmin_c = rec->argmin_c, argmin_h = rec->argmin_h;
   const double lam_c = rec->active_c ? sc->Ldtc : 0.0, lam_h = rec->active_h ? sc->Ldth : 0.0;
   const unsigned long long fl = a.flags[i];
-  const double ptiny = 1.e-36;
   const unsigned mask = a.elemBC[i];
   // neighbour resolution exactly as the forward kernel
   int im[3], ip[3];
@@ -136,102 +137,65 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
   im[2] = limiter_index(mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, a.lzetam[i], i, E);
   ip[2] = limiter_index(mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, a.lzetap[i], i, E);
 
-  double self[3], mv[3], pv[3], norm[3], phi[3], delx[3];
+  // forward values from the material kernel's tape (slots: see tapeMat)
+  auto tm = [&](int q) { return a.mat[q * E + i]; };
+  double self[3], norm[3], tdm[3], tdp[3], phi[3], delx[3];
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     self[d] = a.dvl[d][i];
-    mv[d] = im[d] >= 0 ? a.dvl[d][im[d]] : 0.0;
-    pv[d] = ip[d] >= 0 ? a.dvl[d][ip[d]] : 0.0;
-    norm[d] = 1.0 / (self[d] + ptiny);
+    norm[d] = tm(d);
+    tdm[d] = tm(3 + d);  // minus neighbour's delv * norm
+    tdp[d] = tm(6 + d);  // plus neighbour's delv * norm
     const int src = (int)((fl >> (3 * d)) & 7ull);
-    const double dm = mv[d] * norm[d], dp = pv[d] * norm[d];
-    phi[d] = src == PHI_MEAN ? 0.5 * (dm + dp)
-           : src == PHI_M ? dm * prm.monoq_limiter_mult
-           : src == PHI_P ? dp * prm.monoq_limiter_mult
+    phi[d] = src == PHI_MEAN ? 0.5 * (tdm[d] + tdp[d])
+           : src == PHI_M ? tdm[d] * prm.monoq_limiter_mult
+           : src == PHI_P ? tdp[d] * prm.monoq_limiter_mult
            : src == PHI_ZERO ? 0.0 : prm.monoq_max_slope;
     delx[d] = a.dxl[d][i];
   }
-  const double vdov = a.vdov[i], vnew = a.vnew[i], mass = a.elemMass[i];
+  const double vdov = a.vdov[i], vnew = a.vnew[i];
   const double delvc = a.delv[i], arealg = a.arealg[i];
   const bool vmin_c = (fl & TF_VNEW_MIN) != 0, vmax_c = (fl & TF_VNEW_MAX) != 0;
   const double vnewc = vmin_c ? prm.eosvmin : vmax_c ? prm.eosvmax : vnew;
-  // reciprocals shared by the recompute and the transpose
-  const double inv_vnewc = 1.0 / vnewc;
+  const bool vmax_hit = (fl & TF_VMAX_HIT) != 0, half_eq = (fl & TF_HALF_EQ_COMP) != 0;
+  const double compression = tm(14), chs = tm(15);
+  // 1/vnewc = compression + 1 and 1/vchalf = compHalfStep + 1 on the branches
+  // where the forward formed them
+  const double inv_vnewc = vmax_hit ? 1.0 / vnewc : compression + 1.0;
   const double inv_vnew = (vnewc == vnew) ? inv_vnewc : 1.0 / vnew;
+  const double inv_vchalf = (vmax_hit || half_eq) ? 0.0 : chs + 1.0;
   const bool qzero = (fl & TF_QZERO) != 0;
-  double dx[3] = {0.0, 0.0, 0.0}, rho = 0.0, qlin = 0.0, qquad = 0.0, s1sum = 0.0, s2sum = 0.0;
+  double dx[3] = {0.0, 0.0, 0.0};
+  const double rho = tm(9), qlin = tm(10), qquad = tm(11), s1sum = tm(12), s2sum = tm(13);
   if (!qzero) {
 #pragma unroll
     for (int d = 0; d < 3; ++d) dx[d] = (fl & (TF_DXCLAMP0 << d)) ? 0.0 : self[d] * delx[d];
-    rho = (mass * a.inv_volo[i]) * inv_vnew;
-    s1sum = fma(dx[0], 1.0 - phi[0], fma(dx[1], 1.0 - phi[1], dx[2] * (1.0 - phi[2])));
-    s2sum = fma(dx[0] * dx[0], fma(-phi[0], phi[0], 1.0),
-                fma(dx[1] * dx[1], fma(-phi[1], phi[1], 1.0), (dx[2] * dx[2]) * fma(-phi[2], phi[2], 1.0)));
-    qlin = (-prm.qlc_monoq * rho) * s1sum;
-    qquad = (prm.qqc_monoq * rho) * s2sum;
   }
-  // EOS forward (values only; branches from the tape)
-  const bool vmax_hit = (fl & TF_VMAX_HIT) != 0, half_eq = (fl & TF_HALF_EQ_COMP) != 0;
-  const double p_old = vmax_hit ? 0.0 : a.p0[i], q_old = a.q0[i], e_old = a.e0[i];
-  const double compression = vmax_hit ? 0.0 : inv_vnewc - 1.0;
-  const double vchalf = fma(delvc, -0.5, vnewc);
-  const double inv_vchalf = (vmax_hit || half_eq) ? 0.0 : 1.0 / vchalf;
-  const double chs = vmax_hit ? 0.0 : half_eq ? compression : inv_vchalf - 1.0;
+  const double p_old = vmax_hit ? 0.0 : a.p0[i], q_old = a.q0[i];
   const double c1s = 2.0 / 3.0;  // irho0 = 1 / refdens
   const double pq = p_old + q_old;
   const bool e1min = (fl & TF_E1_MIN) != 0;
-  const double e1 = e1min ? prm.emin : fma(-0.5 * delvc, pq, e_old);
+  const double e1 = tm(16), pH = tm(17), vhalf = tm(18);
   const double bvc_h = c1s * (chs + 1.0);
   const bool pH_on = !vmax_hit && !(fl & (TF_PH_CUT | TF_PH_MIN));
-  const double pH = pH_on ? bvc_h * e1 : (fl & TF_PH_MIN) ? prm.pmin : 0.0;
-  // vhalf = 1 / (1 + compHalfStep), which is vchalf, vnewc or 1 by the branch taken
-  const double vhalf = vmax_hit ? 1.0 : half_eq ? vnewc : vchalf;
   const bool comp = (fl & TF_COMPRESS) != 0;
   const bool s1t = (fl & TF_S1_TINY) != 0, s2t = (fl & TF_S2_TINY) != 0, sst = (fl & TF_SS_TINY) != 0;
   // each square root s = sqrt(c) comes with h = 0.5 / s = 0.5 rsqrt(c)
-  double ssc1 = 0.0, s1 = 0.0, h1 = 0.0, qn1 = 0.0;
-  if (comp) {
-    ssc1 = fma(c1s, e1, ((vhalf * vhalf) * bvc_h) * pH) * irho0;
-    if (s1t) {
-      s1 = 0.333333e-18;
-    } else {
-      const double r = rsqrt(ssc1);
-      s1 = ssc1 * r;
-      h1 = 0.5 * r;
-    }
-    qn1 = fma(s1, qlin, qquad);
-  }
+  const double s1 = tm(19), qn1 = tm(20);
+  const double h1 = (comp && !s1t) ? 0.5 * rsqrt(tm(28)) : 0.0;
   const bool e2fix = (fl & (TF_E2_CUT | TF_E2_MIN)) != 0;
   const double k2 = fma(3.0, pq, -4.0 * (pH + qn1));
-  const double e2 = (fl & TF_E2_MIN) ? prm.emin : (fl & TF_E2_CUT) ? 0.0 : fma(0.5 * delvc, k2, e1);
+  const double e2 = tm(21), pn1 = tm(22);
   const double bvc = c1s * (compression + 1.0);
   const bool pn1_on = !vmax_hit && !(fl & (TF_PN1_CUT | TF_PN1_MIN));
-  const double pn1 = pn1_on ? bvc * e2 : (fl & TF_PN1_MIN) ? prm.pmin : 0.0;
   const double vv_bvc = (vnewc * vnewc) * bvc;
-  double ssc2 = 0.0, s2 = 0.0, h2 = 0.0, qt = 0.0;
-  if (comp) {
-    ssc2 = fma(c1s, e2, vv_bvc * pn1) * irho0;
-    if (s2t) {
-      s2 = 0.333333e-18;
-    } else {
-      const double r = rsqrt(ssc2);
-      s2 = ssc2 * r;
-      h2 = 0.5 * r;
-    }
-    qt = fma(s2, qlin, qquad);
-  }
+  const double s2 = tm(23), qt = tm(24);
+  const double h2 = (comp && !s2t) ? 0.5 * rsqrt(tm(29)) : 0.0;
   const double k3 = fma(7.0, pq, -8.0 * (pH + qn1)) + (pn1 + qt);
   const bool e3fix = (fl & (TF_E3_CUT | TF_E3_MIN)) != 0;
-  const double e3 = (fl & TF_E3_MIN) ? prm.emin : (fl & TF_E3_CUT) ? 0.0 : e2 - (k3 * delvc) * (1.0 / 6.0);
+  const double e3 = tm(25), pn2 = tm(26), ss = tm(27);
   const bool pn2_on = !vmax_hit && !(fl & (TF_PN2_CUT | TF_PN2_MIN));
-  const double pn2 = pn2_on ? bvc * e3 : (fl & TF_PN2_MIN) ? prm.pmin : 0.0;
-  const double ssc3 = fma(c1s, e3, vv_bvc * pn2) * irho0;
-  double ss = 0.333333e-18, hs = 0.0;
-  if (!sst) {
-    const double r = rsqrt(ssc3);
-    ss = ssc3 * r;
-    hs = 0.5 * r;
-  }
+  const double hs = sst ? 0.0 : 0.5 * rsqrt(tm(30));
 
   // ---------------- reverse ----------------
   double Le3 = a.le[i], Lpn2 = a.lp[i], Lq = a.lq[i], Lss = a.lss[i], Lv1 = a.lv[i];
@@ -349,8 +313,8 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
     else if (src == PHI_M) Ldm = prm.monoq_limiter_mult * Lphi[d];
     else if (src == PHI_P) Ldp = prm.monoq_limiter_mult * Lphi[d];
     const double Lm = Ldm * norm[d], Lp = Ldp * norm[d];
-    const double Lnorm = Ldm * mv[d] + Ldp * pv[d];
-    Lself[d] += -Lnorm * norm[d] * norm[d];
+    // norm = 1/(self + ptiny): d(mv norm)/dself = -(mv norm) norm
+    Lself[d] += -fma(Ldm, tdm[d], Ldp * tdp[d]) * norm[d];
     double sm = 0.0, sp = 0.0;
     if (im[d] == i) Lself[d] += Lm; else if (im[d] >= 0) sm = Lm;
     if (ip[d] == i) Lself[d] += Lp; else if (ip[d] >= 0) sp = Lp;
@@ -395,12 +359,11 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
     int nd[8];
 #pragma unroll
     for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
-    double X[3][8], V[3][8];
+    double X[3][8];
 #pragma unroll
-    for (int c = 0; c < 8; ++c) {
-      X[0][c] = a.x1[nd[c]]; X[1][c] = a.y1[nd[c]]; X[2][c] = a.z1[nd[c]];
-      V[0][c] = a.xd1[nd[c]]; V[1][c] = a.yd1[nd[c]]; V[2][c] = a.zd1[nd[c]];
-    }
+    for (int c = 0; c < 8; ++c) { X[0][c] = a.x1[nd[c]]; X[1][c] = a.y1[nd[c]]; X[2][c] = a.z1[nd[c]]; }
+    // forward values from the kinematics kernel's tape (slots: see tapeKin)
+    auto tk = [&](int q) { return a.kin[q * E + e]; };
     double LX[3][8], LV[3][8];
 #pragma unroll
     for (int k = 0; k < 3; ++k)
@@ -412,19 +375,16 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
     a.lv[e] -= a.ldelv[e];  // delv = vnew - v
     // Walsh vectors of positions and velocities
     V3 W[3], VW[3];
-    {
-      double w[3][3], vw[3][3];
 #pragma unroll
-      for (int k = 0; k < 3; ++k) { walsh1(X[k], w[k]); walsh1(V[k], vw[k]); }
-#pragma unroll
-      for (int d = 0; d < 3; ++d) { W[d] = v3(w[0][d], w[1][d], w[2][d]); VW[d] = v3(vw[0][d], vw[1][d], vw[2][d]); }
+    for (int d = 0; d < 3; ++d) {
+      W[d] = v3(tk(d), tk(3 + d), tk(6 + d));
+      VW[d] = v3(tk(9 + d), tk(12 + d), tk(15 + d));
     }
     V3 LW[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)}, LVW[3] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
     // ---- monotonic-Q gradients ----
     {
-      const double ptiny = 1.e-36;
       const double vol = volo * vnew;
-      const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
+      const double norm64 = tk(40);  // 1/(64 vol + 64 ptiny)
       double Lvol = 0.0, Lnorm64 = 0.0;
       // limiter reads of this element's delv by its neighbours (inverse
       // neighbour list, fixed order) join its own delv adjoints
@@ -442,9 +402,8 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
         const V3 P = W[Pi[d]], Q = W[Qi[d]];
-        const V3 A = vcross(P, Q);
-        const double s2 = fma(A.x, A.x, fma(A.y, A.y, fma(A.z, A.z, 256.0 * ptiny)));
-        const double rs = rsqrt(s2);
+        const V3 A = v3(tk(28 + 3 * d), tk(29 + 3 * d), tk(30 + 3 * d));  // P x Q
+        const double rs = tk(37 + d);  // 1/sqrt(|A|^2 + 256 ptiny)
         const double Ldx = a.ldx[d][e], Ldv = Ldvs[d];
         Lvol += Ldx * 16.0 * rs;
         const double Ls2 = Ldx * 16.0 * vol * (-0.5) * rs * rs * rs;
@@ -467,11 +426,10 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       for (int d = 0; d < 3; ++d) {
         F[d] = v3(fma(dt2, VW[d].x, W[d].x), fma(dt2, VW[d].y, W[d].y), fma(dt2, VW[d].z, W[d].z));
       }
-      const V3 C0 = vcross(F[1], F[2]), C1 = vcross(F[2], F[0]), C2 = vcross(F[0], F[1]);
-      const double det = vdot(F[1], C1);
-      const double s = vdot(C0, VW[0]) + vdot(C1, VW[1]) + vdot(C2, VW[2]);
-      const double inv = 1.0 / det;
-      const double vdov = s * inv;
+      // cofactor columns C0 = F1 x F2, C1 = F2 x F0, C2 = F0 x F1 and 1/det
+      const V3 C0 = v3(tk(18), tk(19), tk(20)), C1 = v3(tk(21), tk(22), tk(23)), C2 = v3(tk(24), tk(25), tk(26));
+      const double inv = tk(27);
+      const double vdov = a.vdov[e];
       const double Ls = a.lvdov[e] * inv;
       const double Ldet = -a.lvdov[e] * vdov * inv;
       V3 LC[3];
@@ -513,8 +471,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       V3 U1 = d31; vadd(U1, d72);
       V3 U2 = d43; vadd(U2, d57);
       V3 U3 = d14; vadd(U3, d25);
-      const double v12 = vdot(U1, vcross(d63, d20)) + vdot(U2, vcross(d64, d70)) + vdot(U3, vcross(d61, d50));
-      const double volume = v12 * (1.0 / 12.0);
+      const double volume = vnew * volo;  // vnew = volume / volo
       // characteristic length from the face the tape recorded
       // (selected without indexing, so the diagonals stay in registers)
       const int f = (int)((a.flags[e] >> TF_FACE_SHIFT) & 7ull);
@@ -524,9 +481,8 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       else if (f == 3) { fa = d61; fb = d25; }
       else if (f == 4) { fa = d72; fb = d63; }
       else if (f == 5) { fa = d43; fb = d70; }
-      const V3 nf = vcross(fa, fb);
-      const double cl = vdot(nf, nf);
-      const double rsc = rsqrt(cl);
+      const V3 nf = v3(tk(41), tk(42), tk(43));  // fa x fb
+      const double rsc = tk(44);                  // 1/|fa x fb|
       const double Lar = a.larealg[e];
       double Lvolume = Lar * 2.0 * rsc + Lvnew * a.inv_volo[e];
       const double Lcl = Lar * 2.0 * volume * (-0.5) * rsc * rsc * rsc;

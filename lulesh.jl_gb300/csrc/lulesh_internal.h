@@ -120,6 +120,16 @@ struct DevDomain {
   // hourglass modes over 12*determ (12) and mode sums S_k[m] of the
   // velocities (12)
   double* tapeGeo;
+  // [45][E]: the kinematics kernel's Walsh vectors of positions (9) and
+  // velocities (9), cofactor columns (9), 1/det (1), monotonic-Q cross
+  // products (9) with their reciprocal norms (3), 1/(64 vol) (1), the largest
+  // face's diagonal cross product (3) and rsqrt of its square norm (1)
+  double* tapeKin;
+  // [31][E]: the material kernel's limiter terms (norm, scaled neighbours:
+  // 9), Q terms (rho, qlin, qquad, and their two sums: 5) and EOS values
+  // (compression, compHalfStep, e1, pHalf, vhalf, s1, q1, e2, p1, s2, q2, e3,
+  // p2, ss: 14; the three squared sound speeds: 3)
+  double* tapeMat;
 };
 
 }  // namespace lulesh

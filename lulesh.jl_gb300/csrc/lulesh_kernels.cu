@@ -305,11 +305,15 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     // diagonals a, b, |f|^2|g|^2 - (f.g)^2 = |f x g|^2 = 4 |a x b|^2; the 4
     // is folded into arealg below.
     int fidx = 0;
+    double fcx = 0.0, fcy = 0.0, fcz = 0.0;  // the largest face's cross product (TAPE)
     auto face = [&](const double* a, const double* b, int f) {
       double cx, cy, cz;
       cross(a[0], a[1], a[2], b[0], b[1], b[2], cx, cy, cz);
       const double area4 = fma(cx, cx, fma(cy, cy, cz * cz));
-      if (TAPE && area4 > charLength) fidx = f;
+      if (TAPE && (f == 0 || area4 > charLength)) {
+        fidx = f;
+        fcx = cx; fcy = cy; fcz = cz;
+      }
       charLength = fmax(area4, charLength);
     };
     face(d20, d31, 0);   // nodes 1,2,3,4
@@ -318,14 +322,21 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     face(d61, d25, 3);   // 2,3,7,6
     face(d72, d63, 4);   // 3,4,8,7
     face(d43, d70, 5);   // 4,1,5,8
-    if (TAPE) d.tapeFlags[e] = (unsigned long long)fidx << TF_FACE_SHIFT;
+    if (TAPE) {
+      d.tapeFlags[e] = (unsigned long long)fidx << TF_FACE_SHIFT;
+      d.tapeKin[41 * E + e] = fcx; d.tapeKin[42 * E + e] = fcy; d.tapeKin[43 * E + e] = fcz;
+    }
   }
   const double vnew = volume * LDG(&d.inv_volo[e]);
   if (le_zero(vnew)) atomicOr(&st->status, ST_KINEMATICS);
   d.vnew[e] = vnew;
   d.delv[e] = vnew - LDG(&d.v[e]);
   // 4*volume/sqrt(max area) with area = 4*area4
-  d.arealg[e] = (2.0 * volume) * rsqrt(charLength);
+  {
+    const double rcl = rsqrt(charLength);
+    d.arealg[e] = (2.0 * volume) * rcl;
+    if (TAPE) d.tapeKin[44 * E + e] = rcl;
+  }
 
   // Velocity gradient trace at the half-step position (src/domain.jl:2128-2158)
   double wx[3], wy[3], wz[3];
@@ -342,6 +353,13 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
 #pragma unroll
     for (int c = 0; c < 8; ++c) v8[c] = LDG(&d.zd[nd[c]]);
     walsh1(v8, vzw);
+  }
+  if (TAPE) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      d.tapeKin[a * E + e] = wx[a]; d.tapeKin[(3 + a) * E + e] = wy[a]; d.tapeKin[(6 + a) * E + e] = wz[a];
+      d.tapeKin[(9 + a) * E + e] = vxw[a]; d.tapeKin[(12 + a) * E + e] = vyw[a]; d.tapeKin[(15 + a) * E + e] = vzw[a];
+    }
   }
   {
     const double dt2 = -0.5 * dt;
@@ -369,6 +387,13 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     const double inv = 1.0 / det;
     const double vdov = ((d1 + d2) + d3) * inv;
     d.vdov[e] = vdov;
+    if (TAPE) {
+      // cofactor columns C_xi, C_eta, C_zeta (x, y, z each), then 1/det
+      const double cof[9] = {Cxxi, Cyxi, Czxi, Cxet, Cyet, Czet, Cxze, Cyze, Czze};
+#pragma unroll
+      for (int q = 0; q < 9; ++q) d.tapeKin[(18 + q) * E + e] = cof[q];
+      d.tapeKin[27 * E + e] = inv;
+    }
     if (AUX) {
       const double third = vdov / 3.0;
       d.dxx[e] = d1 * inv - third;
@@ -385,19 +410,33 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     const double vol = LDG(&d.volo[e]) * vnew;
     const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
     const double vol16 = 16.0 * vol;
-    double ax, ay, az;
+    double ax, ay, az, rs;
+    // taped per direction d (xi, eta, zeta): the cross product A and 1/|A|
+    auto tape_a = [&](int dir) {
+      if (TAPE) {
+        d.tapeKin[(28 + 3 * dir) * E + e] = ax; d.tapeKin[(29 + 3 * dir) * E + e] = ay;
+        d.tapeKin[(30 + 3 * dir) * E + e] = az; d.tapeKin[(37 + dir) * E + e] = rs;
+      }
+    };
+    if (TAPE) d.tapeKin[40 * E + e] = norm64;
     // zeta: xi x eta
     cross(wx[0], wy[0], wz[0], wx[1], wy[1], wz[1], ax, ay, az);
-    d.delx_zeta[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    rs = rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delx_zeta[e] = vol16 * rs;
     d.delv_zeta[e] = norm64 * fma(ax, vxw[2], fma(ay, vyw[2], az * vzw[2]));
+    tape_a(2);
     // xi: eta x zeta
     cross(wx[1], wy[1], wz[1], wx[2], wy[2], wz[2], ax, ay, az);
-    d.delx_xi[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    rs = rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delx_xi[e] = vol16 * rs;
     d.delv_xi[e] = norm64 * fma(ax, vxw[0], fma(ay, vyw[0], az * vzw[0]));
+    tape_a(0);
     // eta: zeta x xi
     cross(wx[2], wy[2], wz[2], wx[0], wy[0], wz[0], ax, ay, az);
-    d.delx_eta[e] = vol16 * rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    rs = rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
+    d.delx_eta[e] = vol16 * rs;
     d.delv_eta[e] = norm64 * fma(ax, vxw[1], fma(ay, vyw[1], az * vzw[1]));
+    tape_a(1);
   }
 }
 
@@ -407,10 +446,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
 
 // One limiter direction, src/domain.jl:2330-2376. `src` reports which value
 // the result is (PHI_*), for the adjoint's tape.
-__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm, int& src) {
+__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm, int& src,
+                                            double& t_norm, double& t_dm, double& t_dp) {
   const double norm = 1.0 / (self + 1.e-36);
   dm *= norm;
   dp *= norm;
+  t_norm = norm; t_dm = dm; t_dp = dp;  // kept for the adjoint's tape
   double phi = 0.5 * (dm + dp);
   src = PHI_MEAN;
   dm *= prm.monoq_limiter_mult;
@@ -519,15 +560,22 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const int ixp = (MODE & 4) ? LDG(&d.lxip[i]) : LDG(&d.lxip[i]) - 1;
     double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
     double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
-    const double phixi = monoq_phi(dvxi, dm, dp, prm, src0);
+    double tl[9];  // limiter terms per direction: norm, dm/norm, dp/norm (TAPE)
+    const double phixi = monoq_phi(dvxi, dm, dp, prm, src0, tl[0], tl[3], tl[6]);
     dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);
-    const double phieta = monoq_phi(dveta, dm, dp, prm, src1);
+    const double phieta = monoq_phi(dveta, dm, dp, prm, src1, tl[1], tl[4], tl[7]);
     dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, E, bad);
-    const double phizeta = monoq_phi(dvzeta, dm, dp, prm, src2);
+    const double phizeta = monoq_phi(dvzeta, dm, dp, prm, src2, tl[2], tl[5], tl[8]);
     if (bad) err |= ST_BAD_BC;
-    if (TAPE) fl |= (unsigned long long)(src0 | (src1 << 3) | (src2 << 6));
+    // d.tapeMat slot q of this element (TAPE only)
+    auto tm = [&](int q, double v) { if (TAPE) d.tapeMat[q * E + i] = v; };
+    if (TAPE) {
+      fl |= (unsigned long long)(src0 | (src1 << 3) | (src2 << 6));
+#pragma unroll
+      for (int q = 0; q < 9; ++q) tm(q, tl[q]);
+    }
 
     const double vdov = LDG(&d.vdov[i]);
     const double vnew = LDG(&d.vnew[i]);
@@ -536,7 +584,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     if (gt_zero(vdov)) {
       qlin = 0.0;
       qquad = 0.0;
-      if (TAPE) fl |= TF_QZERO;
+      if (TAPE) {
+        fl |= TF_QZERO;
+#pragma unroll
+        for (int q = 9; q < 14; ++q) tm(q, 0.0);
+      }
     } else {
       double dxxi = dvxi * LDG(&d.delx_xi[i]);
       double dxeta = dveta * LDG(&d.delx_eta[i]);
@@ -545,11 +597,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       if (gt_zero(dxeta)) { dxeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 1; }
       if (gt_zero(dxzeta)) { dxzeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 2; }
       const double rho = LDG(&d.elemMass[i]) / (volo * vnew);
-      qlin = (-prm.qlc_monoq * rho) *
-             fma(dxxi, 1.0 - phixi, fma(dxeta, 1.0 - phieta, dxzeta * (1.0 - phizeta)));
-      qquad = (prm.qqc_monoq * rho) *
-              fma(dxxi * dxxi, fma(-phixi, phixi, 1.0),
-                  fma(dxeta * dxeta, fma(-phieta, phieta, 1.0), (dxzeta * dxzeta) * fma(-phizeta, phizeta, 1.0)));
+      const double s1sum = fma(dxxi, 1.0 - phixi, fma(dxeta, 1.0 - phieta, dxzeta * (1.0 - phizeta)));
+      const double s2sum = fma(dxxi * dxxi, fma(-phixi, phixi, 1.0),
+                               fma(dxeta * dxeta, fma(-phieta, phieta, 1.0), (dxzeta * dxzeta) * fma(-phizeta, phizeta, 1.0)));
+      qlin = (-prm.qlc_monoq * rho) * s1sum;
+      qquad = (prm.qqc_monoq * rho) * s2sum;
+      tm(9, rho); tm(10, qlin); tm(11, qquad); tm(12, s1sum); tm(13, s2sum);
     }
     if (AUX) { d.ql[i] = qlin; d.qq[i] = qquad; }
 
@@ -606,28 +659,42 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const double vhalf = 1.0 / (1.0 + compHalfStep);
     const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
     if (TAPE && compress) fl |= TF_COMPRESS;
+    tm(14, compression); tm(15, compHalfStep); tm(16, e_new); tm(17, pHalfStep); tm(18, vhalf);
     double q_new = 0.0;
     if (compress) {
       const double ssc = fma(c1s, e_new, ((vhalf * vhalf) * bvc_half) * pHalfStep) * inv_rho0;
-      q_new = fma(tiny_sqrt(ssc, TF_S1_TINY), qlin, qquad);
+      const double s1 = tiny_sqrt(ssc, TF_S1_TINY);
+      q_new = fma(s1, qlin, qquad);
+      tm(19, s1); tm(28, ssc);
+    } else {
+      tm(19, 0.0); tm(28, 0.0);
     }
+    tm(20, q_new);
     e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E2_CUT; }
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
     const double bvc = c1s * (compression + 1.0);
     double p_new = pressure(e_new, bvc, TF_PN1_CUT, TF_PN1_MIN);
     const double vv_bvc = (vnewc * vnewc) * bvc;
+    tm(21, e_new); tm(22, p_new);
     double q_tilde = 0.0;
     if (compress) {
       const double ssc = fma(c1s, e_new, vv_bvc * p_new) * inv_rho0;
-      q_tilde = fma(tiny_sqrt(ssc, TF_S2_TINY), qlin, qquad);
+      const double s2 = tiny_sqrt(ssc, TF_S2_TINY);
+      q_tilde = fma(s2, qlin, qquad);
+      tm(23, s2); tm(29, ssc);
+    } else {
+      tm(23, 0.0); tm(29, 0.0);
     }
+    tm(24, q_tilde);
     e_new = e_new - ((fma(7.0, pq_old, -8.0 * (pHalfStep + q_new)) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E3_CUT; }
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
     p_new = pressure(e_new, bvc, TF_PN2_CUT, TF_PN2_MIN);
     // the last q evaluation and the sound speed share one expression
-    const double ss_new = tiny_sqrt(fma(c1s, e_new, vv_bvc * p_new) * inv_rho0, TF_SS_TINY);
+    const double ssc3 = fma(c1s, e_new, vv_bvc * p_new) * inv_rho0;
+    const double ss_new = tiny_sqrt(ssc3, TF_SS_TINY);
+    tm(25, e_new); tm(26, p_new); tm(27, ss_new); tm(30, ssc3);
     if (compress) {
       q_new = fma(ss_new, qlin, qquad);
       if (abs_lt(q_new, prm.q_cut)) { q_new = 0.0; if (TAPE) fl |= TF_Q_CUT; }
