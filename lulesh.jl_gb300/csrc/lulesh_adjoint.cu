@@ -59,7 +59,7 @@ struct CycleTape {
   double *vnew, *delv, *arealg, *vdov, *dv[3], *dx[3];
   unsigned long long* flags;
   double *dtc, *dth;
-  double* geo;  // [48][E] force-kernel tape
+  double* geo;  // [66][E] force-kernel tape
   double* kin;  // [45][E] kinematics-kernel tape
   double* mat;  // [31][E] material-kernel tape
 };
@@ -147,15 +147,17 @@ static void set_scalars(lulesh_domain* d, const Scalars5& s) {
   d->sc[LULESH_S_CYCLE] = (double)s.cycle;
 }
 
-// One taped cycle, queued on the stream: timeIncrement! on the device
-// (recorded), the step kernels with the cycle's kinematics outputs,
-// accelerations, branch flags and dt candidates going to the tape, then the
-// arg-min elements of the Courant and hydro minima.
-static void tape_cycle(lulesh_adjoint* a, const CycleTape& tp, CycleRec* rec) {
+// One taped cycle, queued on the stream: the start state to its slot and
+// timeIncrement! on the device (recorded), the step kernels with the cycle's
+// intermediate values, accelerations, branch flags and dt candidates going to
+// the tape, then the arg-min elements of the Courant and hydro minima.
+static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, CycleRec* rec) {
   lulesh_domain* d = a->dom;
   const Params prm = make_params(d);
   cudaStream_t s = d->stream;
-  ka_tape_begin<<<1, 1, 0, s>>>(d->dd.st, rec, prm);
+  const int nmax = std::max(a->E, a->N);
+  ka_tape_begin<<<(nmax + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(domain_set(a), buf_set(slot), a->E, a->N,
+                                                                        d->dd.st, rec, prm);
   DevDomain td = d->dd;
   td.vnew = tp.vnew; td.delv = tp.delv; td.arealg = tp.arealg; td.vdov = tp.vdov;
   td.delv_xi = tp.dv[0]; td.delv_eta = tp.dv[1]; td.delv_zeta = tp.dv[2];
@@ -168,10 +170,8 @@ static void tape_cycle(lulesh_adjoint* a, const CycleTape& tp, CycleRec* rec) {
   launch_node(td, prm, true, d->tuning, s);  // aux: the node kernel stores the accelerations
   launch_kinematics(td, prm, false, d->tuning, s);
   launch_material(td, prm, false, d->tuning, s);
-  ka_tape_end<<<1, 1, 0, s>>>(d->dd.st, rec);
   const int ge = (a->E + kAdjBlock - 1) / kAdjBlock;
-  ka_argmin<<<ge, kAdjBlock, 0, s>>>(tp.dtc, a->E, d->dd.st, 0, &rec->argmin_c);
-  ka_argmin<<<ge, kAdjBlock, 0, s>>>(tp.dth, a->E, d->dd.st, 1, &rec->argmin_h);
+  ka_tape_close<<<ge, kAdjBlock, 0, s>>>(tp.dtc, tp.dth, a->E, d->dd.st, rec);
 }
 
 static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const StateBuf& s1, const CycleTape& t) {
@@ -213,7 +213,6 @@ static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec) {
     default: LULESH_KA_FORCE(3); break;
   }
 #undef LULESH_KA_FORCE
-  ka_gather_corners<<<gn, kAdjBlock, 0, s>>>(a->ad);
   ka_cycle_close<<<1, kCloseBlock, 0, s>>>(a->ad, ge, gn, rec, a->dsc, prm);
 }
 
@@ -307,7 +306,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
     if ((rc = dalloc(a, &t.ax, N)) || (rc = dalloc(a, &t.ay, N)) || (rc = dalloc(a, &t.az, N)) ||
         (rc = dalloc(a, &t.vnew, E)) || (rc = dalloc(a, &t.delv, E)) || (rc = dalloc(a, &t.arealg, E)) ||
         (rc = dalloc(a, &t.vdov, E)) || (rc = dalloc(a, &t.flags, E)) || (rc = dalloc(a, &t.dtc, E)) ||
-        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 48 * (size_t)E)) ||
+        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 66 * (size_t)E)) ||
         (rc = dalloc(a, &t.kin, 45 * (size_t)E)) || (rc = dalloc(a, &t.mat, 31 * (size_t)E)))
       return fail(rc);
     for (int k = 0; k < 3; ++k)
@@ -323,7 +322,8 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
       (rc = dalloc(a, &ad.lss, E)) || (rc = dalloc(a, &ad.lv, E)) || (rc = dalloc(a, &ad.lvnew, E)) ||
       (rc = dalloc(a, &ad.ldelv, E)) || (rc = dalloc(a, &ad.larealg, E)) || (rc = dalloc(a, &ad.lvdov, E)) ||
       (rc = dalloc(a, &ad.lnb, 6 * (size_t)E)) || (rc = dalloc(a, &ad.cX, 24 * (size_t)E)) ||
-      (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
+      (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) ||
+      (rc = dalloc(a, &ad.fX, 24 * (size_t)E)) || (rc = dalloc(a, &ad.fV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
       (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
       (rc = dalloc(a, &ad.part_dtn, gn)) || (rc = dalloc(a, &ad.part_hg, ge)) || (rc = dalloc(a, &a->scal, 4)) ||
       (rc = dalloc(a, &a->rec, K)) || (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
@@ -463,6 +463,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   auto t0 = std::chrono::steady_clock::now();
   int64_t done = 0;
   int nseg = 0;
+  bool last_taped = false;
   a->seg_len.clear();
   while (done < num_cycles && d->sc[LULESH_S_TIME] < d->sc[LULESH_S_STOPTIME]) {
     if ((int)a->ckpts.size() == nseg) {
@@ -474,7 +475,21 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     a->ckpt_scalars[nseg] = get_scalars(d);
     const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
     const int64_t want = std::min<int64_t>(K, num_cycles - done);
-    rc = lulesh_run(d, c0 + want, nullptr);
+    if (want == num_cycles - done) {
+      // the final segment runs taped, so the reverse sweep needs no recompute of it
+      state_to_device_mirror(d);
+      ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
+      for (int j = 0; j < (int)want; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
+      copy_state_from_domain(a, a->slots[want]);
+      ACK(cudaGetLastError());
+      ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+      ACK(cudaStreamSynchronize(s));
+      state_from_device_mirror(d);
+      rc = d->status;
+      last_taped = true;
+    } else {
+      rc = lulesh_run(d, c0 + want, nullptr);
+    }
     const int64_t n = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
     if (n > 0) { a->seg_len.push_back((int)n); ++nseg; done += n; }
     if (rc) { out.status = rc; out.cycles = done; if (res) *res = out; return rc; }
@@ -506,21 +521,24 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   const Scalars5 final_sc = get_scalars(d);
   // ---- reverse sweep ----
   ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
+  ACK(cudaMemsetAsync(a->ad.fX, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
   for (int k = nseg - 1; k >= 0; --k) {
     const int n = a->seg_len[k];
-    copy_state_to_domain(a, a->ckpts[k]);
-    ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
-    for (int j = 0; j < n; ++j) {
-      copy_state_from_domain(a, a->slots[j]);
-      tape_cycle(a, a->tape[j], a->rec + j);
+    if (!(k == nseg - 1 && last_taped)) {
+      copy_state_to_domain(a, a->ckpts[k]);
+      ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+      for (int j = 0; j < n; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
+      copy_state_from_domain(a, a->slots[n]);
     }
-    copy_state_from_domain(a, a->slots[n]);
     for (int j = n - 1; j >= 0; --j) {
       set_cycle_pointers(a, a->slots[j], a->slots[j + 1], a->tape[j]);
       reverse_cycle(a, a->rec + j);
     }
     ACK(cudaGetLastError());
   }
+  // the first cycle's force transpose is still in the force corner buffers
+  ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
   copy_state_to_domain(a, a->final_state);
   AdjScal hsc;
   ACK(cudaMemcpyAsync(&hsc, a->dsc, sizeof(AdjScal), cudaMemcpyDeviceToHost, s));

@@ -69,7 +69,8 @@ struct AdjDev {
   double *lvnew, *ldelv, *larealg, *lvdov;    // E
   double *ldv[3], *ldx[3];                    // E
   double* lnb;                                // [6][E]: limiter neighbour slots
-  double *cX, *cV;                            // [3][8][E] corner buffers
+  double *cX, *cV;                            // [3][8][E] kinematics corner buffers
+  double *fX, *fV;                            // [3][8][E] force corner buffers (gathered one cycle later)
   double *part_dt, *part_dtn, *part_hg;       // per-block partial sums (kinematics, node, force)
   double *sLdv, *sLhm;                        // [3][8][E], [3][4][E]: hourglass -> geometry
 };
@@ -524,7 +525,9 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
   block_sum_to(Ldt, a.part_dt);
 }
 
-// Sums the corner buffers into node adjoints (added to what is there).
+// Sums the force corner buffers into node adjoints (added to what is there):
+// the last step of a reverse sweep (each cycle's ka_node gathers the previous
+// transposed cycle's force corners itself).
 __global__ void __launch_bounds__(kAdjBlock) ka_gather_corners(AdjDev a) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= a.N) return;
@@ -533,8 +536,8 @@ __global__ void __launch_bounds__(kAdjBlock) ka_gather_corners(AdjDev a) {
   double gx = 0, gy = 0, gz = 0, hx = 0, hy = 0, hz = 0;
   for (int j = s; j < t; ++j) {
     const int c = a.cornerList[j];
-    gx += a.cX[c]; gy += a.cX[E8 + c]; gz += a.cX[2 * E8 + c];
-    hx += a.cV[c]; hy += a.cV[E8 + c]; hz += a.cV[2 * E8 + c];
+    gx += a.fX[c]; gy += a.fX[E8 + c]; gz += a.fX[2 * E8 + c];
+    hx += a.fV[c]; hy += a.fV[E8 + c]; hz += a.fV[2 * E8 + c];
   }
   a.lx[i] += gx; a.ly[i] += gy; a.lz[i] += gz;
   a.lxd[i] += hx; a.lyd[i] += hy; a.lzd[i] += hz;
@@ -556,22 +559,27 @@ __global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, const CycleRec* r
     double* Lf[3] = {a.lfx, a.lfy, a.lfz};
     const double* xd1[3] = {a.xd1, a.yd1, a.zd1};
     const double* acc[3] = {a.ax, a.ay, a.az};
-    // the kinematics transpose's corner adjoints join the end-state adjoints
+    // the end-state adjoints gather the force transpose of the cycle after
+    // this one (pending corners) and this cycle's kinematics transpose
     double gx[3] = {0.0, 0.0, 0.0}, gv[3] = {0.0, 0.0, 0.0};
+    double fx[3] = {0.0, 0.0, 0.0}, fv[3] = {0.0, 0.0, 0.0};
     {
       const int s = a.nodeElemStart[i], t = a.nodeElemStart[i + 1];
       const long long E8 = 8ll * a.E;
       for (int j = s; j < t; ++j) {
         const int c = a.cornerList[j];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) { gx[k] += a.cX[k * E8 + c]; gv[k] += a.cV[k * E8 + c]; }
+        for (int k = 0; k < 3; ++k) {
+          fx[k] += a.fX[k * E8 + c]; fv[k] += a.fV[k * E8 + c];
+          gx[k] += a.cX[k * E8 + c]; gv[k] += a.cV[k * E8 + c];
+        }
       }
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double lxn = Lx[k][i] + gx[k];
+      const double lxn = (Lx[k][i] + fx[k]) + gx[k];
       const double v1 = xd1[k][i];
-      double lv = (Lxd[k][i] + gv[k]) + lxn * dt;   // x1 = x0 + xd1*dt
+      double lv = ((Lxd[k][i] + fv[k]) + gv[k]) + lxn * dt;   // x1 = x0 + xd1*dt
       Ldt += lxn * v1;
       double lf = 0.0;
       if (v1 == 0.0) {
@@ -651,7 +659,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
 #pragma unroll
       for (int k = 0; k < 3; ++k)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) { a.cV[(k * 8 + c) * E + e] = 0.0; a.sLdv[(k * 8 + c) * E + e] = 0.0; }
+        for (int c = 0; c < 8; ++c) { a.fV[(k * 8 + c) * E + e] = 0.0; a.sLdv[(k * 8 + c) * E + e] = 0.0; }
 #pragma unroll
       for (int k = 0; k < 12; ++k) a.sLhm[k * E + e] = 0.0;
     } else {
@@ -736,7 +744,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
         walsh_modes_t(T[k], q);
 #pragma unroll
         for (int c = 0; c < 8; ++c)
-          a.cV[(k * 8 + c) * E + e] =
+          a.fV[(k * 8 + c) * E + e] =
               coef * fma(-dv[2][c], B[k][2], fma(-dv[1][c], B[k][1], fma(-dv[0][c], B[k][0], q[c])));
       }
       // dL/ddv_j = -coef sum_k (lf_k A[k][j] + V_k B[k][j])
@@ -770,10 +778,15 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
   block_sum_to(Lhg_coef, a.part_hg);
 }
 
-// Position transpose of k_force: the stress force (face-diagonal cross
-// products, with the reference's face-5 normal quirk unless corrected), the
-// hourglass modes (Gamma^T of dL/dhm) and the volume derivatives (through
-// the 12 edge sums), written to the position corner buffer.
+// Position transpose of k_force, written to the position corner buffer:
+//  * the hourglass modes: Gamma^T of dL/dhm;
+//  * the volume derivatives: the forward's dv is the gradient of 12*volume
+//    (calcElemVolume's three triple products U.(V x W) of face diagonals), so
+//    the transpose of G -> sum <G, dv> is the Hessian-vector product of those
+//    triple products along G (the faithful slots 1 and 3 swapped back);
+//  * the stress force f_n = s8 B_n with B_n the node's face-diagonal cross
+//    products (the reference's face-5 quirk unless corrected).
+// All three use the 12 face diagonals of the element.
 template <int MODE>
 __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
   const int E = a.E;
@@ -785,6 +798,9 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
   double X[3][8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) { X[0][c] = a.x0[nd[c]]; X[1][c] = a.y0[nd[c]]; X[2][c] = a.z0[nd[c]]; }
+  auto dg = [&](int p, int q) { return v3(X[0][p] - X[0][q], X[1][p] - X[1][q], X[2][p] - X[2][q]); };
+  const V3 d20 = dg(2, 0), d31 = dg(3, 1), d50 = dg(5, 0), d14 = dg(1, 4), d61 = dg(6, 1), d25 = dg(2, 5);
+  const V3 d72 = dg(7, 2), d36 = dg(3, 6), d43 = dg(4, 3), d07 = dg(0, 7), d64 = dg(6, 4), d57 = dg(5, 7);
   double LX[3][8];
   // hourglass modes hm_k = Gamma(X_k)
 #pragma unroll
@@ -796,72 +812,59 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
 #pragma unroll
     for (int c = 0; c < 8; ++c) LX[k][c] = q[c];
   }
-  // volume derivatives through the edge sums
+  auto add = [&](int c, const V3& v) { LX[0][c] += v.x; LX[1][c] += v.y; LX[2][c] += v.z; };
+  auto sub = [&](int c, const V3& v) { LX[0][c] -= v.x; LX[1][c] -= v.y; LX[2][c] -= v.z; };
+  // volume derivatives: Hessian-vector product of the triple products
   {
-    constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
-    constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
-    constexpr int pe[8][6] = {{5, 3, 4, 8, 7, 9}, {3, 0, 2, 9, 6, 11}, {0, 1, 7, 11, 4, 10},
-                              {1, 5, 6, 10, 2, 8}, {10, 11, 7, 1, 4, 0}, {11, 9, 2, 0, 6, 3},
-                              {9, 8, 4, 3, 7, 5}, {8, 10, 6, 5, 2, 1}};
-    constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
-    double ex[12], ey[12], ez[12], Lex[12], Ley[12], Lez[12];
+    double G[3][8];
 #pragma unroll
-    for (int j = 0; j < 12; ++j) {
-      ex[j] = X[0][ea[j]] + X[0][eb[j]];
-      ey[j] = X[1][ea[j]] + X[1][eb[j]];
-      ez[j] = X[2][ea[j]] + X[2][eb[j]];
-      Lex[j] = 0.0; Ley[j] = 0.0; Lez[j] = 0.0;
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) G[j][c] = a.sLdv[(j * 8 + c) * E + e];
+    if (!(MODE & 2)) {
+      // the faithful forward stores node 3's derivative in slot 1 and node 1's in slot 3
+#pragma unroll
+      for (int j = 0; j < 3; ++j) { const double t = G[j][1]; G[j][1] = G[j][3]; G[j][3] = t; }
     }
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      const int p12 = pe[n][0], p01 = pe[n][1], p04 = pe[n][2], p34 = pe[n][3], p25 = pe[n][4], p35 = pe[n][5];
-      const int slot = (MODE & 2) ? owner[n] : n;
-      const double gx = a.sLdv[(0 * 8 + slot) * E + e], gy = a.sLdv[(1 * 8 + slot) * E + e],
-                   gz = a.sLdv[(2 * 8 + slot) * E + e];
-      // dvx = ey12 ez01 - ey01 ez12 + ey04 ez34 - ey34 ez04 - ey25 ez35 + ey35 ez25
-      Ley[p12] = fma(gx, ez[p01], Ley[p12]); Lez[p01] = fma(gx, ey[p12], Lez[p01]);
-      Ley[p01] = fma(-gx, ez[p12], Ley[p01]); Lez[p12] = fma(-gx, ey[p01], Lez[p12]);
-      Ley[p04] = fma(gx, ez[p34], Ley[p04]); Lez[p34] = fma(gx, ey[p04], Lez[p34]);
-      Ley[p34] = fma(-gx, ez[p04], Ley[p34]); Lez[p04] = fma(-gx, ey[p34], Lez[p04]);
-      Ley[p25] = fma(-gx, ez[p35], Ley[p25]); Lez[p35] = fma(-gx, ey[p25], Lez[p35]);
-      Ley[p35] = fma(gx, ez[p25], Ley[p35]); Lez[p25] = fma(gx, ey[p35], Lez[p25]);
-      // dvy = -ex12 ez01 + ex01 ez12 - ex04 ez34 + ex34 ez04 + ex25 ez35 - ex35 ez25
-      Lex[p12] = fma(-gy, ez[p01], Lex[p12]); Lez[p01] = fma(-gy, ex[p12], Lez[p01]);
-      Lex[p01] = fma(gy, ez[p12], Lex[p01]); Lez[p12] = fma(gy, ex[p01], Lez[p12]);
-      Lex[p04] = fma(-gy, ez[p34], Lex[p04]); Lez[p34] = fma(-gy, ex[p04], Lez[p34]);
-      Lex[p34] = fma(gy, ez[p04], Lex[p34]); Lez[p04] = fma(gy, ex[p34], Lez[p04]);
-      Lex[p25] = fma(gy, ez[p35], Lex[p25]); Lez[p35] = fma(gy, ex[p25], Lez[p35]);
-      Lex[p35] = fma(-gy, ez[p25], Lex[p35]); Lez[p25] = fma(-gy, ex[p35], Lez[p25]);
-      // dvz = -ey12 ex01 + ey01 ex12 - ey04 ex34 + ey34 ex04 + ey25 ex35 - ey35 ex25
-      Ley[p12] = fma(-gz, ex[p01], Ley[p12]); Lex[p01] = fma(-gz, ey[p12], Lex[p01]);
-      Ley[p01] = fma(gz, ex[p12], Ley[p01]); Lex[p12] = fma(gz, ey[p01], Lex[p12]);
-      Ley[p04] = fma(-gz, ex[p34], Ley[p04]); Lex[p34] = fma(-gz, ey[p04], Lex[p34]);
-      Ley[p34] = fma(gz, ex[p04], Ley[p34]); Lex[p04] = fma(gz, ey[p34], Lex[p04]);
-      Ley[p25] = fma(gz, ex[p35], Ley[p25]); Lex[p35] = fma(gz, ey[p25], Lex[p35]);
-      Ley[p35] = fma(-gz, ex[p25], Ley[p35]); Lex[p25] = fma(-gz, ey[p35], Lex[p25]);
+    auto gd = [&](int p, int q) { return v3(G[0][p] - G[0][q], G[1][p] - G[1][q], G[2][p] - G[2][q]); };
+    auto hvp = [&](const V3& U, const V3& V, const V3& W, const V3& dU, const V3& dV, const V3& dW,
+                   int u0, int u1, int u2, int u3, int v0, int v1, int w0, int w1) {
+      V3 gU = vcross(dV, W); vadd(gU, vcross(V, dW));
+      V3 gV = vcross(W, dU); vadd(gV, vcross(dW, U));
+      V3 gW = vcross(dU, V); vadd(gW, vcross(U, dV));
+      add(u0, gU); sub(u1, gU); add(u2, gU); sub(u3, gU);
+      add(v0, gV); sub(v1, gV);
+      add(w0, gW); sub(w1, gW);
+    };
+    // 12*volume = (d31 + d72).(d63 x d20) + (d43 + d57).(d64 x d70) + (d14 + d25).(d61 x d50)
+    {
+      V3 U = d31; vadd(U, d72);
+      V3 dU = gd(3, 1); vadd(dU, gd(7, 2));
+      const V3 V = v3(-d36.x, -d36.y, -d36.z);
+      hvp(U, V, d20, dU, gd(6, 3), gd(2, 0), 3, 1, 7, 2, 6, 3, 2, 0);
     }
-#pragma unroll
-    for (int j = 0; j < 12; ++j) {
-      LX[0][ea[j]] += Lex[j]; LX[0][eb[j]] += Lex[j];
-      LX[1][ea[j]] += Ley[j]; LX[1][eb[j]] += Ley[j];
-      LX[2][ea[j]] += Lez[j]; LX[2][eb[j]] += Lez[j];
+    {
+      V3 U = d43; vadd(U, d57);
+      V3 dU = gd(4, 3); vadd(dU, gd(5, 7));
+      const V3 W = v3(-d07.x, -d07.y, -d07.z);
+      hvp(U, d64, W, dU, gd(6, 4), gd(7, 0), 4, 3, 5, 7, 6, 4, 7, 0);
+    }
+    {
+      V3 U = d14; vadd(U, d25);
+      V3 dU = gd(1, 4); vadd(dU, gd(2, 5));
+      hvp(U, d61, d50, dU, gd(6, 1), gd(5, 0), 1, 4, 2, 5, 6, 1, 5, 0);
     }
   }
   // stress part: f = s8 * B with B the sum of the node's three face cross products
   {
     const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
     const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
-    constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
-                              {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
     constexpr int nf[8][3] = {{0, 1, 4}, {0, 1, 2}, {0, 2, 3}, {0, 3, 4},
                               {1, 4, 5}, {1, 2, 5}, {2, 3, 5}, {3, 4, 5}};
+    // face normals (the forward's cross products, from the tape)
     V3 N[6];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
-      const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
-      N[f] = vcross(d1, d2);
-    }
+    for (int f = 0; f < 6; ++f) N[f] = v3(a.geo[(48 + f) * E + e], a.geo[(54 + f) * E + e], a.geo[(60 + f) * E + e]);
     // sum_n lf_n . B_n = sum_f N_f . LU_f with LU_f the sum of lf over the
     // face's nodes (node 1's quirk included); the normals' adjoints are s8 LU_f
     V3 LU[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
@@ -877,30 +880,28 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
       }
     }
     double Ls8 = 0.0;
-    V3 LN[6];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      Ls8 += vdot(N[f], LU[f]);
-      LN[f] = v3(s8 * LU[f].x, s8 * LU[f].y, s8 * LU[f].z);
-    }
+    for (int f = 0; f < 6; ++f) Ls8 += vdot(N[f], LU[f]);
     const double Lpq = -0.125 * Ls8;
     a.lp[e] += Lpq;
     a.lq[e] += Lpq;
-#pragma unroll
-    for (int f = 0; f < 6; ++f) {
-      const V3 d1 = v3(X[0][fd[f][0]] - X[0][fd[f][1]], X[1][fd[f][0]] - X[1][fd[f][1]], X[2][fd[f][0]] - X[2][fd[f][1]]);
-      const V3 d2 = v3(X[0][fd[f][2]] - X[0][fd[f][3]], X[1][fd[f][2]] - X[1][fd[f][3]], X[2][fd[f][2]] - X[2][fd[f][3]]);
-      const V3 L1 = vcross(d2, LN[f]), L2 = vcross(LN[f], d1);
-      LX[0][fd[f][0]] += L1.x; LX[1][fd[f][0]] += L1.y; LX[2][fd[f][0]] += L1.z;
-      LX[0][fd[f][1]] -= L1.x; LX[1][fd[f][1]] -= L1.y; LX[2][fd[f][1]] -= L1.z;
-      LX[0][fd[f][2]] += L2.x; LX[1][fd[f][2]] += L2.y; LX[2][fd[f][2]] += L2.z;
-      LX[0][fd[f][3]] -= L2.x; LX[1][fd[f][3]] -= L2.y; LX[2][fd[f][3]] -= L2.z;
-    }
+    // N_f = d1 x d2 with (d1, d2) = (p0 - p1, p2 - p3) of the face's corners
+    auto face_t = [&](int f, const V3& d1, const V3& d2, int p0, int p1, int p2, int p3) {
+      const V3 LN = v3(s8 * LU[f].x, s8 * LU[f].y, s8 * LU[f].z);
+      const V3 L1 = vcross(d2, LN), L2 = vcross(LN, d1);
+      add(p0, L1); sub(p1, L1); add(p2, L2); sub(p3, L2);
+    };
+    face_t(0, d20, d31, 2, 0, 3, 1);
+    face_t(1, d50, d14, 5, 0, 1, 4);
+    face_t(2, d61, d25, 6, 1, 2, 5);
+    face_t(3, d72, d36, 7, 2, 3, 6);
+    face_t(4, d43, d07, 4, 3, 0, 7);
+    face_t(5, d64, d57, 6, 4, 5, 7);
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll
-    for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
+    for (int c = 0; c < 8; ++c) a.fX[(k * 8 + c) * E + e] = LX[k][c];
 }
 
 // Sum of `n` partials in a fixed order by one block of BS threads; every
@@ -995,14 +996,37 @@ __global__ void __launch_bounds__(kCloseBlock) ka_cycle_close(AdjDev a, int ge, 
   *sc = v;
 }
 
-// Start of a taped cycle (one thread): folds the previous cycle's minima,
-// records timeIncrement!'s inputs, advances time and records the new dt.
-__global__ void ka_tape_begin(DevState* st, CycleRec* rec, Params prm) {
+// Copies the 11 state fields (node fields n < N, element fields n < E).
+__device__ __forceinline__ void copy_state_at(int i, const StateSet& src, const StateSet& dst, int E, int N) {
+  if (i < N) {
+#pragma unroll
+    for (int k = 0; k < 6; ++k) dst.f[k][i] = src.f[k][i];
+  }
+  if (i < E) {
+#pragma unroll
+    for (int k = 6; k < 11; ++k) dst.f[k][i] = src.f[k][i];
+  }
+}
+
+__global__ void __launch_bounds__(kAdjBlock) ka_copy_state(StateSet src, StateSet dst, int E, int N) {
+  copy_state_at(blockIdx.x * blockDim.x + threadIdx.x, src, dst, E, N);
+}
+
+// Start of a taped cycle: every thread copies the cycle's start state to its
+// slot; thread 0 folds the previous cycle's minima, records timeIncrement!'s
+// inputs, advances time and records the new dt. A run that has reached
+// stoptime (the examples/benchmark.jl loop condition) or an earlier error
+// makes the cycle a no-op (done / status, which the step kernels check).
+__global__ void __launch_bounds__(kAdjBlock) ka_tape_begin(StateSet src, StateSet dst, int E, int N, DevState* st,
+                                                            CycleRec* rec, Params prm) {
+  copy_state_at(blockIdx.x * blockDim.x + threadIdx.x, src, dst, E, N);
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  if (st->status != 0u || st->done) return;
   if (st->acc_courant != kInfBits) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
   if (st->acc_hydro != kInfBits) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
   st->acc_courant = kInfBits;
   st->acc_hydro = kInfBits;
+  if (!(st->time < prm.stoptime)) { st->done = 1; return; }
   CycleRec r;
   r.time_prev = st->time;
   r.dt_prev = st->deltatime;
@@ -1021,34 +1045,20 @@ __global__ void ka_tape_begin(DevState* st, CycleRec* rec, Params prm) {
   *rec = r;
 }
 
-// End of a taped cycle (one thread): which minima the cycle reached.
-__global__ void ka_tape_end(const DevState* st, CycleRec* rec) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  rec->active_c = st->acc_courant != kInfBits;
-  rec->active_h = st->acc_hydro != kInfBits;
-}
-
-// Smallest element index whose dt candidate equals the cycle's minimum: the
-// element the reference's strict-less-than scan keeps (src/domain.jl:3003-3008).
-__global__ void __launch_bounds__(kAdjBlock) ka_argmin(const double* cand, int E, const DevState* st, int which,
-                                                        int* out) {
+// End of a taped cycle: which minima the cycle reached, and the smallest
+// element index attaining each (the element the reference's strict-less-than
+// scan keeps, src/domain.jl:3003-3008 and :3041-3046).
+__global__ void __launch_bounds__(kAdjBlock) ka_tape_close(const double* dtc, const double* dth, int E,
+                                                            const DevState* st, CycleRec* rec) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned long long minbits = which ? st->acc_hydro : st->acc_courant;
-  if (minbits == kInfBits || i >= E) return;
-  if ((unsigned long long)__double_as_longlong(cand[i]) == minbits) atomicMin(out, i);
-}
-
-// Copies the 11 state fields (node fields n < N, element fields n < E).
-__global__ void __launch_bounds__(kAdjBlock) ka_copy_state(StateSet src, StateSet dst, int E, int N) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < N) {
-#pragma unroll
-    for (int k = 0; k < 6; ++k) dst.f[k][i] = src.f[k][i];
+  const unsigned long long bc = st->acc_courant, bh = st->acc_hydro;
+  if (i == 0) {
+    rec->active_c = bc != kInfBits;
+    rec->active_h = bh != kInfBits;
   }
-  if (i < E) {
-#pragma unroll
-    for (int k = 6; k < 11; ++k) dst.f[k][i] = src.f[k][i];
-  }
+  if (i >= E) return;
+  if (bc != kInfBits && (unsigned long long)__double_as_longlong(dtc[i]) == bc) atomicMin(&rec->argmin_c, i);
+  if (bh != kInfBits && (unsigned long long)__double_as_longlong(dth[i]) == bh) atomicMin(&rec->argmin_h, i);
 }
 
 // Loss seed and value: L = sum_e w_e e + sum_n 0.5 w_n |u|^2 with

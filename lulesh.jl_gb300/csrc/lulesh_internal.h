@@ -116,9 +116,9 @@ struct DevDomain {
   unsigned long long* tapeFlags;
   double* tapeDtc;
   double* tapeDth;
-  // [48][E]: the force kernel's volume derivatives dv_j[n] (24, node order),
-  // hourglass modes over 12*determ (12) and mode sums S_k[m] of the
-  // velocities (12)
+  // [66][E]: the force kernel's volume derivatives dv_j[n] (24, node order),
+  // hourglass modes over 12*determ (12), mode sums S_k[m] of the velocities
+  // (12) and face-diagonal cross products (x, y, z of the 6 faces: 18)
   double* tapeGeo;
   // [45][E]: the kinematics kernel's Walsh vectors of positions (9) and
   // velocities (9), cofactor columns (9), 1/det (1), monotonic-Q cross

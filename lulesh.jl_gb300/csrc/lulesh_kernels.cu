@@ -81,6 +81,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
       const double d2x = x[fd[f][2]] - x[fd[f][3]], d2y = y[fd[f][2]] - y[fd[f][3]],
                    d2z = z[fd[f][2]] - z[fd[f][3]];
       cross(d1x, d1y, d1z, d2x, d2y, d2z, nx[f], ny[f], nz[f]);
+      if (TAPE) {
+        d.tapeGeo[(48 + f) * E + e] = nx[f];
+        d.tapeGeo[(54 + f) * E + e] = ny[f];
+        d.tapeGeo[(60 + f) * E + e] = nz[f];
+      }
     }
     // node -> its three faces (faces numbered 0..5 = reference faces 1..6)
     Bx[0] = (nx[0] + nx[1]) + nx[4]; By[0] = (ny[0] + ny[1]) + ny[4]; Bz[0] = (nz[0] + nz[1]) + nz[4];
