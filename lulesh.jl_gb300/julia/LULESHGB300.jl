@@ -21,7 +21,7 @@ module LULESHGB300
 
 using LULESH
 
-export GPUDomain, LuleshGPUError
+export GPUDomain, LuleshGPUError, GPUAdjoint, energy_gradient!
 
 const libpath = get(ENV, "LULESH_GB300_LIB",
                     joinpath(@__DIR__, "..", "lib", "liblulesh_gb300.so"))
@@ -166,6 +166,93 @@ function Base.setproperty!(d::GPUDomain, s::Symbol, v)
         setfield!(d, s, v)
     end
     return v
+end
+
+# ---- reverse-mode adjoint of a run (lulesh_adj_* of include/lulesh_gb300.h) ----
+#
+# The reference differentiates one lagrangeLeapFrog call with Enzyme
+# (examples/benchmark.jl:48-52, 85-86); this differentiates whole runs with
+# the library's hand-written adjoint kernels. The objective after the run is
+# the energy within `radius` of the origin (element internal energy times
+# mass plus nodal kinetic energy, masked by the initial mesh); `set_seed!`
+# replaces it with linear weights on state fields.
+
+struct AdjResult
+    loss::Float64
+    grad_hgcoef::Float64
+    forward_ms::Float64
+    reverse_ms::Float64
+    cycles::Int64
+    checkpoints::Int32
+    status::Int32
+end
+
+mutable struct GPUAdjoint
+    handle::Ptr{Cvoid}
+    domain::GPUDomain
+    function GPUAdjoint(d::GPUDomain; radius::Real = 0.3, checkpoint_every::Integer = 20)
+        h = Ref{Ptr{Cvoid}}(C_NULL)
+        rc = ccall((:lulesh_adj_create, libpath), Cint, (Ptr{Cvoid}, Float64, Int32, Ptr{Ptr{Cvoid}}),
+                   getfield(d, :handle), Float64(radius), Int32(checkpoint_every), h)
+        rc == 0 || throw(LuleshGPUError("adjoint: status $rc", rc))
+        a = new(h[], d)
+        finalizer(x -> x.handle == C_NULL || ccall((:lulesh_adj_destroy, libpath), Cint, (Ptr{Cvoid},), x.handle), a)
+        return a
+    end
+end
+
+"Linear objective weights for one state field (x y z xd yd zd e p q v ss)."
+function set_seed!(a::GPUAdjoint, field::Symbol, w::Vector{Float64})
+    rc = ccall((:lulesh_adj_set_seed, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Int64),
+               a.handle, FIELD_IDS[field][1], w, length(w))
+    rc == 0 || throw(LuleshGPUError("seed $field: status $rc", rc))
+    return a
+end
+
+clear_seeds!(a::GPUAdjoint) = (ccall((:lulesh_adj_clear_seeds, libpath), Cint, (Ptr{Cvoid},), a.handle); a)
+
+"""
+    gradient!(a, num_cycles) -> AdjResult
+
+Advances the domain by up to `num_cycles` cycles (timeIncrement! +
+lagrangeLeapFrog each, stopping at stoptime) and computes the gradient of
+the objective w.r.t. the state before the run; `grad(a, :e)` returns it per
+field, the result holds dL/dhgcoef.
+"""
+function gradient!(a::GPUAdjoint, num_cycles::Integer)
+    r = Ref{AdjResult}()
+    rc = ccall((:lulesh_adj_gradient, libpath), Cint, (Ptr{Cvoid}, Int64, Ptr{AdjResult}),
+               a.handle, Int64(num_cycles), r)
+    rc == 0 || step_error(a.domain, rc)
+    return r[]
+end
+
+function grad(a::GPUAdjoint, field::Symbol)
+    id = FIELD_IDS[field][1]
+    n = id >= 32 ? (getfield(a.domain, :nx) + 1)^3 : getfield(a.domain, :nx)^3
+    out = Vector{Float64}(undef, n)
+    rc = ccall((:lulesh_adj_get_gradient, libpath), Cint, (Ptr{Cvoid}, Int32, Ptr{Float64}, Int64),
+               a.handle, id, out, n)
+    rc == 0 || throw(LuleshGPUError("gradient of $field: status $rc", rc))
+    return out
+end
+
+"""
+    energy_gradient!(d, e0, hgcoef, num_cycles; radius = 0.3, checkpoint_every = 20)
+        -> (L, dL/de0, dL/dhgcoef)
+
+Sets the domain's energy field to `e0` and hgcoef, runs `num_cycles` cycles
+and returns the energy within `radius` of the origin with its gradient. The
+domain is left at the final state; the other state fields are the domain's
+own at the call.
+"""
+function energy_gradient!(d::GPUDomain, e0::Vector{Float64}, hgcoef::Real, num_cycles::Integer;
+                          radius::Real = 0.3, checkpoint_every::Integer = 20)
+    d.e = e0
+    d.hgcoef = Float64(hgcoef)
+    a = GPUAdjoint(d; radius = radius, checkpoint_every = checkpoint_every)
+    r = gradient!(a, num_cycles)
+    return r.loss, grad(a, :e), r.grad_hgcoef
 end
 
 # verifyAndWriteFinalOutput reads domain.cycle and domain.e[...] only
