@@ -321,6 +321,39 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
                    "median_rel_err": float(np.median(errs))}}
 
 
+def c3_leg(L, torch, dev, nx, cycles, warmup=2):
+    """Config C3: the nx^3 Sedov problem with 11 unbalanced regions (balance 4,
+    cost 2) and the region cost model on (each element's EOS evaluated its
+    region's rep count times: 1, 3 or 30), timed over `cycles` cycles after
+    `warmup`; the same problem without the extra EOS work (the reference's
+    behaviour) is timed beside it. Results are identical (tested)."""
+    out = {"config": f"Sedov {nx}^3, 11 regions, balance 4, cost 2, region reps on, FP64",
+           "nx": nx, "cycles": cycles}
+    for reps in (True, False):
+        g = L.Domain(L.LuleshProblem(nx=nx, nr=11, balance=4, cost=2, region_reps=reps, device=dev))
+        if reps:
+            sizes, counts = g.field("regElemSize"), g.field("regReps")
+            out["elements_by_reps"] = {str(int(r)): int(sizes[counts == r].sum()) for r in np.unique(counts)}
+            out["mean_eos_evaluations"] = float((sizes * counts).sum() / sizes.sum())
+        stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+        L.run(g, warmup)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c0 = g.cycle
+        torch.cuda.synchronize(dev)
+        a.record(stream)
+        sc = L.run(g, c0 + cycles)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        done = sc["cycle"] - c0
+        ms = a.elapsed_time(b)
+        key = "with_region_reps" if reps else "without_region_reps"
+        out[key] = {"zones_cycles_per_s": g.numElem * done / (ms * 1e-3), "ms_per_cycle": ms / done,
+                    "cycles": int(done), "origin_energy": float(g.field("e")[0])}
+        g.close()
+    out["reps_cost_factor"] = out["with_region_reps"]["ms_per_cycle"] / out["without_region_reps"]["ms_per_cycle"]
+    return out
+
+
 def run_ours(args):
     world, rank, local = _dist()
     import torch
@@ -418,6 +451,12 @@ def run_ours(args):
         g.close()
         ensemble = ensemble_leg(L, torch, dev, args.ens_instances, args.ens_cycles)
 
+    c3 = None
+    if not args.no_c3:
+        if ensemble is None:
+            g.close()
+        c3 = c3_leg(L, torch, dev, args.c3_nx, args.c3_cycles)
+
     adjoint = None
     if not args.no_adjoint:
         if ensemble is None:
@@ -444,7 +483,8 @@ def run_ours(args):
             "kernel_ms_per_cycle": {k: v / cycles for k, v in ktimes.items()},
             "dominant_kernel": dominant,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
-            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint}
+            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint,
+            "c3_unbalanced_regions": c3}
     print(json.dumps(line), flush=True)
     g.close()
     return 0
@@ -465,6 +505,9 @@ def main():
     ap.add_argument("--ens-instances", type=int, default=256)
     ap.add_argument("--ens-cycles", type=int, default=300)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
+    ap.add_argument("--no-c3", action="store_true", help="skip the unbalanced-regions leg")
+    ap.add_argument("--c3-nx", type=int, default=256)
+    ap.add_argument("--c3-cycles", type=int, default=50)
     ap.add_argument("--adj-nx", type=int, default=48)
     ap.add_argument("--adj-cycles", type=int, default=200)
     ap.add_argument("--adj-every", type=int, default=20)

@@ -324,6 +324,28 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
   d->regNumList = m.regNumList; d->regElemlist = m.regElemlist; d->regCSR = m.regCSR;
   d->regReps = m.regReps; d->regSorted = m.regSorted; d->regElemSize = m.regElemSize;
   if ((rc = upload_node_bc(d))) return fail(rc);
+  if (d->params.region_reps) {
+    // the region cost model: elements in region order (regElemlist, grouped by
+    // sorted region) and each position's region rep count
+    std::vector<int> order(E), reps(E);
+    int64_t pos = 0;
+    for (size_t r = 0; r < m.regElemSize.size(); ++r)
+      for (int64_t k = 0; k < m.regElemSize[r]; ++k, ++pos) {
+        order[pos] = (int)(m.regElemlist[pos] - 1);
+        reps[pos] = (int)m.regReps[r];
+      }
+    if ((err = cudaMalloc(&d->region_buf, 2 * (size_t)E * sizeof(int))) != cudaSuccess) {
+      cudaGetLastError();
+      d->region_buf = nullptr;
+      return fail(LULESH_ERR_MEMORY);
+    }
+    int* ob = static_cast<int*>(d->region_buf);
+    if ((err = cudaMemcpy(ob, order.data(), E * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (err = cudaMemcpy(ob + E, reps.data(), E * sizeof(int), cudaMemcpyHostToDevice)) != cudaSuccess)
+      return fail(cuda_fail(err));
+    dd.regOrder = ob;
+    dd.posReps = ob + E;
+  }
   state_to_device_mirror(d);
   if ((rc = h2d(dd.st, d->hst, 1, s))) return fail(rc);
   if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(cuda_fail(err));
@@ -339,6 +361,7 @@ int lulesh_destroy(lulesh_domain* d) {
   for (auto& ev : d->ring) if (ev) cudaEventDestroy(ev);
   if (d->hst) cudaFreeHost(d->hst);
   if (d->arena) cudaFree(d->arena);
+  if (d->region_buf) cudaFree(d->region_buf);
   if (d->stream) cudaStreamDestroy(d->stream);
   delete d;
   return LULESH_OK;

@@ -22,6 +22,7 @@ struct lulesh_domain {
   int32_t status = 0, site = 0;
   lulesh::DevDomain dd{};
   void* arena = nullptr;
+  void* region_buf = nullptr;  // regOrder + posReps when params.region_reps
   cudaStream_t stream = nullptr;
   lulesh::DevState* hst = nullptr;  // pinned mirror of the device state
   cudaGraphExec_t graph = nullptr;

@@ -111,6 +111,10 @@ struct DevDomain {
   const int* nodeInst;
   const double* instHg;
   int ninst;
+  // region cost model (null unless region_reps): elements in region order and
+  // the EOS evaluation count of each position's region
+  const int* regOrder;
+  const int* posReps;
   // adjoint taping (null unless recording): branch flags and each element's
   // Courant and hydro dt candidates (+inf where vdov == 0)
   unsigned long long* tapeFlags;

@@ -544,10 +544,17 @@ __device__ __forceinline__ void warp_min2_by_instance(unsigned long long a, unsi
   }
 }
 
-template <int MODE, bool AUX, bool ENS, bool TAPE>
+// An empty register move the compiler cannot see through: a value passed
+// through it must be recomputed from it.
+__device__ __forceinline__ void opaque(double& x) { asm volatile("" : "+d"(x)); }
+
+// REGION: threads take elements in region order (d.regOrder) so that a warp
+// runs one region's rep count; each element's EOS is evaluated that many times.
+template <int MODE, bool AUX, bool ENS, bool TAPE, bool REGION>
 __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params prm) {
   const int E = d.E;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = REGION ? (t < E ? LDG(&d.regOrder[t]) : E) : t;
   // every thread of the block takes part in the dt reduction
   unsigned long long courant = kInfBits, hydro = kInfBits;
   const int inst = (ENS && i < E) ? LDG(&d.elemInst[i]) : 0;
@@ -616,9 +623,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     if (q_old_in > prm.qstop) err |= ST_QSTOP;
 
     // ---- applyMaterialPropertiesForElems, src/domain.jl:2860-2910 ----
-    double vnewc = vnew;
-    if (prm.eosvmin != 0.0 && vnewc < prm.eosvmin) { vnewc = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
-    if (prm.eosvmax != 0.0 && vnewc > prm.eosvmax) { vnewc = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
+    double vnewc_in = vnew;
+    if (prm.eosvmin != 0.0 && vnewc_in < prm.eosvmin) { vnewc_in = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
+    if (prm.eosvmax != 0.0 && vnewc_in > prm.eosvmax) { vnewc_in = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
     {
       double vc = LDG(&d.v[i]);
       if (prm.eosvmin != 0.0 && vc < prm.eosvmin) vc = prm.eosvmin;
@@ -628,10 +635,28 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     // ---- evalEOSForElems + calcEnergyForElems + calcSoundSpeedForElems,
     //      src/domain.jl:2617-2857, per element ----
-    const double delvc = LDG(&d.delv[i]);
-    const double e_old = d.e[i];
-    double p_old = d.p[i];
-    const double q_old = q_old_in;
+    // The region cost model (LULESH 2.0's rep loop in EvalEOSForElems, which
+    // the reference computes in regReps but never applies) evaluates the
+    // energy update `reps` times with identical inputs; the inputs pass
+    // through an opaque register move each time so no evaluation is folded
+    // away, and the last one is kept. Results do not depend on reps.
+    const int reps = REGION ? LDG(&d.posReps[t]) : 1;
+    const double delvc_in = LDG(&d.delv[i]);
+    const double e_old_in = d.e[i];
+    const double p_old_in = d.p[i];
+    const double c1s = 2.0 / 3.0;
+    const double inv_rho0 = 1.0 / prm.refdens;
+    double e_out = 0.0, p_out = 0.0, vv_out = 0.0;
+    bool compress_out = false;
+    // TINY-guarded sound-speed square root (src/domain.jl:2655-2659, 2738-2742)
+    auto tiny_sqrt = [&](double ssc, unsigned long long bit) -> double {
+      if (ssc <= 0.111111e-36) { if (TAPE) fl |= bit; return 0.333333e-18; }
+      return sqrt(ssc);
+    };
+#pragma unroll 1
+    for (int rep = 0; rep < reps; ++rep) {
+    double delvc = delvc_in, e_old = e_old_in, p_old = p_old_in, q_old = q_old_in, vnewc = vnewc_in;
+    if (REGION) { opaque(delvc); opaque(e_old); opaque(p_old); opaque(q_old); opaque(vnewc); }
     double compression = 1.0 / vnewc - 1.0;
     const double vchalf = fma(delvc, -0.5, vnewc);
     double compHalfStep = 1.0 / vchalf - 1.0;
@@ -640,8 +665,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       p_old = 0.0; compression = 0.0; compHalfStep = 0.0;
       if (TAPE) fl |= TF_VMAX_HIT;
     }
-    const double c1s = 2.0 / 3.0;
-    const double inv_rho0 = 1.0 / prm.refdens;
     const bool vmax_hit = vnewc >= prm.eosvmax;
     // calcPressureForElems (src/domain.jl:2585-2614) for one element; the
     // cut / pmin outcomes go to the tape bits given
@@ -651,10 +674,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       if (vmax_hit) pn = 0.0;
       if (pn < prm.pmin) { pn = prm.pmin; if (TAPE) fl |= min_bit; }
       return pn;
-    };
-    auto tiny_sqrt = [&](double ssc, unsigned long long bit) -> double {
-      if (ssc <= 0.111111e-36) { if (TAPE) fl |= bit; return 0.333333e-18; }
-      return sqrt(ssc);
     };
     const double pq_old = p_old + q_old;
     double e_new = fma(-0.5 * delvc, pq_old, e_old);
@@ -696,6 +715,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E3_CUT; }
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
     p_new = pressure(e_new, bvc, TF_PN2_CUT, TF_PN2_MIN);
+    e_out = e_new; p_out = p_new; vv_out = vv_bvc; compress_out = compress;
+    }  // rep loop
+    const double e_new = e_out, p_new = p_out, vv_bvc = vv_out;
+    const bool compress = compress_out;
+    double q_new = 0.0;
     // the last q evaluation and the sound speed share one expression
     const double ssc3 = fma(c1s, e_new, vv_bvc * p_new) * inv_rho0;
     const double ss_new = tiny_sqrt(ssc3, TF_SS_TINY);
@@ -807,19 +831,25 @@ void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuni
   const int bs = t.mat;
   const int grid = (d.E + bs - 1) / bs;
   const bool fix = (d.mode & 4) != 0;
+  const bool region = d.regOrder != nullptr;
+#define LULESH_MAT(M, AUX, ENS, TAPE, REGION) k_material<M, AUX, ENS, TAPE, REGION><<<grid, bs, 0, s>>>(d, prm)
   if (d.elemInst) {
-    if (fix) k_material<4, false, true, false><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<0, false, true, false><<<grid, bs, 0, s>>>(d, prm);
+    if (fix) LULESH_MAT(4, false, true, false, false);
+    else LULESH_MAT(0, false, true, false, false);
   } else if (d.tapeFlags) {
-    if (fix) k_material<4, false, false, true><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<0, false, false, true><<<grid, bs, 0, s>>>(d, prm);
+    if (fix) LULESH_MAT(4, false, false, true, false);
+    else LULESH_MAT(0, false, false, true, false);
+  } else if (region) {
+    if (fix) { if (aux) LULESH_MAT(4, true, false, false, true); else LULESH_MAT(4, false, false, false, true); }
+    else { if (aux) LULESH_MAT(0, true, false, false, true); else LULESH_MAT(0, false, false, false, true); }
   } else if (fix) {
-    if (aux) k_material<4, true, false, false><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<4, false, false, false><<<grid, bs, 0, s>>>(d, prm);
+    if (aux) LULESH_MAT(4, true, false, false, false);
+    else LULESH_MAT(4, false, false, false, false);
   } else {
-    if (aux) k_material<0, true, false, false><<<grid, bs, 0, s>>>(d, prm);
-    else k_material<0, false, false, false><<<grid, bs, 0, s>>>(d, prm);
+    if (aux) LULESH_MAT(0, true, false, false, false);
+    else LULESH_MAT(0, false, false, false, false);
   }
+#undef LULESH_MAT
 }
 
 void launch_time_increment(DevState* st, int n, const Params& prm, cudaStream_t s) {
