@@ -196,23 +196,28 @@ def run_reference(args):
     return 0
 
 
-def ensemble_leg(L, torch, dev, n, cycles):
+def ensemble_leg(L, torch, dev, n, cycles, world=1, rank=0):
     """Config C4: n seeded Sedov instances (nx in [16, 64], einit x U-log[0.5, 2],
     hgcoef in [2, 4], nr 1 or 11) advanced `cycles` cycles as one device-resident
-    ensemble, against looping the single-problem GPU path over the same instances."""
-    inst = L.sedov_instances(0xC4, n, 16, 64)
+    ensemble, against looping the single-problem GPU path over the same instances.
+    With several ranks each advances its lulesh_ens_partition shard (no
+    collective on the data path); times are the max over ranks."""
+    all_inst = L.sedov_instances(0xC4, n, 16, 64)
+    _, inst = L.shard(all_inst, world, rank) if world > 1 else (None, all_inst)
     ens = L.Ensemble(inst, mode=0, device=dev)
     tuning = ens.autotune(cycles=2)  # returns the ensemble to its initial state
-    init_dt = [ens.scalars(i)["deltatime"] for i in range(n)]
+    mine = len(inst)
+    init_dt = [ens.scalars(i)["deltatime"] for i in range(mine)]
     stream = torch.cuda.ExternalStream(ens.stream(), device=dev)
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize(dev)
+    barrier(world)
     a.record(stream)
     ens.run(cycles)
     b.record(stream)
     torch.cuda.synchronize(dev)
-    ens_s = a.elapsed_time(b) * 1e-3
-    done = sum(ens.scalars(i)["cycle"] == cycles for i in range(n))
+    ens_s = max_over_ranks(a.elapsed_time(b) * 1e-3, world)
+    done = sum(ens.scalars(i)["cycle"] == cycles for i in range(mine))
     total_elems = ens.total_elem
     ens.close()
     # the same instances, one single-problem handle after another (setup untimed)
@@ -232,13 +237,15 @@ def ensemble_leg(L, torch, dev, n, cycles):
         torch.cuda.synchronize(dev)
         loop_s += a.elapsed_time(b) * 1e-3
         g.close()
+    loop_s = max_over_ranks(loop_s, world)
     return {"config": f"{n} Sedov instances, nx uniform in [16, 64] (seed 0xC4), {cycles} cycles each, FP64",
-            "instances": n, "cycles": cycles, "total_elements": total_elems,
-            "instances_completed": done,
+            "instances": n, "cycles": cycles, "total_elements_rank0": total_elems,
+            "instances_rank0": mine, "instances_completed_rank0": int(done),
+            "sharding": f"lulesh_ens_partition over {world} rank(s)" if world > 1 else "one GPU",
             "problems_per_s": n / ens_s, "seconds": ens_s,
             "looped_plain_problems_per_s": n / loop_s, "looped_plain_seconds": loop_s,
             "speedup_vs_looped_plain": loop_s / ens_s,
-            "zones_cycles_per_s": total_elems * cycles / ens_s,
+            "zones_cycles_per_s_rank0": total_elems * cycles / ens_s,
             "tuning": tuning}
 
 
@@ -421,6 +428,11 @@ def run_ours(args):
            "h2d_bytes_per_step": scalar_bytes + state_bytes / cycles,
            "d2h_bytes_per_step": scalar_bytes + state_bytes / cycles}
 
+    # the ensemble leg runs on every rank (each advances its shard)
+    ensemble = None
+    if not args.no_ensemble:
+        ensemble = ensemble_leg(L, torch, dev, args.ens_instances, args.ens_cycles, world, rank)
+
     if rank != 0:
         g.close()
         return 0
@@ -446,21 +458,13 @@ def run_ours(args):
         fp64.update({"kernel": "k_force", "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
                      "fp64_inst_per_launch": prof["fp64_inst_per_launch"]})
 
-    ensemble = None
-    if not args.no_ensemble:
-        g.close()
-        ensemble = ensemble_leg(L, torch, dev, args.ens_instances, args.ens_cycles)
-
+    g.close()  # the remaining legs build their own problems
     c3 = None
     if not args.no_c3:
-        if ensemble is None:
-            g.close()
         c3 = c3_leg(L, torch, dev, args.c3_nx, args.c3_cycles)
 
     adjoint = None
     if not args.no_adjoint:
-        if ensemble is None:
-            g.close()
         adjoint = adjoint_leg(L, torch, dev, args.adj_nx, args.adj_cycles, args.adj_every, args.adj_dirs)
 
     cpu = None

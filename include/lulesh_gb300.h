@@ -238,6 +238,13 @@ int lulesh_ens_get_tuning(const lulesh_ensemble* ens, lulesh_tuning* out);
 int lulesh_ens_set_tuning(lulesh_ensemble* ens, const lulesh_tuning* t);
 int lulesh_ens_autotune(lulesh_ensemble* ens, int32_t cycles, lulesh_tuning* chosen);
 
+/* Splits instances over `parts` GPUs (one rank each) for a run with no
+ * data-path collective: longest-processing-time greedy on the cost nx^3
+ * (largest first, ties by index), each instance to the part with the least
+ * cost so far (ties to the lowest part). part_of[i] receives instance i's
+ * part. Host only; deterministic, so every rank computes the same split. */
+int lulesh_ens_partition(const lulesh_instance* instances, int32_t n, int32_t parts, int32_t* part_of);
+
 /* Diagnostic without a reference counterpart: measures the device's FP64
  * FMA and add issue rates (instructions per second), the roof this FP64
  * step is bound by. */

@@ -140,6 +140,26 @@ static void launch_cycle(lulesh_ensemble* s) {
 
 extern "C" {
 
+int lulesh_ens_partition(const lulesh_instance* in, int32_t n, int32_t parts, int32_t* part_of) {
+  if (!in || !part_of || n < 0 || parts < 1) return LULESH_ERR_ARGUMENT;
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) {
+    if (in[i].nx < 1) return LULESH_ERR_ARGUMENT;
+    order[i] = i;
+  }
+  auto cost = [&](int i) { return (double)in[i].nx * in[i].nx * in[i].nx; };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+  std::vector<double> load(parts, 0.0);
+  for (int i : order) {
+    int best = 0;
+    for (int p = 1; p < parts; ++p)
+      if (load[p] < load[best]) best = p;
+    part_of[i] = best;
+    load[best] += cost(i);
+  }
+  return LULESH_OK;
+}
+
 int lulesh_ens_sedov_instances(uint64_t seed, int32_t n, int32_t nx_min, int32_t nx_max,
                                lulesh_instance* out) {
   if (!out || n < 1 || nx_min < 1 || nx_max < nx_min) return LULESH_ERR_ARGUMENT;

@@ -21,7 +21,7 @@ __all__ = [
     "LuleshProblem", "Domain", "timeIncrement", "lagrangeLeapFrog", "run",
     "verifyAndWriteFinalOutput", "LuleshError", "load_library", "library_path",
     "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2", "Ensemble", "sedov_instances",
-    "Adjoint", "STATE_FIELDS",
+    "Adjoint", "STATE_FIELDS", "partition", "shard",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -173,6 +173,7 @@ def load_library():
         "lulesh_ens_get_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
         "lulesh_ens_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
         "lulesh_ens_autotune": (ctypes.c_int, [P, i32, ctypes.POINTER(Tuning)]),
+        "lulesh_ens_partition": (ctypes.c_int, [ctypes.POINTER(Instance), i32, i32, ctypes.POINTER(i32)]),
         "lulesh_adj_create": (ctypes.c_int, [P, dbl, i32, ctypes.POINTER(P)]),
         "lulesh_adj_destroy": (ctypes.c_int, [P]),
         "lulesh_adj_set_seed": (ctypes.c_int, [P, i32, P, i64]),
@@ -402,6 +403,37 @@ def sedov_instances(seed=0xC4, n=256, nx_min=16, nx_max=64):
     return [{k: getattr(a, k) for k, _ in Instance._fields_} for a in arr]
 
 
+def _instance_array(instances):
+    """lulesh_instance array; missing keys take the reference's defaults."""
+    arr = (Instance * max(1, len(instances)))()
+    for a, spec in zip(arr, instances):
+        a.nx = int(spec["nx"])
+        a.nr = int(spec.get("nr", 11))
+        a.balance = int(spec.get("balance", 1))
+        a.cost = int(spec.get("cost", 1))
+        a.einit = float(spec.get("einit", 0.0))
+        a.hgcoef = float(spec.get("hgcoef", 3.0))
+        a.region_seed = int(spec.get("region_seed", 0))
+    return arr
+
+
+def partition(instances, parts):
+    """lulesh_ens_partition: the part (GPU rank) of every instance, balancing
+    the cost nx^3 greedily, largest first. Deterministic."""
+    L = load_library()
+    n = len(instances)
+    out = (ctypes.c_int32 * max(1, n))()
+    _check(L.lulesh_ens_partition(_instance_array(instances), n, int(parts), out), "partition")
+    return [int(out[i]) for i in range(n)]
+
+
+def shard(instances, world, rank):
+    """The instances rank `rank` of `world` advances (indices and specs)."""
+    part = partition(instances, world)
+    idx = [i for i, p in enumerate(part) if p == rank]
+    return idx, [instances[i] for i in idx]
+
+
 class Ensemble:
     """Many independent Sedov problems advanced together on one GPU.
 
@@ -414,15 +446,7 @@ class Ensemble:
     def __init__(self, instances, mode=MODE_FAITHFUL, device=0):
         L = load_library()
         n = len(instances)
-        arr = (Instance * n)()
-        for a, spec in zip(arr, instances):
-            a.nx = int(spec["nx"])
-            a.nr = int(spec.get("nr", 11))
-            a.balance = int(spec.get("balance", 1))
-            a.cost = int(spec.get("cost", 1))
-            a.einit = float(spec.get("einit", 0.0))
-            a.hgcoef = float(spec.get("hgcoef", 3.0))
-            a.region_seed = int(spec.get("region_seed", 0))
+        arr = _instance_array(instances)
         h = ctypes.c_void_p()
         _check(L.lulesh_ens_create(arr, n, int(mode), int(device), ctypes.byref(h)), "ensemble create")
         self._L, self._h, self.n = L, h, n
