@@ -66,21 +66,31 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
   }
 
+  // The 12 face diagonals (two per face, in calcElemNodeNormals' argument
+  // order p2 - p0, p3 - p1) serve the node normals and the volume derivatives.
+  // Face f: (2,0,3,1) (5,0,1,4) (6,1,2,5) (7,2,3,6) (4,3,0,7) (6,4,5,7).
+  double g[12][3];
+  {
+    constexpr int pa[12] = {2, 3, 5, 1, 6, 2, 7, 3, 4, 0, 6, 5};
+    constexpr int pb[12] = {0, 1, 0, 4, 1, 5, 2, 6, 3, 7, 4, 7};
+#pragma unroll
+    for (int q = 0; q < 12; ++q) {
+      g[q][0] = x[pa[q]] - x[pb[q]];
+      g[q][1] = y[pa[q]] - y[pb[q]];
+      g[q][2] = z[pa[q]] - z[pb[q]];
+    }
+  }
+
   // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
   // face-diagonal cross products; true B = -Bc/8.
   double Bx[8], By[8], Bz[8];
   {
-    // face diagonals (p2 - p0, p3 - p1) in the reference's argument order
-    constexpr int fd[6][4] = {{2, 0, 3, 1}, {5, 0, 1, 4}, {6, 1, 2, 5},
-                              {7, 2, 3, 6}, {4, 3, 0, 7}, {6, 4, 5, 7}};
     double nx[6], ny[6], nz[6];
 #pragma unroll
     for (int f = 0; f < 6; ++f) {
-      const double d1x = x[fd[f][0]] - x[fd[f][1]], d1y = y[fd[f][0]] - y[fd[f][1]],
-                   d1z = z[fd[f][0]] - z[fd[f][1]];
-      const double d2x = x[fd[f][2]] - x[fd[f][3]], d2y = y[fd[f][2]] - y[fd[f][3]],
-                   d2z = z[fd[f][2]] - z[fd[f][3]];
-      cross(d1x, d1y, d1z, d2x, d2y, d2z, nx[f], ny[f], nz[f]);
+      const double* d1 = g[2 * f];
+      const double* d2 = g[2 * f + 1];
+      cross(d1[0], d1[1], d1[2], d2[0], d2[1], d2[2], nx[f], ny[f], nz[f]);
       if (TAPE) {
         d.tapeGeo[(48 + f) * E + e] = nx[f];
         d.tapeGeo[(54 + f) * E + e] = ny[f];
@@ -103,48 +113,52 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     Bx[7] = (nx[3] + nx[4]) + nx[5]; By[7] = (ny[3] + ny[4]) + ny[5]; Bz[7] = (nz[3] + nz[4]) + nz[5];
   }
 
-  // calcElemVolumeDerivative (src/domain.jl:1213-1256), times 12, from the
-  // 12 edge sums. The n-th call differentiates w.r.t. node owner[n]; the
-  // reference stores it in slot n (slots 1 and 3 exchanged).
+  // calcElemVolumeDerivative (src/domain.jl:1178-1256), times 12: its eight
+  // voluDer calls are the gradient of 12*volume, and 12*volume is
+  // calcElemVolume's sum of three triple products U.(V x W) of face
+  // diagonals (src/utils.jl:36-116): (d31+d72).(d63 x d20),
+  // (d43+d57).(d64 x d70), (d14+d25).(d61 x d50). The gradient w.r.t. U, V,
+  // W is V x W, W x U, U x V, scattered to their corners. The n-th reference
+  // call differentiates w.r.t. node owner[n] and stores in slot n (slots 1
+  // and 3 exchanged) unless corrected.
   double dvx[8], dvy[8], dvz[8];
   {
-    // edges: 01 03 04 12 15 23 26 37 45 47 56 67
-    double ex[12], ey[12], ez[12];
-    constexpr int ea[12] = {0, 0, 0, 1, 1, 2, 2, 3, 4, 4, 5, 6};
-    constexpr int eb[12] = {1, 3, 4, 2, 5, 3, 6, 7, 5, 7, 6, 7};
-#pragma unroll
-    for (int k = 0; k < 12; ++k) {
-      ex[k] = x[ea[k]] + x[eb[k]];
-      ey[k] = y[ea[k]] + y[eb[k]];
-      ez[k] = z[ea[k]] + z[eb[k]];
+    double gU[3][3], gV[3][3], gW[3][3];
+    auto grads = [&](int t, const double U[3], const double V[3], const double W[3]) {
+      cross(V[0], V[1], V[2], W[0], W[1], W[2], gU[t][0], gU[t][1], gU[t][2]);
+      cross(W[0], W[1], W[2], U[0], U[1], U[2], gV[t][0], gV[t][1], gV[t][2]);
+      cross(U[0], U[1], U[2], V[0], V[1], V[2], gW[t][0], gW[t][1], gW[t][2]);
+    };
+    {
+      // diagonals: 0 d20, 1 d31, 2 d50, 3 d14, 4 d61, 5 d25, 6 d72, 7 d36, 8 d43, 9 d07, 10 d64, 11 d57
+      const double U1[3] = {g[1][0] + g[6][0], g[1][1] + g[6][1], g[1][2] + g[6][2]};
+      const double V1[3] = {-g[7][0], -g[7][1], -g[7][2]};
+      grads(0, U1, V1, g[0]);
+      const double U2[3] = {g[8][0] + g[11][0], g[8][1] + g[11][1], g[8][2] + g[11][2]};
+      const double W2[3] = {-g[9][0], -g[9][1], -g[9][2]};
+      grads(1, U2, g[10], W2);
+      const double U3[3] = {g[3][0] + g[5][0], g[3][1] + g[5][1], g[3][2] + g[5][2]};
+      grads(2, U3, g[4], g[2]);
     }
-    constexpr int perm[8][6] = {{1, 2, 3, 4, 5, 7}, {0, 1, 2, 7, 4, 6}, {3, 0, 1, 6, 7, 5},
-                                {2, 3, 0, 5, 6, 4}, {7, 6, 5, 0, 3, 1}, {4, 7, 6, 1, 0, 2},
-                                {5, 4, 7, 2, 1, 3}, {6, 5, 4, 3, 2, 0}};
-    constexpr int owner[8] = {0, 3, 2, 1, 4, 5, 6, 7};
+    // corners: U1 = +3 -1 +7 -2, V1 = +6 -3, W1 = +2 -0; U2 = +4 -3 +5 -7,
+    // V2 = +6 -4, W2 = +7 -0; U3 = +1 -4 +2 -5, V3 = +6 -1, W3 = +5 -0
+    double gr[8][3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      gr[0][k] = -((gW[0][k] + gW[1][k]) + gW[2][k]);
+      gr[1][k] = (gU[2][k] - gU[0][k]) - gV[2][k];
+      gr[2][k] = (gW[0][k] - gU[0][k]) + gU[2][k];
+      gr[3][k] = (gU[0][k] - gV[0][k]) - gU[1][k];
+      gr[4][k] = (gU[1][k] - gV[1][k]) - gU[2][k];
+      gr[5][k] = (gU[1][k] - gU[2][k]) + gW[2][k];
+      gr[6][k] = (gV[0][k] + gV[1][k]) + gV[2][k];
+      gr[7][k] = (gU[0][k] - gU[1][k]) + gW[1][k];
+    }
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
-      const int* q = perm[n];
-      // edge index of an unordered node pair
-      auto eidx = [](int a, int b) -> int {
-        const int lo = a < b ? a : b, hi = a < b ? b : a;
-        return lo == 0 ? (hi == 1 ? 0 : hi == 3 ? 1 : 2)
-             : lo == 1 ? (hi == 2 ? 3 : 4)
-             : lo == 2 ? (hi == 3 ? 5 : 6)
-             : lo == 3 ? 7
-             : lo == 4 ? (hi == 5 ? 8 : 9)
-             : lo == 5 ? 10 : 11;
-      };
-      const int p12 = eidx(q[1], q[2]), p01 = eidx(q[0], q[1]), p04 = eidx(q[0], q[4]);
-      const int p34 = eidx(q[3], q[4]), p25 = eidx(q[2], q[5]), p35 = eidx(q[3], q[5]);
-      const double vx = fma(ey[p12], ez[p01], fma(-ey[p01], ez[p12], fma(ey[p04], ez[p34],
-                        fma(-ey[p34], ez[p04], fma(-ey[p25], ez[p35], ey[p35] * ez[p25])))));
-      const double vy = fma(-ex[p12], ez[p01], fma(ex[p01], ez[p12], fma(-ex[p04], ez[p34],
-                        fma(ex[p34], ez[p04], fma(ex[p25], ez[p35], -(ex[p35] * ez[p25]))))));
-      const double vz = fma(-ey[p12], ex[p01], fma(ey[p01], ex[p12], fma(-ey[p04], ex[p34],
-                        fma(ey[p34], ex[p04], fma(ey[p25], ex[p35], -(ey[p35] * ex[p25]))))));
-      const int slot = (MODE & 2) ? owner[n] : n;
-      dvx[slot] = vx; dvy[slot] = vy; dvz[slot] = vz;
+      // faithful slots: node 3's derivative in slot 1 and node 1's in slot 3
+      const int src = (MODE & 2) ? n : (n == 1 ? 3 : n == 3 ? 1 : n);
+      dvx[n] = gr[src][0]; dvy[n] = gr[src][1]; dvz[n] = gr[src][2];
     }
   }
 
