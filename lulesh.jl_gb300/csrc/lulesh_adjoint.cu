@@ -59,8 +59,8 @@ struct CycleTape {
   double *vnew, *delv, *arealg, *vdov, *dv[3], *dx[3];
   unsigned long long* flags;
   double *dtc, *dth;
-  double* geo;  // [66][E] force-kernel tape
-  double* kin;  // [45][E] kinematics-kernel tape
+  double* geo;  // [102][E] force-kernel tape
+  double* kin;  // [90][E] kinematics-kernel tape
   double* mat;  // [31][E] material-kernel tape
 };
 
@@ -306,8 +306,8 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
     if ((rc = dalloc(a, &t.ax, N)) || (rc = dalloc(a, &t.ay, N)) || (rc = dalloc(a, &t.az, N)) ||
         (rc = dalloc(a, &t.vnew, E)) || (rc = dalloc(a, &t.delv, E)) || (rc = dalloc(a, &t.arealg, E)) ||
         (rc = dalloc(a, &t.vdov, E)) || (rc = dalloc(a, &t.flags, E)) || (rc = dalloc(a, &t.dtc, E)) ||
-        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 66 * (size_t)E)) ||
-        (rc = dalloc(a, &t.kin, 45 * (size_t)E)) || (rc = dalloc(a, &t.mat, 31 * (size_t)E)))
+        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 102 * (size_t)E)) ||
+        (rc = dalloc(a, &t.kin, 90 * (size_t)E)) || (rc = dalloc(a, &t.mat, 31 * (size_t)E)))
       return fail(rc);
     for (int k = 0; k < 3; ++k)
       if ((rc = dalloc(a, &t.dv[k], E)) || (rc = dalloc(a, &t.dx[k], E))) return fail(rc);

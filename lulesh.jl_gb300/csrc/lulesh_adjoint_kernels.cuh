@@ -58,8 +58,8 @@ struct AdjDev {
   const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
   const double *dvl[3], *dxl[3];              // delv_{xi,eta,zeta}, delx_{xi,eta,zeta}
   const unsigned long long* flags;
-  const double* geo;
-  const double* kin;                          // [45][E] kinematics-kernel tape
+  const double* geo;                          // [102][E] force-kernel tape (dv, hms, S, N, diagonals)
+  const double* kin;                          // [90][E] kinematics-kernel tape
   const double* mat;                          // [31][E] material-kernel tape                          // [48][E] force-kernel tape (dv, hms, S)
   // adjoints of the state (in place: S1 on entry, S0 on exit)
   double *lx, *ly, *lz, *lxd, *lyd, *lzd;     // N
@@ -357,12 +357,6 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
   const double dt = rec->dt;
   double Ldt = 0.0;
   if (e < E) {
-    int nd[8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
-    double X[3][8];
-#pragma unroll
-    for (int c = 0; c < 8; ++c) { X[0][c] = a.x1[nd[c]]; X[1][c] = a.y1[nd[c]]; X[2][c] = a.z1[nd[c]]; }
     // forward values from the kinematics kernel's tape (slots: see tapeKin)
     auto tk = [&](int q) { return a.kin[q * E + e]; };
     double LX[3][8], LV[3][8];
@@ -465,9 +459,10 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
     }
     // ---- volume and characteristic length ----
     {
-      auto dg = [&](int p, int q) { return v3(X[0][p] - X[0][q], X[1][p] - X[1][q], X[2][p] - X[2][q]); };
-      const V3 d61 = dg(6, 1), d70 = dg(7, 0), d63 = dg(6, 3), d20 = dg(2, 0), d50 = dg(5, 0), d64 = dg(6, 4);
-      const V3 d31 = dg(3, 1), d72 = dg(7, 2), d43 = dg(4, 3), d57 = dg(5, 7), d14 = dg(1, 4), d25 = dg(2, 5);
+      // the 12 diagonals of the new positions, from the tape
+      auto dg = [&](int q) { return v3(tk(45 + 3 * q), tk(46 + 3 * q), tk(47 + 3 * q)); };
+      const V3 d61 = dg(0), d70 = dg(1), d63 = dg(2), d20 = dg(3), d50 = dg(4), d64 = dg(5);
+      const V3 d31 = dg(6), d72 = dg(7), d43 = dg(8), d57 = dg(9), d14 = dg(10), d25 = dg(11);
       // the three triple products of calcElemVolume: U.(V x W)
       V3 U1 = d31; vadd(U1, d72);
       V3 U2 = d43; vadd(U2, d57);
@@ -494,11 +489,12 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
       V3 L61 = v3(0, 0, 0), L70 = v3(0, 0, 0), L63 = v3(0, 0, 0), L20 = v3(0, 0, 0), L50 = v3(0, 0, 0), L64 = v3(0, 0, 0);
       V3 L31 = v3(0, 0, 0), L72 = v3(0, 0, 0), L43 = v3(0, 0, 0), L57 = v3(0, 0, 0), L14 = v3(0, 0, 0), L25 = v3(0, 0, 0);
       {
-        const V3 gU1 = vcross(d63, d20), gV1 = vcross(d20, U1), gW1 = vcross(U1, d63);
+        // V x W of each triple product is taped; the other two factors are not
+        const V3 gU1 = v3(tk(81), tk(82), tk(83)), gV1 = vcross(d20, U1), gW1 = vcross(U1, d63);
         vaxpy(L31, Lv12, gU1); vaxpy(L72, Lv12, gU1); vaxpy(L63, Lv12, gV1); vaxpy(L20, Lv12, gW1);
-        const V3 gU2 = vcross(d64, d70), gV2 = vcross(d70, U2), gW2 = vcross(U2, d64);
+        const V3 gU2 = v3(tk(84), tk(85), tk(86)), gV2 = vcross(d70, U2), gW2 = vcross(U2, d64);
         vaxpy(L43, Lv12, gU2); vaxpy(L57, Lv12, gU2); vaxpy(L64, Lv12, gV2); vaxpy(L70, Lv12, gW2);
-        const V3 gU3 = vcross(d61, d50), gV3 = vcross(d50, U3), gW3 = vcross(U3, d61);
+        const V3 gU3 = v3(tk(87), tk(88), tk(89)), gV3 = vcross(d50, U3), gW3 = vcross(U3, d61);
         vaxpy(L14, Lv12, gU3); vaxpy(L25, Lv12, gU3); vaxpy(L61, Lv12, gV3); vaxpy(L50, Lv12, gW3);
       }
       if (f == 0) { vadd(L20, Lfa); vadd(L31, Lfb); }
@@ -518,8 +514,9 @@ __global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const Cycle
     for (int k = 0; k < 3; ++k)
 #pragma unroll
       for (int c = 0; c < 8; ++c) {
-        a.cX[(k * 8 + c) * E + e] = LX[k][c];
-        a.cV[(k * 8 + c) * E + e] = LV[k][c];
+        // plus the pending force-transpose corners of the cycle after this one
+        a.cX[(k * 8 + c) * E + e] = LX[k][c] + a.fX[(k * 8 + c) * E + e];
+        a.cV[(k * 8 + c) * E + e] = LV[k][c] + a.fV[(k * 8 + c) * E + e];
       }
   }
   block_sum_to(Ldt, a.part_dt);
@@ -559,27 +556,24 @@ __global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, const CycleRec* r
     double* Lf[3] = {a.lfx, a.lfy, a.lfz};
     const double* xd1[3] = {a.xd1, a.yd1, a.zd1};
     const double* acc[3] = {a.ax, a.ay, a.az};
-    // the end-state adjoints gather the force transpose of the cycle after
-    // this one (pending corners) and this cycle's kinematics transpose
+    // the end-state adjoints gather this cycle's kinematics transpose and
+    // (added per corner by ka_kinematics) the force transpose of the cycle
+    // after this one
     double gx[3] = {0.0, 0.0, 0.0}, gv[3] = {0.0, 0.0, 0.0};
-    double fx[3] = {0.0, 0.0, 0.0}, fv[3] = {0.0, 0.0, 0.0};
     {
       const int s = a.nodeElemStart[i], t = a.nodeElemStart[i + 1];
       const long long E8 = 8ll * a.E;
       for (int j = s; j < t; ++j) {
         const int c = a.cornerList[j];
 #pragma unroll
-        for (int k = 0; k < 3; ++k) {
-          fx[k] += a.fX[k * E8 + c]; fv[k] += a.fV[k * E8 + c];
-          gx[k] += a.cX[k * E8 + c]; gv[k] += a.cV[k * E8 + c];
-        }
+        for (int k = 0; k < 3; ++k) { gx[k] += a.cX[k * E8 + c]; gv[k] += a.cV[k * E8 + c]; }
       }
     }
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double lxn = (Lx[k][i] + fx[k]) + gx[k];
+      const double lxn = Lx[k][i] + gx[k];
       const double v1 = xd1[k][i];
-      double lv = ((Lxd[k][i] + fv[k]) + gv[k]) + lxn * dt;   // x1 = x0 + xd1*dt
+      double lv = (Lxd[k][i] + gv[k]) + lxn * dt;   // x1 = x0 + xd1*dt
       Ldt += lxn * v1;
       double lf = 0.0;
       if (v1 == 0.0) {
@@ -795,12 +789,10 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
   int nd[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
-  double X[3][8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) { X[0][c] = a.x0[nd[c]]; X[1][c] = a.y0[nd[c]]; X[2][c] = a.z0[nd[c]]; }
-  auto dg = [&](int p, int q) { return v3(X[0][p] - X[0][q], X[1][p] - X[1][q], X[2][p] - X[2][q]); };
-  const V3 d20 = dg(2, 0), d31 = dg(3, 1), d50 = dg(5, 0), d14 = dg(1, 4), d61 = dg(6, 1), d25 = dg(2, 5);
-  const V3 d72 = dg(7, 2), d36 = dg(3, 6), d43 = dg(4, 3), d07 = dg(0, 7), d64 = dg(6, 4), d57 = dg(5, 7);
+  // the 12 face diagonals of the cycle's start positions, from the tape
+  auto dg = [&](int q) { return v3(a.geo[(66 + 3 * q) * E + e], a.geo[(67 + 3 * q) * E + e], a.geo[(68 + 3 * q) * E + e]); };
+  const V3 d20 = dg(0), d31 = dg(1), d50 = dg(2), d14 = dg(3), d61 = dg(4), d25 = dg(5);
+  const V3 d72 = dg(6), d36 = dg(7), d43 = dg(8), d07 = dg(9), d64 = dg(10), d57 = dg(11);
   double LX[3][8];
   // hourglass modes hm_k = Gamma(X_k)
 #pragma unroll

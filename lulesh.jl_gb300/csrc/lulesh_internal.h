@@ -120,14 +120,18 @@ struct DevDomain {
   unsigned long long* tapeFlags;
   double* tapeDtc;
   double* tapeDth;
-  // [66][E]: the force kernel's volume derivatives dv_j[n] (24, node order),
-  // hourglass modes over 12*determ (12), mode sums S_k[m] of the velocities
-  // (12) and face-diagonal cross products (x, y, z of the 6 faces: 18)
+  // [102][E]: the force kernel's volume derivatives dv_j[n] (24, node
+  // order), hourglass modes over 12*determ (12), mode sums S_k[m] of the
+  // velocities (12), face-diagonal cross products (x, y, z of the 6 faces:
+  // 18) and the 12 face diagonals d20 d31 d50 d14 d61 d25 d72 d36 d43 d07
+  // d64 d57 (36)
   double* tapeGeo;
-  // [45][E]: the kinematics kernel's Walsh vectors of positions (9) and
+  // [90][E]: the kinematics kernel's Walsh vectors of positions (9) and
   // velocities (9), cofactor columns (9), 1/det (1), monotonic-Q cross
   // products (9) with their reciprocal norms (3), 1/(64 vol) (1), the largest
-  // face's diagonal cross product (3) and rsqrt of its square norm (1)
+  // face's diagonal cross product (3) and rsqrt of its square norm (1), the
+  // 12 diagonals d61 d70 d63 d20 d50 d64 d31 d72 d43 d57 d14 d25 of the new
+  // positions (36) and the V x W factors of the three volume triple products (9)
   double* tapeKin;
   // [31][E]: the material kernel's limiter terms (norm, scaled neighbours:
   // 9), Q terms (rho, qlin, qquad, and their two sums: 5) and EOS values

@@ -78,6 +78,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
       g[q][0] = x[pa[q]] - x[pb[q]];
       g[q][1] = y[pa[q]] - y[pb[q]];
       g[q][2] = z[pa[q]] - z[pb[q]];
+      if (TAPE) {
+        d.tapeGeo[(66 + 3 * q) * E + e] = g[q][0];
+        d.tapeGeo[(67 + 3 * q) * E + e] = g[q][1];
+        d.tapeGeo[(68 + 3 * q) * E + e] = g[q][2];
+      }
     }
   }
 
@@ -315,11 +320,27 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
       d50[k] = p[5] - p[0]; d64[k] = p[6] - p[4]; d31[k] = p[3] - p[1]; d72[k] = p[7] - p[2];
       d43[k] = p[4] - p[3]; d57[k] = p[5] - p[7]; d14[k] = p[1] - p[4]; d25[k] = p[2] - p[5];
     }
+    double gu[3][3];  // V x W of each triple product (kept for the tape)
     const double v12 =
-        triple(d31[0] + d72[0], d63[0], d20[0], d31[1] + d72[1], d63[1], d20[1], d31[2] + d72[2], d63[2], d20[2]) +
-        triple(d43[0] + d57[0], d64[0], d70[0], d43[1] + d57[1], d64[1], d70[1], d43[2] + d57[2], d64[2], d70[2]) +
-        triple(d14[0] + d25[0], d61[0], d50[0], d14[1] + d25[1], d61[1], d50[1], d14[2] + d25[2], d61[2], d50[2]);
+        triple(d31[0] + d72[0], d63[0], d20[0], d31[1] + d72[1], d63[1], d20[1], d31[2] + d72[2], d63[2], d20[2],
+               gu[0]) +
+        triple(d43[0] + d57[0], d64[0], d70[0], d43[1] + d57[1], d64[1], d70[1], d43[2] + d57[2], d64[2], d70[2],
+               gu[1]) +
+        triple(d14[0] + d25[0], d61[0], d50[0], d14[1] + d25[1], d61[1], d50[1], d14[2] + d25[2], d61[2], d50[2],
+               gu[2]);
     volume = v12 * (1.0 / 12.0);
+    if (TAPE) {
+      // the 12 diagonals d61 d70 d63 d20 d50 d64 d31 d72 d43 d57 d14 d25 and the crosses
+      const double* dgl[12] = {d61, d70, d63, d20, d50, d64, d31, d72, d43, d57, d14, d25};
+#pragma unroll
+      for (int q = 0; q < 12; ++q)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d.tapeKin[(45 + 3 * q + k) * E + e] = dgl[q][k];
+#pragma unroll
+      for (int t = 0; t < 3; ++t)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) d.tapeKin[(81 + 3 * t + k) * E + e] = gu[t][k];
+    }
     // areaFace (src/domain.jl:1874-1891): with f, g = a -/+ b for the face
     // diagonals a, b, |f|^2|g|^2 - (f.g)^2 = |f x g|^2 = 4 |a x b|^2; the 4
     // is folded into arealg below.
