@@ -85,7 +85,6 @@ struct lulesh_adjoint {
   std::vector<StateBuf> slots;   // K+1 states of the current segment
   std::vector<CycleTape> tape;   // K cycles
   std::vector<StateBuf> ckpts;   // segment start states
-  std::vector<Scalars5> ckpt_scalars;
   std::vector<int> seg_len;      // cycles of each segment
   DevState* ckpt_st = nullptr;   // device: step state at each checkpoint
   int ckpt_st_cap = 0;
@@ -98,6 +97,11 @@ struct lulesh_adjoint {
   CycleRec* rec = nullptr;      // device: K cycle records of the current segment
   AdjScal* dsc = nullptr;       // device: carried scalar adjoints
   std::map<int32_t, double*> seeds;  // linear-objective weights per state field
+  // graph of K forward cycles for the checkpointed sweep, with what it bakes in
+  cudaGraphExec_t fwd_graph = nullptr;
+  Params fwd_prm{};
+  Tuning fwd_tuning{};
+  bool fwd_aux = false;
 };
 
 static int dmalloc(lulesh_adjoint* a, void** p, size_t bytes) {
@@ -420,6 +424,7 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   if (!a) return LULESH_ERR_ARGUMENT;
   cudaSetDevice(a->dom->params.device);
   cudaStreamSynchronize(a->dom->stream);
+  if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
   for (void* p : a->allocs) cudaFree(p);
   delete a;
   return LULESH_OK;
@@ -458,65 +463,82 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   const int K = a->K;
   lulesh_adj_result out{};
   int rc;
-  // ---- forward sweep with checkpoints: lulesh_run per segment, which stops
-  // early at stoptime as the examples/benchmark.jl loop does ----
+  // ---- forward sweep with checkpoints ----
+  // Segments of K cycles: each starts by copying the state and the device step
+  // state to its checkpoint; every segment but the last then runs as a
+  // captured graph of exactly K cycles (dt on the device; once time reaches
+  // stoptime, as in the examples/benchmark.jl loop, the remaining cycles are
+  // no-ops), and the last runs taped so that the reverse sweep need not
+  // recompute it. Nothing waits on the host until the sweep ends.
   auto t0 = std::chrono::steady_clock::now();
-  int64_t done = 0;
-  int nseg = 0;
-  bool last_taped = false;
-  a->seg_len.clear();
-  while (done < num_cycles && d->sc[LULESH_S_TIME] < d->sc[LULESH_S_STOPTIME]) {
-    if ((int)a->ckpts.size() == nseg) {
-      a->ckpts.emplace_back();
-      if ((rc = alloc_state(a, a->ckpts.back()))) { a->ckpts.pop_back(); return rc; }
-    }
-    if ((int)a->ckpt_scalars.size() == nseg) a->ckpt_scalars.emplace_back();
-    copy_state_from_domain(a, a->ckpts[nseg]);
-    a->ckpt_scalars[nseg] = get_scalars(d);
-    const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
-    const int64_t want = std::min<int64_t>(K, num_cycles - done);
-    if (want == num_cycles - done) {
-      // the final segment runs taped, so the reverse sweep needs no recompute of it
-      state_to_device_mirror(d);
-      ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
-      for (int j = 0; j < (int)want; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
-      copy_state_from_domain(a, a->slots[want]);
-      ACK(cudaGetLastError());
-      ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
-      ACK(cudaStreamSynchronize(s));
-      state_from_device_mirror(d);
-      rc = d->status;
-      last_taped = true;
-    } else {
-      rc = lulesh_run(d, c0 + want, nullptr);
-    }
-    const int64_t n = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
-    if (n > 0) { a->seg_len.push_back((int)n); ++nseg; done += n; }
-    if (rc) { out.status = rc; out.cycles = done; if (res) *res = out; return rc; }
-    if (n < want) break;
+  const int nplan = (int)((num_cycles + K - 1) / K);
+  const int last_len = (int)(num_cycles - (int64_t)(nplan - 1) * K);
+  while ((int)a->ckpts.size() < nplan) {
+    a->ckpts.emplace_back();
+    if ((rc = alloc_state(a, a->ckpts.back()))) { a->ckpts.pop_back(); return rc; }
   }
+  if (a->ckpt_st_cap < nplan) {
+    DevState* p = nullptr;
+    if ((rc = dalloc(a, &p, nplan))) return rc;
+    a->ckpt_st = p;
+    a->ckpt_st_cap = nplan;
+  }
+  const Params prm = make_params(d);
+  const bool aux = d->params.keep_aux != 0;
+  if (nplan > 1 && (!a->fwd_graph || std::memcmp(&a->fwd_prm, &prm, sizeof(Params)) != 0 ||
+                    std::memcmp(&a->fwd_tuning, &d->tuning, sizeof(Tuning)) != 0 || a->fwd_aux != aux)) {
+    if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
+    a->fwd_graph = nullptr;
+    cudaGraph_t g;
+    ACK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    for (int j = 0; j < K; ++j) {
+      launch_time_increment(d->dd.st, 1, prm, s);
+      launch_force(d->dd, prm, d->tuning, s);
+      launch_node(d->dd, prm, aux, d->tuning, s);
+      launch_kinematics(d->dd, prm, aux, d->tuning, s);
+      launch_material(d->dd, prm, aux, d->tuning, s);
+    }
+    ACK(cudaStreamEndCapture(s, &g));
+    const cudaError_t ge = cudaGraphInstantiate(&a->fwd_graph, g, 0);
+    cudaGraphDestroy(g);
+    ACK(ge);
+    a->fwd_prm = prm;
+    a->fwd_tuning = d->tuning;
+    a->fwd_aux = aux;
+  }
+  const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
+  state_to_device_mirror(d);  // no cycle limit: the segments count the cycles
+  ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
+  for (int k = 0; k < nplan; ++k) {
+    copy_state_from_domain(a, a->ckpts[k]);
+    ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+    if (k < nplan - 1) {
+      ACK(cudaGraphLaunch(a->fwd_graph, s));
+    } else {
+      for (int j = 0; j < last_len; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
+      copy_state_from_domain(a, a->slots[last_len]);
+    }
+  }
+  ACK(cudaGetLastError());
+  ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  ACK(cudaStreamSynchronize(s));
+  state_from_device_mirror(d);
+  const int64_t done = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
+  // segments that ran (a run that reached stoptime leaves later ones empty)
+  a->seg_len.clear();
+  for (int k = 0; k < nplan; ++k) {
+    const int64_t cap = k < nplan - 1 ? K : last_len;
+    const int64_t len = std::max<int64_t>(0, std::min<int64_t>(cap, done - (int64_t)k * K));
+    if (len == 0) break;
+    a->seg_len.push_back((int)len);
+  }
+  const int nseg = (int)a->seg_len.size();
+  const bool last_taped = nseg == nplan;
+  if (d->status) { out.status = d->status; out.cycles = done; if (res) *res = out; return d->status; }
   auto t1 = std::chrono::steady_clock::now();
   out.cycles = done;
   out.checkpoints = nseg;
-  // step state at each checkpoint, as lulesh_run uploads it
-  if (a->ckpt_st_cap < nseg) {
-    DevState* p = nullptr;
-    if ((rc = dalloc(a, &p, nseg))) return rc;
-    a->ckpt_st = p;
-    a->ckpt_st_cap = nseg;
-  }
-  {
-    std::vector<DevState> hs(nseg);
-    const Scalars5 now = get_scalars(d);
-    for (int k = 0; k < nseg; ++k) {
-      set_scalars(d, a->ckpt_scalars[k]);
-      state_to_device_mirror(d);
-      hs[k] = *d->hst;
-    }
-    set_scalars(d, now);
-    if (nseg) ACK(cudaMemcpyAsync(a->ckpt_st, hs.data(), nseg * sizeof(DevState), cudaMemcpyHostToDevice, s));
-    if ((rc = objective(a, true, &out.loss))) return rc;  // synchronises the stream (hs stays valid)
-  }
+  if ((rc = objective(a, true, &out.loss))) return rc;
   copy_state_from_domain(a, a->final_state);
   const Scalars5 final_sc = get_scalars(d);
   // ---- reverse sweep ----
