@@ -102,6 +102,10 @@ struct lulesh_adjoint {
   Params fwd_prm{};
   Tuning fwd_tuning{};
   bool fwd_aux = false;
+  // graph of one full segment's recompute and transpose
+  cudaGraphExec_t rev_graph = nullptr;
+  Params rev_prm{};
+  Tuning rev_tuning{};
 };
 
 static int dmalloc(lulesh_adjoint* a, void** p, size_t bytes) {
@@ -425,6 +429,7 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   cudaSetDevice(a->dom->params.device);
   cudaStreamSynchronize(a->dom->stream);
   if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
+  if (a->rev_graph) cudaGraphExecDestroy(a->rev_graph);
   for (void* p : a->allocs) cudaFree(p);
   delete a;
   return LULESH_OK;
@@ -545,11 +550,11 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
   ACK(cudaMemsetAsync(a->ad.fX, 0, 24 * sizeof(double) * (size_t)a->E, s));
   ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
-  for (int k = nseg - 1; k >= 0; --k) {
-    const int n = a->seg_len[k];
-    if (!(k == nseg - 1 && last_taped)) {
-      copy_state_to_domain(a, a->ckpts[k]);
-      ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+  // a full segment's recompute and transpose read and write the same slots,
+  // tape and records whichever segment it is: one captured graph serves all
+  // (rebuilt when the parameters it bakes in change)
+  auto queue_segment = [&](int n, bool recompute) {
+    if (recompute) {
       for (int j = 0; j < n; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
       copy_state_from_domain(a, a->slots[n]);
     }
@@ -557,6 +562,31 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
       set_cycle_pointers(a, a->slots[j], a->slots[j + 1], a->tape[j]);
       reverse_cycle(a, a->rec + j);
     }
+  };
+  const bool full_recomputed = nseg > 1 || (nseg == 1 && !last_taped);
+  if (full_recomputed && (!a->rev_graph || std::memcmp(&a->rev_prm, &prm, sizeof(Params)) != 0 ||
+                          std::memcmp(&a->rev_tuning, &d->tuning, sizeof(Tuning)) != 0)) {
+    if (a->rev_graph) cudaGraphExecDestroy(a->rev_graph);
+    a->rev_graph = nullptr;
+    cudaGraph_t g;
+    ACK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    queue_segment(K, true);
+    ACK(cudaStreamEndCapture(s, &g));
+    const cudaError_t ge = cudaGraphInstantiate(&a->rev_graph, g, 0);
+    cudaGraphDestroy(g);
+    ACK(ge);
+    a->rev_prm = prm;
+    a->rev_tuning = d->tuning;
+  }
+  for (int k = nseg - 1; k >= 0; --k) {
+    const int n = a->seg_len[k];
+    const bool recompute = !(k == nseg - 1 && last_taped);
+    if (recompute) {
+      copy_state_to_domain(a, a->ckpts[k]);
+      ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+    }
+    if (recompute && n == K) ACK(cudaGraphLaunch(a->rev_graph, s));
+    else queue_segment(n, recompute);
     ACK(cudaGetLastError());
   }
   // the first cycle's force transpose is still in the force corner buffers
