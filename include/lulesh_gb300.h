@@ -162,6 +162,17 @@ int lulesh_upload_field(lulesh_domain* dom, int32_t field, const void* host, int
  * out[3] = MaxRelDiff of the plane-0 symmetry check. */
 int lulesh_verify(lulesh_domain* dom, double out[4]);
 
+/* Full-state files. The reference has no checkpoint format; these write the
+ * handle's step state (x y z xd yd zd e p q v ss and every Domain scalar,
+ * cycle included) to a binary file with a header naming the problem
+ * (nx, nr, balance, cost, mode, sizes) and a trailing 64-bit FNV-1a hash, and
+ * load it into a handle of the same problem, which then continues exactly as
+ * the saved run would have. Loading checks the header and the hash before it
+ * changes anything; a mismatch or a short file returns LULESH_ERR_ARGUMENT.
+ * Format: lulesh.jl_gb300/csrc/lulesh_state_io.cu. */
+int lulesh_save_state(lulesh_domain* dom, const char* path);
+int lulesh_load_state(lulesh_domain* dom, const char* path);
+
 /* numElem and numNode of the handle. */
 int lulesh_sizes(const lulesh_domain* dom, int64_t* num_elem, int64_t* num_node);
 

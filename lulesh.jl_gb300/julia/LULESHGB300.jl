@@ -21,7 +21,7 @@ module LULESHGB300
 
 using LULESH
 
-export GPUDomain, LuleshGPUError, GPUAdjoint, energy_gradient!
+export GPUDomain, LuleshGPUError, GPUAdjoint, energy_gradient!, save_state, load_state!
 
 const libpath = get(ENV, "LULESH_GB300_LIB",
                     joinpath(@__DIR__, "..", "lib", "liblulesh_gb300.so"))
@@ -166,6 +166,21 @@ function Base.setproperty!(d::GPUDomain, s::Symbol, v)
         setfield!(d, s, v)
     end
     return v
+end
+
+# ---- full-state files (lulesh_save_state / lulesh_load_state) ----
+"Write the domain's step state (state fields and scalars) to `path`."
+function save_state(d::GPUDomain, path::AbstractString)
+    rc = ccall((:lulesh_save_state, libpath), Cint, (Ptr{Cvoid}, Cstring), getfield(d, :handle), path)
+    rc == 0 || throw(LuleshGPUError("save_state($path): status $rc", rc))
+    return path
+end
+
+"Load a state file written for the same problem into `d`."
+function load_state!(d::GPUDomain, path::AbstractString)
+    rc = ccall((:lulesh_load_state, libpath), Cint, (Ptr{Cvoid}, Cstring), getfield(d, :handle), path)
+    rc == 0 || throw(LuleshGPUError("load_state!($path): status $rc", rc))
+    return d
 end
 
 # ---- reverse-mode adjoint of a run (lulesh_adj_* of include/lulesh_gb300.h) ----

@@ -21,7 +21,7 @@ __all__ = [
     "LuleshProblem", "Domain", "timeIncrement", "lagrangeLeapFrog", "run",
     "verifyAndWriteFinalOutput", "LuleshError", "load_library", "library_path",
     "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2", "Ensemble", "sedov_instances",
-    "Adjoint", "STATE_FIELDS", "partition", "shard",
+    "Adjoint", "STATE_FIELDS", "partition", "shard", "read_state",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -174,6 +174,8 @@ def load_library():
         "lulesh_ens_set_tuning": (ctypes.c_int, [P, ctypes.POINTER(Tuning)]),
         "lulesh_ens_autotune": (ctypes.c_int, [P, i32, ctypes.POINTER(Tuning)]),
         "lulesh_ens_partition": (ctypes.c_int, [ctypes.POINTER(Instance), i32, i32, ctypes.POINTER(i32)]),
+        "lulesh_save_state": (ctypes.c_int, [P, ctypes.c_char_p]),
+        "lulesh_load_state": (ctypes.c_int, [P, ctypes.c_char_p]),
         "lulesh_adj_create": (ctypes.c_int, [P, dbl, i32, ctypes.POINTER(P)]),
         "lulesh_adj_destroy": (ctypes.c_int, [P]),
         "lulesh_adj_set_seed": (ctypes.c_int, [P, i32, P, i64]),
@@ -315,6 +317,15 @@ class Domain:
         t = Tuning()
         _check(self._L.lulesh_autotune(self._h, int(cycles), ctypes.byref(t)), "autotune")
         return t.as_dict()
+
+    def save_state(self, path):
+        """Write the step state (state fields and Domain scalars) to `path`."""
+        _check(self._L.lulesh_save_state(self._h, os.fsencode(path)), f"save state to {path}")
+
+    def load_state(self, path):
+        """Load a state file written for the same problem; the run then
+        continues as the saved one would have."""
+        _check(self._L.lulesh_load_state(self._h, os.fsencode(path)), f"load state from {path}")
 
     def __getattr__(self, name):
         if name in FIELDS:
@@ -579,3 +590,36 @@ class Adjoint:
         _check(self._L.lulesh_adj_get_gradient(self._h, fid, out.ctypes.data_as(ctypes.c_void_p), n),
                f"gradient {name}")
         return out
+
+
+def read_state(path):
+    """Host-side reader of a lulesh_save_state file (no GPU needed): a dict
+    with the problem header, the Domain scalars by name and the state fields
+    as numpy arrays. Checks the magic and the trailing FNV-1a hash."""
+    with open(path, "rb") as f:
+        raw = f.read()
+    if raw[:8] != b"LULESHS1":
+        raise ValueError(f"{path}: not a LULESH state file")
+    body, (stored,) = raw[8:-8], np.frombuffer(raw[-8:], dtype="<u8")
+    h = 1469598103934665603
+    for b in body:
+        h = ((h ^ b) * 1099511628211) & 0xFFFFFFFFFFFFFFFF
+    if h != int(stored):
+        raise ValueError(f"{path}: hash mismatch")
+    head = np.frombuffer(body, dtype="<i4", count=6)
+    sizes = np.frombuffer(body, dtype="<i8", count=2, offset=24)
+    ns, nf = np.frombuffer(body, dtype="<i4", count=2, offset=40)
+    off = 48
+    sc = np.frombuffer(body, dtype="<f8", count=int(ns), offset=off)
+    off += 8 * int(ns)
+    names = {v[0]: k for k, v in FIELDS.items()}
+    fields = {}
+    for _ in range(int(nf)):
+        fid = int(np.frombuffer(body, dtype="<i4", count=1, offset=off)[0])
+        n = int(np.frombuffer(body, dtype="<i8", count=1, offset=off + 4)[0])
+        fields[names[fid]] = np.frombuffer(body, dtype="<f8", count=n, offset=off + 12).copy()
+        off += 12 + 8 * n
+    inv = {i: k for k, i in SCALARS.items()}
+    return {"version": int(head[0]), "nx": int(head[1]), "nr": int(head[2]), "balance": int(head[3]),
+            "cost": int(head[4]), "mode": int(head[5]), "numElem": int(sizes[0]), "numNode": int(sizes[1]),
+            "scalars": {inv[i]: float(v) for i, v in enumerate(sc)}, "fields": fields}
