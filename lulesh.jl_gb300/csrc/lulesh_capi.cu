@@ -57,6 +57,7 @@ Params lulesh::make_params(const lulesh_domain* d) {
   p.emin = d->sc[LULESH_S_EMIN];
   p.dvovmax = d->sc[LULESH_S_DVOVMAX];
   p.refdens = d->sc[LULESH_S_REFDENS];
+  p.inv_refdens = 1.0 / p.refdens;
   p.dtfixed = d->sc[LULESH_S_DTFIXED];
   p.deltatimemultlb = d->sc[LULESH_S_DELTATIMEMULTLB];
   p.deltatimemultub = d->sc[LULESH_S_DELTATIMEMULTUB];

@@ -62,6 +62,7 @@ struct Params {
   double u_cut, hgcoef, qstop, monoq_max_slope, monoq_limiter_mult, e_cut, p_cut, q_cut, v_cut;
   double qlc_monoq, qqc_monoq, qqc, eosvmax, eosvmin, pmin, emin, dvovmax, refdens;
   double dtfixed, deltatimemultlb, deltatimemultub, stoptime, dtmax;
+  double inv_refdens;  // 1 / refdens, formed once on the host
 };
 
 // Device-resident step state. acc_* are running minima (bit patterns of

@@ -626,6 +626,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     const double vdov = LDG(&d.vdov[i]);
     const double vnew = LDG(&d.vnew[i]);
+    const double inv_vnew = 1.0 / vnew;
     const double volo = LDG(&d.volo[i]);
     double qlin, qquad;
     if (gt_zero(vdov)) {
@@ -643,7 +644,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       if (gt_zero(dxxi)) { dxxi = 0.0; if (TAPE) fl |= TF_DXCLAMP0; }
       if (gt_zero(dxeta)) { dxeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 1; }
       if (gt_zero(dxzeta)) { dxzeta = 0.0; if (TAPE) fl |= TF_DXCLAMP0 << 2; }
-      const double rho = LDG(&d.elemMass[i]) / (volo * vnew);
+      // rho = elemMass / (volo vnew), from the reciprocals of volo and vnew
+      const double rho = (LDG(&d.elemMass[i]) * LDG(&d.inv_volo[i])) * inv_vnew;
       const double s1sum = fma(dxxi, 1.0 - phixi, fma(dxeta, 1.0 - phieta, dxzeta * (1.0 - phizeta)));
       const double s2sum = fma(dxxi * dxxi, fma(-phixi, phixi, 1.0),
                                fma(dxeta * dxeta, fma(-phieta, phieta, 1.0), (dxzeta * dxzeta) * fma(-phizeta, phizeta, 1.0)));
@@ -680,7 +682,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const double e_old_in = d.e[i];
     const double p_old_in = d.p[i];
     const double c1s = 2.0 / 3.0;
-    const double inv_rho0 = 1.0 / prm.refdens;
+    const double inv_rho0 = prm.inv_refdens;
     double e_out = 0.0, p_out = 0.0, vv_out = 0.0;
     bool compress_out = false;
     // TINY-guarded sound-speed square root (src/domain.jl:2655-2659, 2738-2742)
@@ -692,7 +694,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     for (int rep = 0; rep < reps; ++rep) {
     double delvc = delvc_in, e_old = e_old_in, p_old = p_old_in, q_old = q_old_in, vnewc = vnewc_in;
     if (REGION) { opaque(delvc); opaque(e_old); opaque(p_old); opaque(q_old); opaque(vnewc); }
-    double compression = 1.0 / vnewc - 1.0;
+    // 1/vnewc is 1/vnew unless vnewc was clamped (the rep passes form it anew)
+    double compression = ((REGION || vnewc_in != vnew) ? 1.0 / vnewc : inv_vnew) - 1.0;
     const double vchalf = fma(delvc, -0.5, vnewc);
     double compHalfStep = 1.0 / vchalf - 1.0;
     if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) { compHalfStep = compression; if (TAPE) fl |= TF_HALF_EQ_COMP; }
