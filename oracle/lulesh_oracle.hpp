@@ -1,6 +1,6 @@
 // LULESH oracle: a CPU restatement of JuliaLabs/LULESH.jl's single-rank
 // Sedov setup and LagrangeLeapFrog timestep, used ONLY as test infrastructure
-// (parity checker, CPU baseline timing, golden-fixture generator). The product
+// (parity reference, CPU baseline timing, golden-fixture generator). The product
 // library never links, loads or calls anything in this directory.
 //
 // Parity status: UNPINNED against the Julia reference itself. The reference

@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle (test infrastructure only).
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg use
-this module, as the checker or the timed CPU baseline. The oracle restates
+this module, as the parity reference or the timed CPU baseline. The oracle restates
 LULESH.jl's Domain setup and LagrangeLeapFrog step (see lulesh_oracle.hpp).
 """
 import ctypes

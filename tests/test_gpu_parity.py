@@ -1,6 +1,6 @@
 """GPU parity of liblulesh_gb300 against the CPU oracle (through the C ABI).
 
-Tolerances (the benchmark spec's FP64 bar): the same cycle count and final time
+Tolerances (the FP64 parity bar): the same cycle count and final time
 (relative 1e-12), origin energy to relative 1e-9 and every field to a maximum
 relative error of 1e-8, with the field's cut-off (or 1e-12 of its largest
 magnitude) as the floor of the denominator. Integer and setup fields must be
