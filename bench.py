@@ -139,14 +139,15 @@ def barrier(world):
         dist.barrier()
 
 
-def cpu_oracle_rate(nx, seconds, threads=0, min_cycles=2, warm=1):
-    """Oracle (reference restatement) zones*cycles/s over a time-bounded sample."""
+def cpu_oracle_rate(nx, seconds, threads=0, min_cycles=2, warm=1, serial=False):
+    """Oracle (reference restatement) zones*cycles/s over a time-bounded sample;
+    `serial` times the single-threaded build (the reference is single-threaded)."""
     import oracle
-    L = oracle.load(openmp=True)
-    if threads:
+    L = oracle.load(openmp=not serial)
+    if threads and not serial:
         L.ora_set_threads(threads)
-    used = L.ora_max_threads()
-    d = oracle.OracleDomain(nx, nr=11)
+    used = 1 if serial else L.ora_max_threads()
+    d = oracle.OracleDomain(nx, nr=11, openmp=not serial)
     for _ in range(warm):
         d.time_increment()
         d.lagrange_leapfrog()
@@ -470,8 +471,11 @@ def run_ours(args):
     cpu = None
     if world == 1 and not args.no_cpu:
         rate, used, n, dt = cpu_oracle_rate(args.nx, args.cpu_seconds)
+        rate1, _, n1, dt1 = cpu_oracle_rate(args.nx, args.cpu_seconds / 2, serial=True)
         cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
-               "sample": f"{n} cycles of the {args.nx}^3 problem in {dt:.1f} s (oracle, OpenMP)"}
+               "sample": f"{n} cycles of the {args.nx}^3 problem in {dt:.1f} s (oracle, OpenMP)",
+               "single_thread": {"value": rate1, "cores": 1,
+                                 "sample": f"{n1} cycles in {dt1:.1f} s (oracle, serial build)"}}
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": cycles,
             "warmup": args.warmup, "ms_per_step": ms_max / cycles, "higher_is_better": True,
