@@ -318,6 +318,29 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
         an = float(np.dot(ge, de)) + ghg * dhg
         errs.append(abs(an - fd) / max(abs(fd), 1e-12 * abs(loss)))
     adj.close()
+    # the same gradient with the whole run taped in HBM (no recompute): one
+    # segment of `cycles` cycles, about 8 * (238 E + 3 N) bytes per cycle
+    tape_gb = 8.0 * (238 * g.numElem + 3 * g.numNode) * cycles / 1e9
+    full = None
+    try:
+        adj2 = L.Adjoint(g, radius=0.3, checkpoint_every=cycles)
+    except L.LuleshError as exc:
+        full = {"skipped": str(exc), "tape_gb": tape_gb}
+    if full is None:
+        restore()
+        adj2.gradient(cycles)  # warm-up
+        times2 = []
+        for _ in range(2):
+            restore()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            adj2.gradient(cycles)
+            torch.cuda.synchronize(dev)
+            times2.append(time.perf_counter() - t0)
+        same = bool(np.array_equal(adj2.grad("e"), ge)) and adj2.result.grad_hgcoef == ghg
+        full = {"checkpoint_every": cycles, "tape_gb": tape_gb, "adjoint_s": min(times2),
+                "adjoint_over_forward": min(times2) / fwd_s, "gradient_bitwise_equal": same}
+        adj2.close()
     g.close()
     return {"config": f"Sedov {nx}^3, {cycles} cycles, energy within r < 0.3, d/d(e0, hgcoef), "
                       f"checkpoints every {every} cycles, FP64",
@@ -326,7 +349,8 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
             "adjoint_sweep_ms": {"checkpointed_forward": res.forward_ms, "reverse": res.reverse_ms},
             "loss": loss, "grad_hgcoef": ghg, "grad_e_origin": float(ge[0]),
             "fd": {"directions": dirs, "step": h, "max_rel_err": max(errs),
-                   "median_rel_err": float(np.median(errs))}}
+                   "median_rel_err": float(np.median(errs))},
+            "whole_run_taped": full}
 
 
 def c3_leg(L, torch, dev, nx, cycles, warmup=2):
