@@ -486,9 +486,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
 
 // One limiter direction, src/domain.jl:2330-2376. `src` reports which value
 // the result is (PHI_*), for the adjoint's tape.
-__device__ __forceinline__ double monoq_phi(double self, double dm, double dp, const Params& prm, int& src,
+__device__ __forceinline__ double monoq_phi(double norm, double dm, double dp, const Params& prm, int& src,
                                             double& t_norm, double& t_dm, double& t_dp) {
-  const double norm = 1.0 / (self + 1.e-36);
+  // norm = 1 / (delv + ptiny) of this direction
   dm *= norm;
   dp *= norm;
   t_norm = norm; t_dm = dm; t_dp = dp;  // kept for the adjoint's tape
@@ -608,13 +608,24 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
     double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
     double tl[9];  // limiter terms per direction: norm, dm/norm, dp/norm (TAPE)
-    const double phixi = monoq_phi(dvxi, dm, dp, prm, src0, tl[0], tl[3], tl[6]);
+    // the three 1/(delv + ptiny) from one division: r = 1/(sx sy sz)
+    double inx, iny, inz;
+    {
+      const double sx = dvxi + 1.e-36, sy = dveta + 1.e-36, sz = dvzeta + 1.e-36;
+      const double sxy = sx * sy;
+      const double r = 1.0 / (sxy * sz);
+      const double rz = r * sz;  // 1/(sx sy)
+      inz = r * sxy;
+      inx = rz * sy;
+      iny = rz * sx;
+    }
+    const double phixi = monoq_phi(inx, dm, dp, prm, src0, tl[0], tl[3], tl[6]);
     dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);
-    const double phieta = monoq_phi(dveta, dm, dp, prm, src1, tl[1], tl[4], tl[7]);
+    const double phieta = monoq_phi(iny, dm, dp, prm, src1, tl[1], tl[4], tl[7]);
     dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, E, bad);
-    const double phizeta = monoq_phi(dvzeta, dm, dp, prm, src2, tl[2], tl[5], tl[8]);
+    const double phizeta = monoq_phi(inz, dm, dp, prm, src2, tl[2], tl[5], tl[8]);
     if (bad) err |= ST_BAD_BC;
     // d.tapeMat slot q of this element (TAPE only)
     auto tm = [&](int q, double v) { if (TAPE) d.tapeMat[q * E + i] = v; };
@@ -718,7 +729,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
     const double bvc_half = c1s * (compHalfStep + 1.0);
     const double pHalfStep = pressure(e_new, bvc_half, TF_PH_CUT, TF_PH_MIN);
-    const double vhalf = 1.0 / (1.0 + compHalfStep);
+    // vhalf = 1 / (1 + compHalfStep): vchalf, vnewc or 1 by the branch taken
+    const double vhalf = (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) ? 1.0
+                       : (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) ? vnewc : vchalf;
     const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
     if (TAPE && compress) fl |= TF_COMPRESS;
     tm(14, compression); tm(15, compHalfStep); tm(16, e_new); tm(17, pHalfStep); tm(18, vhalf);
