@@ -401,6 +401,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
       d.tapeKin[(9 + a) * E + e] = vxw[a]; d.tapeKin[(12 + a) * E + e] = vyw[a]; d.tapeKin[(15 + a) * E + e] = vzw[a];
     }
   }
+  // 1/det of the velocity gradient and 1/(64 vol + 64 ptiny) of the Q
+  // gradients come from one division
+  const double volq = LDG(&d.volo[e]) * vnew;
+  const double q64 = fma(64.0, volq, 64.0 * 1.e-36);
+  double inv, norm64;
   {
     const double dt2 = -0.5 * dt;
     double F[3][3];  // F[k][a]: coordinate k, direction a (xi, eta, zeta)
@@ -424,7 +429,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     const double d1 = fma(Cxxi, vxw[0], fma(Cxet, vxw[1], Cxze * vxw[2]));
     const double d2 = fma(Cyxi, vyw[0], fma(Cyet, vyw[1], Cyze * vyw[2]));
     const double d3 = fma(Czxi, vzw[0], fma(Czet, vzw[1], Czze * vzw[2]));
-    const double inv = 1.0 / det;
+    {
+      const double r = 1.0 / (det * q64);
+      inv = r * q64;
+      norm64 = r * det;
+    }
     const double vdov = ((d1 + d2) + d3) * inv;
     d.vdov[e] = vdov;
     if (TAPE) {
@@ -447,8 +456,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
   // delv = norm/64 * (A . W(v)) for the cross product A of two Walsh vectors.
   {
     const double ptiny = 1.e-36;
-    const double vol = LDG(&d.volo[e]) * vnew;
-    const double norm64 = 1.0 / fma(64.0, vol, 64.0 * ptiny);
+    const double vol = volq;
     const double vol16 = 16.0 * vol;
     double ax, ay, az, rs;
     // taped per direction d (xi, eta, zeta): the cross product A and 1/|A|
