@@ -159,12 +159,12 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
   const bool vmin_c = (fl & TF_VNEW_MIN) != 0, vmax_c = (fl & TF_VNEW_MAX) != 0;
   const double vnewc = vmin_c ? prm.eosvmin : vmax_c ? prm.eosvmax : vnew;
   const bool vmax_hit = (fl & TF_VMAX_HIT) != 0, half_eq = (fl & TF_HALF_EQ_COMP) != 0;
-  const double compression = tm(14), chs = tm(15);
-  // 1/vnewc = compression + 1 and 1/vchalf = compHalfStep + 1 on the branches
-  // where the forward formed them
-  const double inv_vnewc = vmax_hit ? 1.0 / vnewc : compression + 1.0;
+  // bv = 1 + compression and bvh = 1 + compHalfStep as the forward formed
+  // them: 1/vnewc and 1/vchalf on the branches where they are reciprocals
+  const double bv = tm(14), bvh = tm(15);
+  const double inv_vnewc = vmax_hit ? 1.0 / vnewc : bv;
   const double inv_vnew = (vnewc == vnew) ? inv_vnewc : 1.0 / vnew;
-  const double inv_vchalf = (vmax_hit || half_eq) ? 0.0 : chs + 1.0;
+  const double inv_vchalf = (vmax_hit || half_eq) ? 0.0 : bvh;
   const bool qzero = (fl & TF_QZERO) != 0;
   double dx[3] = {0.0, 0.0, 0.0};
   const double rho = tm(9), qlin = tm(10), qquad = tm(11), s1sum = tm(12), s2sum = tm(13);
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
   const double pq = p_old + q_old;
   const bool e1min = (fl & TF_E1_MIN) != 0;
   const double e1 = tm(16), pH = tm(17), vhalf = tm(18);
-  const double bvc_h = c1s * (chs + 1.0);
+  const double bvc_h = c1s * bvh;
   const bool pH_on = !vmax_hit && !(fl & (TF_PH_CUT | TF_PH_MIN));
   const bool comp = (fl & TF_COMPRESS) != 0;
   const bool s1t = (fl & TF_S1_TINY) != 0, s2t = (fl & TF_S2_TINY) != 0, sst = (fl & TF_SS_TINY) != 0;
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, d
   const bool e2fix = (fl & (TF_E2_CUT | TF_E2_MIN)) != 0;
   const double k2 = fma(3.0, pq, -4.0 * (pH + qn1));
   const double e2 = tm(21), pn1 = tm(22);
-  const double bvc = c1s * (compression + 1.0);
+  const double bvc = c1s * bv;
   const bool pn1_on = !vmax_hit && !(fl & (TF_PN1_CUT | TF_PN1_MIN));
   const double vv_bvc = (vnewc * vnewc) * bvc;
   const double s2 = tm(23), qt = tm(24);
@@ -673,7 +673,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
       const double inv_det = 1.0 / determ;
       const double vi12 = inv_det * (1.0 / 12.0);
       const double ss = a.ss0[e], mass = a.elemMass[e];
-      const double r = rcbrt(determ);
+      const double r = inv_cbrt(determ);
       const double c0 = -hgcoef * 0.01;
       const double coef = ((c0 * ss) * mass) * r;
       // S_k (taped), D[k][j] = V_k . dv_j and T_k, C[k][j] = lf_k . dv_j

@@ -18,7 +18,11 @@
 //    the 36 edge sums are formed once per element;
 //  * the velocity-gradient trace (src/domain.jl:2023-2081, 2156-2158) is
 //    trace(C^T W(v)) / det, with C the cofactors of the Jacobian and W(v) the
-//    Walsh coefficients of the velocities.
+//    Walsh coefficients of the velocities;
+//  * reciprocals of one element share a division (recip3), square roots are
+//    x * rsqrt(x), and the hourglass coefficient's 1/cbrt is a float seed
+//    with one Householder step (inv_cbrt): a division costs about 5 FP64
+//    instructions, sqrt about 9 and the library rcbrt about 18.
 // Products are contracted into FMAs.
 #pragma once
 
@@ -99,6 +103,34 @@ __device__ __forceinline__ bool gt_zero(double a) {  // a > 0.0
 __device__ __forceinline__ bool abs_lt(double a, double c) {  // |a| < c for c >= 0
   return (unsigned long long)(__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) <
          (unsigned long long)__double_as_longlong(c);
+}
+
+// x^(-1/3) for x > 0 in six FP64 instructions: a single-precision seed y0
+// refined by one second-order Householder step. With e = 1 - x y0^3 the
+// exact value is y0 (1 - e)^(-1/3) = y0 (1 + e/3 + 2e^2/9 + 14e^3/81 + ...);
+// the seed's |e| is below 2^-21, so the dropped terms are below 2^-64 and the
+// result is within about one ulp (y0^2 is exact, y0^3 and 1 - x y0^3 are
+// rounded once). Outside [1e-30, 1e30] (beyond the seed's float range) the
+// library rcbrt is used; the range test runs on the integer pipe.
+__device__ __forceinline__ double inv_cbrt(double x) {
+  const long long b = __double_as_longlong(x);
+  if (b < 0x39B4484BFEEBC2A0ll || b > 0x46293E5939A08CEAll) return rcbrt(x);  // 1e-30, 1e30
+  const double y0 = (double)rcbrtf((float)x);
+  const double y2 = y0 * y0;
+  const double e = fma(-x, y2 * y0, 1.0);
+  return fma(y0, e * fma(e, 2.0 / 9.0, 1.0 / 3.0), y0);
+}
+
+// 1/a, 1/b, 1/c from one division: r = 1/(a b c), 1/c = r (a b),
+// 1/a = (r c) b, 1/b = (r c) a. For a, b, c > 0 whose product is a normal
+// double; each result is within a few ulps of the quotient.
+__device__ __forceinline__ void recip3(double a, double b, double c, double& ia, double& ib, double& ic) {
+  const double ab = a * b;
+  const double r = 1.0 / (ab * c);
+  const double rc = r * c;
+  ic = r * ab;
+  ia = rc * b;
+  ib = rc * a;
 }
 
 // timeIncrement!, src/domain.jl:920-961, shared by the host API and the

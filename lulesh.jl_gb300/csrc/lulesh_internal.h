@@ -136,8 +136,8 @@ struct DevDomain {
   double* tapeKin;
   // [31][E]: the material kernel's limiter terms (norm, scaled neighbours:
   // 9), Q terms (rho, qlin, qquad, and their two sums: 5) and EOS values
-  // (compression, compHalfStep, e1, pHalf, vhalf, s1, q1, e2, p1, s2, q2, e3,
-  // p2, ss: 14; the three squared sound speeds: 3)
+  // (1 + compression, 1 + compHalfStep, e1, pHalf, vhalf, s1, q1, e2, p1, s2,
+  // q2, e3, p2, ss: 14; the three squared sound speeds: 3)
   double* tapeMat;
 };
 

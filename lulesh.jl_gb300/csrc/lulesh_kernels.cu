@@ -86,8 +86,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     }
   }
 
+  // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
+  const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
+
   // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
-  // face-diagonal cross products; true B = -Bc/8.
+  // face-diagonal cross products; true B = -Bc/8. The face normals are scaled
+  // by s8 here, so Bx..Bz hold the stress forces s8*Bc.
   double Bx[8], By[8], Bz[8];
   {
     double nx[6], ny[6], nz[6];
@@ -101,6 +105,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
         d.tapeGeo[(54 + f) * E + e] = ny[f];
         d.tapeGeo[(60 + f) * E + e] = nz[f];
       }
+      nx[f] *= s8; ny[f] *= s8; nz[f] *= s8;
     }
     // node -> its three faces (faces numbered 0..5 = reference faces 1..6)
     Bx[0] = (nx[0] + nx[1]) + nx[4]; By[0] = (ny[0] + ny[1]) + ny[4]; Bz[0] = (nz[0] + nz[1]) + nz[4];
@@ -172,9 +177,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   const double determ = LDG(&d.volo[e]) * v;
   if (le_zero(v)) atomicOr(&st->status, ST_HOURGLASS);
 
-  // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
-  const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
-
   double fx[8], fy[8], fz[8];
   if (hgcoef > 0.0) {
     // hourgam (src/domain.jl:1527-1549) with volinv/12 folded into the modes
@@ -203,7 +205,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
         hg[n][m] = fma(-dvz[n], hmz[m], fma(-dvy[n], hmy[m], fma(-dvx[n], hmx[m], gamma_nm(n, m))));
 
     // coefficient = -hgcoef*0.01*ss*mass/cbrt(determ) (src/domain.jl:1605)
-    const double coef = ((-hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * rcbrt(determ);
+    const double coef = ((-hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * inv_cbrt(determ);
 
     // calcElemFBHourglassForce (src/domain.jl:1258-1460), one velocity
     // component at a time to bound register use.
@@ -226,13 +228,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
       }
 #pragma unroll
       for (int n = 0; n < 8; ++n) {
-        const double hgf = fma(hg[n][0], h[0], fma(hg[n][1], h[1], fma(hg[n][2], h[2], hg[n][3] * h[3])));
-        fo[k][n] = fma(s8, Bc[k][n], hgf);
+        fo[k][n] = fma(hg[n][0], h[0], fma(hg[n][1], h[1], fma(hg[n][2], h[2], fma(hg[n][3], h[3], Bc[k][n]))));
       }
     }
   } else {
 #pragma unroll
-    for (int n = 0; n < 8; ++n) { fx[n] = s8 * Bx[n]; fy[n] = s8 * By[n]; fz[n] = s8 * Bz[n]; }
+    for (int n = 0; n < 8; ++n) { fx[n] = Bx[n]; fy[n] = By[n]; fz[n] = Bz[n]; }
   }
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
@@ -645,8 +646,18 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     const double vdov = LDG(&d.vdov[i]);
     const double vnew = LDG(&d.vnew[i]);
-    const double inv_vnew = 1.0 / vnew;
-    const double volo = LDG(&d.volo[i]);
+    const double delvc_in = LDG(&d.delv[i]);
+
+    // ---- applyMaterialPropertiesForElems' clamp, src/domain.jl:2860-2910 ----
+    double vnewc_in = vnew;
+    if (prm.eosvmin != 0.0 && vnewc_in < prm.eosvmin) { vnewc_in = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
+    if (prm.eosvmax != 0.0 && vnewc_in > prm.eosvmax) { vnewc_in = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
+    // 1/vnewc, 1/vchalf (vchalf = vnewc - delvc/2 > 0) and the hydro
+    // constraint's 1/(|vdov| + 1e-20) from one division
+    const double w_hydro = fabs(vdov) + 1.e-20;
+    double inv_vnewc_in, inv_vchalf_in, inv_w;
+    recip3(vnewc_in, fma(delvc_in, -0.5, vnewc_in), w_hydro, inv_vnewc_in, inv_vchalf_in, inv_w);
+    const double inv_vnew = (vnewc_in == vnew) ? inv_vnewc_in : 1.0 / vnew;
     double qlin, qquad;
     if (gt_zero(vdov)) {
       qlin = 0.0;
@@ -678,10 +689,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const double q_old_in = d.q[i];
     if (q_old_in > prm.qstop) err |= ST_QSTOP;
 
-    // ---- applyMaterialPropertiesForElems, src/domain.jl:2860-2910 ----
-    double vnewc_in = vnew;
-    if (prm.eosvmin != 0.0 && vnewc_in < prm.eosvmin) { vnewc_in = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
-    if (prm.eosvmax != 0.0 && vnewc_in > prm.eosvmax) { vnewc_in = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
+    // ---- applyMaterialPropertiesForElems' volume check ----
     {
       double vc = LDG(&d.v[i]);
       if (prm.eosvmin != 0.0 && vc < prm.eosvmin) vc = prm.eosvmin;
@@ -697,7 +705,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     // through an opaque register move each time so no evaluation is folded
     // away, and the last one is kept. Results do not depend on reps.
     const int reps = REGION ? LDG(&d.posReps[t]) : 1;
-    const double delvc_in = LDG(&d.delv[i]);
     const double e_old_in = d.e[i];
     const double p_old_in = d.p[i];
     const double c1s = 2.0 / 3.0;
@@ -707,19 +714,23 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     // TINY-guarded sound-speed square root (src/domain.jl:2655-2659, 2738-2742)
     auto tiny_sqrt = [&](double ssc, unsigned long long bit) -> double {
       if (ssc <= 0.111111e-36) { if (TAPE) fl |= bit; return 0.333333e-18; }
-      return sqrt(ssc);
+      return ssc * rsqrt(ssc);
     };
 #pragma unroll 1
     for (int rep = 0; rep < reps; ++rep) {
     double delvc = delvc_in, e_old = e_old_in, p_old = p_old_in, q_old = q_old_in, vnewc = vnewc_in;
     if (REGION) { opaque(delvc); opaque(e_old); opaque(p_old); opaque(q_old); opaque(vnewc); }
-    // 1/vnewc is 1/vnew unless vnewc was clamped (the rep passes form it anew)
-    double compression = ((REGION || vnewc_in != vnew) ? 1.0 / vnewc : inv_vnew) - 1.0;
     const double vchalf = fma(delvc, -0.5, vnewc);
-    double compHalfStep = 1.0 / vchalf - 1.0;
-    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) { compHalfStep = compression; if (TAPE) fl |= TF_HALF_EQ_COMP; }
+    // the rep passes form the reciprocals anew from their opaque inputs
+    double inv_vnewc = inv_vnewc_in, inv_vchalf = inv_vchalf_in;
+    if (REGION) { double iw; recip3(vnewc, vchalf, w_hydro, inv_vnewc, inv_vchalf, iw); }
+    // compression = 1/vnewc - 1 and compHalfStep = 1/vchalf - 1 enter only as
+    // bvc = c1s (1 + compression) and bvc_half = c1s (1 + compHalfStep):
+    // bv and bvh are those factors over c1s for the branch taken
+    double bv = inv_vnewc, bvh = inv_vchalf;
+    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) { bvh = bv; if (TAPE) fl |= TF_HALF_EQ_COMP; }
     if (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) {
-      p_old = 0.0; compression = 0.0; compHalfStep = 0.0;
+      p_old = 0.0; bv = 1.0; bvh = 1.0;
       if (TAPE) fl |= TF_VMAX_HIT;
     }
     const bool vmax_hit = vnewc >= prm.eosvmax;
@@ -735,14 +746,14 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const double pq_old = p_old + q_old;
     double e_new = fma(-0.5 * delvc, pq_old, e_old);
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
-    const double bvc_half = c1s * (compHalfStep + 1.0);
+    const double bvc_half = c1s * bvh;
     const double pHalfStep = pressure(e_new, bvc_half, TF_PH_CUT, TF_PH_MIN);
     // vhalf = 1 / (1 + compHalfStep): vchalf, vnewc or 1 by the branch taken
     const double vhalf = (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) ? 1.0
                        : (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) ? vnewc : vchalf;
     const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
     if (TAPE && compress) fl |= TF_COMPRESS;
-    tm(14, compression); tm(15, compHalfStep); tm(16, e_new); tm(17, pHalfStep); tm(18, vhalf);
+    tm(14, bv); tm(15, bvh); tm(16, e_new); tm(17, pHalfStep); tm(18, vhalf);
     double q_new = 0.0;
     if (compress) {
       const double ssc = fma(c1s, e_new, ((vhalf * vhalf) * bvc_half) * pHalfStep) * inv_rho0;
@@ -756,7 +767,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E2_CUT; }
     if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
-    const double bvc = c1s * (compression + 1.0);
+    const double bvc = c1s * bv;
     double p_new = pressure(e_new, bvc, TF_PN1_CUT, TF_PN1_MIN);
     const double vv_bvc = (vnewc * vnewc) * bvc;
     tm(21, e_new); tm(22, p_new);
@@ -805,7 +816,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       double dtf = ss_new * ss_new;
       if (vdov < 0.0) dtf = fma(((64.0 * prm.qqc) * prm.qqc) * (arealg * arealg), vdov * vdov, dtf);
       dtc = arealg * rsqrt(dtf);
-      dth = prm.dvovmax / (fabs(vdov) + 1.e-20);
+      dth = prm.dvovmax * inv_w;
       courant = (unsigned long long)__double_as_longlong(dtc);
       hydro = (unsigned long long)__double_as_longlong(dth);
     }
