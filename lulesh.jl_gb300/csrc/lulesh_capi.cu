@@ -57,12 +57,12 @@ Params lulesh::make_params(const lulesh_domain* d) {
   p.emin = d->sc[LULESH_S_EMIN];
   p.dvovmax = d->sc[LULESH_S_DVOVMAX];
   p.refdens = d->sc[LULESH_S_REFDENS];
-  p.inv_refdens = 1.0 / p.refdens;
   p.dtfixed = d->sc[LULESH_S_DTFIXED];
   p.deltatimemultlb = d->sc[LULESH_S_DELTATIMEMULTLB];
   p.deltatimemultub = d->sc[LULESH_S_DELTATIMEMULTUB];
   p.stoptime = d->sc[LULESH_S_STOPTIME];
   p.dtmax = d->sc[LULESH_S_DTMAX];
+  finish_params(p);
   return p;
 }
 

@@ -105,6 +105,21 @@ __device__ __forceinline__ bool abs_lt(double a, double c) {  // |a| < c for c >
          (unsigned long long)__double_as_longlong(c);
 }
 
+// Integer-pipe comparison key of a non-NaN double (fkey_bits): a < b exactly
+// when fkey(a) < fkey(b), -0 equal to +0. A DSETP takes an FP64 pipe slot;
+// the key and a 64-bit integer compare take a few integer instructions, of
+// which the FP64-bound kernels have plenty to spare.
+__device__ __forceinline__ long long fkey(double x) { return fkey_bits(__double_as_longlong(x)); }
+__device__ __forceinline__ bool lt_zero(double a) { return fkey(a) < 0; }  // a < 0.0
+__device__ __forceinline__ bool is_zero(double a) {                         // a == 0.0
+  return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFll) == 0;
+}
+// max of two non-negative doubles (+0 included) by their bit patterns
+__device__ __forceinline__ double max_nonneg(double a, double b) {
+  const long long x = __double_as_longlong(a), y = __double_as_longlong(b);
+  return __longlong_as_double(x > y ? x : y);
+}
+
 // x^(-1/3) for x > 0 in six FP64 instructions: a single-precision seed y0
 // refined by one second-order Householder step. With e = 1 - x y0^3 the
 // exact value is y0 (1 - e)^(-1/3) = y0 (1 + e/3 + 2e^2/9 + 14e^3/81 + ...);

@@ -51,7 +51,7 @@ Params reference_params() {
   p.eosvmax = 1.0e+9; p.eosvmin = 1.0e-9; p.pmin = 0.0; p.emin = -1.0e+15; p.dvovmax = 0.1;
   p.refdens = 1.0; p.dtfixed = -1.0e-6; p.deltatimemultlb = 1.1; p.deltatimemultub = 1.2;
   p.stoptime = 1.0e-2; p.dtmax = 1.0e-2;
-  p.inv_refdens = 1.0 / p.refdens;
+  finish_params(p);
   return p;
 }
 

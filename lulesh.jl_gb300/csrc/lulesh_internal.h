@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cstring>
 #include <cuda_runtime.h>
 
 namespace lulesh {
@@ -62,8 +63,39 @@ struct Params {
   double u_cut, hgcoef, qstop, monoq_max_slope, monoq_limiter_mult, e_cut, p_cut, q_cut, v_cut;
   double qlc_monoq, qqc_monoq, qqc, eosvmax, eosvmin, pmin, emin, dvovmax, refdens;
   double dtfixed, deltatimemultlb, deltatimemultub, stoptime, dtmax;
-  double inv_refdens;  // 1 / refdens, formed once on the host
+  // formed once on the host by finish_params: 1 / refdens, 64 qqc^2, the comparison
+  // keys (fkey) of the thresholds the element kernels test against, and
+  // whether eosvmin / eosvmax are set (nonzero)
+  double inv_refdens, qqc2x64;
+  long long k_qstop, k_max_slope, k_eosvmin, k_eosvmax, k_pmin, k_emin;
+  int has_eosvmin, has_eosvmax;
 };
+
+// Order-preserving integer key of a non-NaN double given its bit pattern:
+// a < b exactly when fkey(a) < fkey(b), and -0 and +0 share the key 0, as
+// IEEE comparison has them. Negative values map to minus their magnitude.
+__host__ __device__ inline long long fkey_bits(long long b) {
+  return b < 0 ? (long long)(0x8000000000000000ull - (unsigned long long)b) : b;
+}
+
+inline long long fkey_host(double x) {
+  long long b;
+  memcpy(&b, &x, sizeof b);
+  return fkey_bits(b);
+}
+
+inline void finish_params(Params& p) {
+  p.inv_refdens = 1.0 / p.refdens;
+  p.qqc2x64 = (64.0 * p.qqc) * p.qqc;
+  p.k_qstop = fkey_host(p.qstop);
+  p.k_max_slope = fkey_host(p.monoq_max_slope);
+  p.k_eosvmin = fkey_host(p.eosvmin);
+  p.k_eosvmax = fkey_host(p.eosvmax);
+  p.k_pmin = fkey_host(p.pmin);
+  p.k_emin = fkey_host(p.emin);
+  p.has_eosvmin = p.eosvmin != 0.0;
+  p.has_eosvmax = p.eosvmax != 0.0;
+}
 
 // Device-resident step state. acc_* are running minima (bit patterns of
 // non-negative doubles, so an unsigned min is the FP min) filled by the

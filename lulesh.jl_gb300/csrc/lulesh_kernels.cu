@@ -178,9 +178,11 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   if (le_zero(v)) atomicOr(&st->status, ST_HOURGLASS);
 
   double fx[8], fy[8], fz[8];
-  if (hgcoef > 0.0) {
+  if (gt_zero(hgcoef)) {
     // hourgam (src/domain.jl:1527-1549) with volinv/12 folded into the modes
-    const double vi12 = 1.0 / (12.0 * determ);
+    // determ^(-1/3) serves the coefficient, its cube the modes' 1/(12 determ)
+    const double rc = inv_cbrt(determ);
+    const double vi12 = (rc * rc) * (rc * (1.0 / 12.0));
 #pragma unroll
     for (int m = 0; m < 4; ++m) { hmx[m] *= vi12; hmy[m] *= vi12; hmz[m] *= vi12; }
     if (TAPE) {
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
         hg[n][m] = fma(-dvz[n], hmz[m], fma(-dvy[n], hmy[m], fma(-dvx[n], hmx[m], gamma_nm(n, m))));
 
     // coefficient = -hgcoef*0.01*ss*mass/cbrt(determ) (src/domain.jl:1605)
-    const double coef = ((-hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * inv_cbrt(determ);
+    const double coef = ((-hgcoef * 0.01) * LDG(&d.ss[e])) * LDG(&d.elemMass[e]) * rc;
 
     // calcElemFBHourglassForce (src/domain.jl:1258-1460), one velocity
     // component at a time to bound register use.
@@ -311,15 +313,23 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
   // calcElemVolume (src/utils.jl:36-116); its 12 differences are the face
   // diagonals that calcElemCharacteristicLength needs too.
   double volume, charLength = 0.0;
+  double wx[3], wy[3], wz[3];  // first-order Walsh vectors (xi, eta, zeta) of x, y, z
   {
     double d61[3], d70[3], d63[3], d20[3], d50[3], d64[3], d31[3], d72[3], d43[3], d57[3], d14[3], d25[3];
     const double* P[3] = {x, y, z};
+    double* W[3] = {wx, wy, wz};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
       const double* p = P[k];
       d61[k] = p[6] - p[1]; d70[k] = p[7] - p[0]; d63[k] = p[6] - p[3]; d20[k] = p[2] - p[0];
       d50[k] = p[5] - p[0]; d64[k] = p[6] - p[4]; d31[k] = p[3] - p[1]; d72[k] = p[7] - p[2];
       d43[k] = p[4] - p[3]; d57[k] = p[5] - p[7]; d14[k] = p[1] - p[4]; d25[k] = p[2] - p[5];
+      // the Walsh vectors from the face diagonals (9 adds instead of 11):
+      // xi = (d20 - d31) + (d64 + d57), eta = (d20 + d31) + (d64 - d57),
+      // zeta = (d50 - d14) + (d72 + d63)
+      W[k][0] = (d20[k] - d31[k]) + (d64[k] + d57[k]);
+      W[k][1] = (d20[k] + d31[k]) + (d64[k] - d57[k]);
+      W[k][2] = (d50[k] - d14[k]) + (d72[k] + d63[k]);
     }
     double gu[3][3];  // V x W of each triple product (kept for the tape)
     const double v12 =
@@ -350,12 +360,13 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     auto face = [&](const double* a, const double* b, int f) {
       double cx, cy, cz;
       cross(a[0], a[1], a[2], b[0], b[1], b[2], cx, cy, cz);
+      // area4 >= +0 and charLength too: their bit patterns order them
       const double area4 = fma(cx, cx, fma(cy, cy, cz * cz));
-      if (TAPE && (f == 0 || area4 > charLength)) {
+      if (TAPE && (f == 0 || __double_as_longlong(area4) > __double_as_longlong(charLength))) {
         fidx = f;
         fcx = cx; fcy = cy; fcz = cz;
       }
-      charLength = fmax(area4, charLength);
+      charLength = max_nonneg(area4, charLength);
     };
     face(d20, d31, 0);   // nodes 1,2,3,4
     face(d64, d57, 1);   // 5,6,7,8
@@ -380,8 +391,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
   }
 
   // Velocity gradient trace at the half-step position (src/domain.jl:2128-2158)
-  double wx[3], wy[3], wz[3];
-  walsh1(x, wx); walsh1(y, wy); walsh1(z, wz);
   double vxw[3], vyw[3], vzw[3];
   {
     double v8[8];
@@ -505,10 +514,13 @@ __device__ __forceinline__ double monoq_phi(double norm, double dm, double dp, c
   src = PHI_MEAN;
   dm *= prm.monoq_limiter_mult;
   dp *= prm.monoq_limiter_mult;
-  if (dm < phi) { phi = dm; src = PHI_M; }
-  if (dp < phi) { phi = dp; src = PHI_P; }
-  if (phi < 0.0) { phi = 0.0; src = PHI_ZERO; }
-  if (phi > prm.monoq_max_slope) { phi = prm.monoq_max_slope; src = PHI_MAX; }
+  // the comparisons on the integer keys (fkey), with IEEE's outcomes
+  long long kphi = fkey(phi);
+  const long long km = fkey(dm), kp = fkey(dp);
+  if (km < kphi) { phi = dm; kphi = km; src = PHI_M; }
+  if (kp < kphi) { phi = dp; kphi = kp; src = PHI_P; }
+  if (kphi < 0) { phi = 0.0; kphi = 0; src = PHI_ZERO; }
+  if (kphi > prm.k_max_slope) { phi = prm.monoq_max_slope; src = PHI_MAX; }
   return phi;
 }
 
@@ -649,15 +661,24 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     const double delvc_in = LDG(&d.delv[i]);
 
     // ---- applyMaterialPropertiesForElems' clamp, src/domain.jl:2860-2910 ----
+    // (the threshold tests of this kernel compare integer keys, fkey)
     double vnewc_in = vnew;
-    if (prm.eosvmin != 0.0 && vnewc_in < prm.eosvmin) { vnewc_in = prm.eosvmin; if (TAPE) fl |= TF_VNEW_MIN; }
-    if (prm.eosvmax != 0.0 && vnewc_in > prm.eosvmax) { vnewc_in = prm.eosvmax; if (TAPE) fl |= TF_VNEW_MAX; }
+    long long kvn = fkey(vnew);
+    bool clamped = false;
+    if (prm.has_eosvmin && kvn < prm.k_eosvmin) {
+      vnewc_in = prm.eosvmin; kvn = prm.k_eosvmin; clamped = true;
+      if (TAPE) fl |= TF_VNEW_MIN;
+    }
+    if (prm.has_eosvmax && kvn > prm.k_eosvmax) {
+      vnewc_in = prm.eosvmax; clamped = true;
+      if (TAPE) fl |= TF_VNEW_MAX;
+    }
     // 1/vnewc, 1/vchalf (vchalf = vnewc - delvc/2 > 0) and the hydro
     // constraint's 1/(|vdov| + 1e-20) from one division
     const double w_hydro = fabs(vdov) + 1.e-20;
     double inv_vnewc_in, inv_vchalf_in, inv_w;
     recip3(vnewc_in, fma(delvc_in, -0.5, vnewc_in), w_hydro, inv_vnewc_in, inv_vchalf_in, inv_w);
-    const double inv_vnew = (vnewc_in == vnew) ? inv_vnewc_in : 1.0 / vnew;
+    const double inv_vnew = clamped ? 1.0 / vnew : inv_vnewc_in;
     double qlin, qquad;
     if (gt_zero(vdov)) {
       qlin = 0.0;
@@ -687,13 +708,14 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     // ---- qstop check on the old q, src/domain.jl:2567-2582 ----
     const double q_old_in = d.q[i];
-    if (q_old_in > prm.qstop) err |= ST_QSTOP;
+    if (fkey(q_old_in) > prm.k_qstop) err |= ST_QSTOP;
 
     // ---- applyMaterialPropertiesForElems' volume check ----
     {
       double vc = LDG(&d.v[i]);
-      if (prm.eosvmin != 0.0 && vc < prm.eosvmin) vc = prm.eosvmin;
-      if (prm.eosvmax != 0.0 && vc > prm.eosvmax) vc = prm.eosvmax;
+      long long kvc = fkey(vc);
+      if (prm.has_eosvmin && kvc < prm.k_eosvmin) { vc = prm.eosvmin; kvc = prm.k_eosvmin; }
+      if (prm.has_eosvmax && kvc > prm.k_eosvmax) vc = prm.eosvmax;
       if (le_zero(vc)) err |= ST_MATERIAL;
     }
 
@@ -713,7 +735,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     bool compress_out = false;
     // TINY-guarded sound-speed square root (src/domain.jl:2655-2659, 2738-2742)
     auto tiny_sqrt = [&](double ssc, unsigned long long bit) -> double {
-      if (ssc <= 0.111111e-36) { if (TAPE) fl |= bit; return 0.333333e-18; }
+      // ssc <= 0.111111e-36 (a positive threshold: the signed bit patterns order)
+      if (__double_as_longlong(ssc) <= 0x3842E7910CC4BCABll) { if (TAPE) fl |= bit; return 0.333333e-18; }
       return ssc * rsqrt(ssc);
     };
 #pragma unroll 1
@@ -727,30 +750,32 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     // compression = 1/vnewc - 1 and compHalfStep = 1/vchalf - 1 enter only as
     // bvc = c1s (1 + compression) and bvc_half = c1s (1 + compHalfStep):
     // bv and bvh are those factors over c1s for the branch taken
+    const long long kv = fkey(vnewc);
+    const bool at_vmin = prm.has_eosvmin && kv <= prm.k_eosvmin;  // eosvmin != 0 && vnewc <= eosvmin
+    const bool vmax_hit = kv >= prm.k_eosvmax;                     // vnewc >= eosvmax
+    const bool at_vmax = prm.has_eosvmax && vmax_hit;
     double bv = inv_vnewc, bvh = inv_vchalf;
-    if (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) { bvh = bv; if (TAPE) fl |= TF_HALF_EQ_COMP; }
-    if (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) {
+    if (at_vmin) { bvh = bv; if (TAPE) fl |= TF_HALF_EQ_COMP; }
+    if (at_vmax) {
       p_old = 0.0; bv = 1.0; bvh = 1.0;
       if (TAPE) fl |= TF_VMAX_HIT;
     }
-    const bool vmax_hit = vnewc >= prm.eosvmax;
     // calcPressureForElems (src/domain.jl:2585-2614) for one element; the
     // cut / pmin outcomes go to the tape bits given
     auto pressure = [&](double enew, double bvc, unsigned long long cut_bit, unsigned long long min_bit) -> double {
       double pn = bvc * enew;
       if (abs_lt(pn, prm.p_cut)) { pn = 0.0; if (TAPE) fl |= cut_bit; }
       if (vmax_hit) pn = 0.0;
-      if (pn < prm.pmin) { pn = prm.pmin; if (TAPE) fl |= min_bit; }
+      if (fkey(pn) < prm.k_pmin) { pn = prm.pmin; if (TAPE) fl |= min_bit; }
       return pn;
     };
     const double pq_old = p_old + q_old;
     double e_new = fma(-0.5 * delvc, pq_old, e_old);
-    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
+    if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
     const double bvc_half = c1s * bvh;
     const double pHalfStep = pressure(e_new, bvc_half, TF_PH_CUT, TF_PH_MIN);
     // vhalf = 1 / (1 + compHalfStep): vchalf, vnewc or 1 by the branch taken
-    const double vhalf = (prm.eosvmax != 0.0 && vnewc >= prm.eosvmax) ? 1.0
-                       : (prm.eosvmin != 0.0 && vnewc <= prm.eosvmin) ? vnewc : vchalf;
+    const double vhalf = at_vmax ? 1.0 : at_vmin ? vnewc : vchalf;
     const bool compress = !gt_zero(delvc);   // delvc <= 0 (non-NaN)
     if (TAPE && compress) fl |= TF_COMPRESS;
     tm(14, bv); tm(15, bvh); tm(16, e_new); tm(17, pHalfStep); tm(18, vhalf);
@@ -766,7 +791,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     tm(20, q_new);
     e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E2_CUT; }
-    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
+    if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
     const double bvc = c1s * bv;
     double p_new = pressure(e_new, bvc, TF_PN1_CUT, TF_PN1_MIN);
     const double vv_bvc = (vnewc * vnewc) * bvc;
@@ -783,7 +808,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     tm(24, q_tilde);
     e_new = e_new - ((fma(7.0, pq_old, -8.0 * (pHalfStep + q_new)) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E3_CUT; }
-    if (e_new < prm.emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
+    if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
     p_new = pressure(e_new, bvc, TF_PN2_CUT, TF_PN2_MIN);
     e_out = e_new; p_out = p_new; vv_out = vv_bvc; compress_out = compress;
     }  // rep loop
@@ -811,10 +836,10 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 
     // ---- Courant and hydro constraints, src/domain.jl:2964-3054 ----
     double dtc = __longlong_as_double((long long)kInfBits), dth = dtc;
-    if (vdov != 0.0) {
+    if (!is_zero(vdov)) {
       const double arealg = LDG(&d.arealg[i]);
       double dtf = ss_new * ss_new;
-      if (vdov < 0.0) dtf = fma(((64.0 * prm.qqc) * prm.qqc) * (arealg * arealg), vdov * vdov, dtf);
+      if (lt_zero(vdov)) dtf = fma(prm.qqc2x64 * (arealg * arealg), vdov * vdov, dtf);
       dtc = arealg * rsqrt(dtf);
       dth = prm.dvovmax * inv_w;
       courant = (unsigned long long)__double_as_longlong(dtc);
