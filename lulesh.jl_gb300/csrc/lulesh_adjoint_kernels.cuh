@@ -118,7 +118,7 @@ __device__ __forceinline__ int limiter_index(unsigned mask, unsigned bits, unsig
 // Courant and hydro candidates).
 // ---------------------------------------------------------------------------
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_material(AdjDev a, Params prm, double irho0, const CycleRec* rec,
+__global__ void __launch_bounds__(kAdjBlock, 4) ka_material(AdjDev a, Params prm, double irho0, const CycleRec* rec,
                                                           const AdjScal* sc) {
   const int E = a.E;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -351,7 +351,7 @@ __device__ __forceinline__ void walsh1_t(const double Lw[3], double L[8]) {
 // ka_kinematics: transpose of k_kinematics (volume, characteristic length,
 // velocity-gradient trace, monotonic-Q gradients), into the corner buffers.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAdjBlock) ka_kinematics(AdjDev a, const CycleRec* rec) {
+__global__ void __launch_bounds__(kAdjBlock, 4) ka_kinematics(AdjDev a, const CycleRec* rec) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const double dt = rec->dt;
@@ -720,28 +720,40 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
           A[k][j] = fma(S[k][0], hms[j][0], fma(S[k][1], hms[j][1], fma(S[k][2], hms[j][2], S[k][3] * hms[j][3])));
           B[k][j] = fma(T[k][0], hms[j][0], fma(T[k][1], hms[j][1], fma(T[k][2], hms[j][2], T[k][3] * hms[j][3])));
         }
-      // dL/dhm_j = vi12 dL/dhms_j; dL/dvi12 = sum_j dL/dhms_j . hm_j = sum_j dL/dhms_j . hms_j / vi12
-      double Lvi12 = 0.0;
+      // dL/dhms_j = -coef P_j with P_j[m] the dot products below; dL/dhm_j =
+      // vi12 dL/dhms_j (hms = vi12 hm); dL/dvi12 = sum_j dL/dhms_j . hms_j / vi12
+      double Pvi = 0.0;  // sum_j P_j . hms_j
+      {
+        const double ncv = -coef * vi12;
 #pragma unroll
-      for (int j = 0; j < 3; ++j)
+        for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int m = 0; m < 4; ++m) {
-          const double Lhms = -coef * fma(S[0][m], C[0][j], fma(S[1][m], C[1][j], fma(S[2][m], C[2][j],
-                              fma(T[0][m], D[0][j], fma(T[1][m], D[1][j], T[2][m] * D[2][j])))));
-          Lvi12 = fma(Lhms, hms[j][m], Lvi12);
-          a.sLhm[(j * 4 + m) * E + e] = vi12 * Lhms;  // hms = vi12 * hm
-        }
-      // dL/dV_k = coef (Gamma^T T_k - sum_j dv_j B[k][j])
+          for (int m = 0; m < 4; ++m) {
+            const double P = fma(S[0][m], C[0][j], fma(S[1][m], C[1][j], fma(S[2][m], C[2][j],
+                             fma(T[0][m], D[0][j], fma(T[1][m], D[1][j], T[2][m] * D[2][j])))));
+            Pvi = fma(P, hms[j][m], Pvi);
+            a.sLhm[(j * 4 + m) * E + e] = ncv * P;
+          }
+      }
+      const double Lvi12 = -coef * Pvi;
+      // the coefficient folded into the tables: nA = -coef A, nB = -coef B
+      double nA[3][3], nB[3][3];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { nA[k][j] = -coef * A[k][j]; nB[k][j] = -coef * B[k][j]; }
+      // dL/dV_k = coef (Gamma^T T_k - sum_j dv_j B[k][j]) = Gamma^T (coef T_k) + sum_j dv_j nB[k][j]
 #pragma unroll
       for (int k = 0; k < 3; ++k) {
-        double q[8];
-        walsh_modes_t(T[k], q);
+        double cT[4], q[8];
+#pragma unroll
+        for (int m = 0; m < 4; ++m) cT[m] = coef * T[k][m];
+        walsh_modes_t(cT, q);
 #pragma unroll
         for (int c = 0; c < 8; ++c)
-          a.fV[(k * 8 + c) * E + e] =
-              coef * fma(-dv[2][c], B[k][2], fma(-dv[1][c], B[k][1], fma(-dv[0][c], B[k][0], q[c])));
+          a.fV[(k * 8 + c) * E + e] = fma(dv[2][c], nB[k][2], fma(dv[1][c], nB[k][1], fma(dv[0][c], nB[k][0], q[c])));
       }
-      // dL/ddv_j = -coef sum_k (lf_k A[k][j] + V_k B[k][j])
+      // dL/ddv_j = -coef sum_k (lf_k A[k][j] + V_k B[k][j]) = sum_k (lf_k nA[k][j] + V_k nB[k][j])
       {
         double Ldv[3][8];
 #pragma unroll
@@ -754,13 +766,13 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
           for (int c = 0; c < 8; ++c) {
             const double lf = Lf[k][nd[c]], vv = Vp[k][nd[c]];
 #pragma unroll
-            for (int j = 0; j < 3; ++j) Ldv[j][c] = fma(lf, A[k][j], fma(vv, B[k][j], Ldv[j][c]));
+            for (int j = 0; j < 3; ++j) Ldv[j][c] = fma(lf, nA[k][j], fma(vv, nB[k][j], Ldv[j][c]));
           }
         }
 #pragma unroll
         for (int j = 0; j < 3; ++j)
 #pragma unroll
-          for (int c = 0; c < 8; ++c) a.sLdv[(j * 8 + c) * E + e] = -coef * Ldv[j][c];
+          for (int c = 0; c < 8; ++c) a.sLdv[(j * 8 + c) * E + e] = Ldv[j][c];
       }
       // coef = c0 ss mass determ^(-1/3), vi12 = 1/(12 determ), determ = volo v
       a.lss[e] += Lcoef * c0 * mass * r;
@@ -964,15 +976,29 @@ __host__ __device__ inline void time_increment_reverse(const CycleRec& r, const 
 }
 
 // Closes the transpose of one cycle (one block): sums the kernels' partial
-// adjoints of dt and hgcoef in a fixed order, then transposes time += dt and
-// timeIncrement! on the carried scalar adjoints.
-constexpr int kCloseBlock = 1024;
+// adjoints of dt and hgcoef in a fixed order (each thread its strided share
+// of all three, a warp tree, then the warps in order), then transposes
+// time += dt and timeIncrement! on the carried scalar adjoints.
+constexpr int kCloseBlock = 256;
 __global__ void __launch_bounds__(kCloseBlock) ka_cycle_close(AdjDev a, int ge, int gn, const CycleRec* rec,
                                                                AdjScal* sc, Params prm) {
-  const double s_kin = block_fixed_sum<kCloseBlock>(a.part_dt, ge);
-  const double s_node = block_fixed_sum<kCloseBlock>(a.part_dtn, gn);
-  const double s_hg = block_fixed_sum<kCloseBlock>(a.part_hg, ge);
+  double t_kin = 0.0, t_node = 0.0, t_hg = 0.0;
+  for (int j = threadIdx.x; j < ge; j += kCloseBlock) { t_kin += a.part_dt[j]; t_hg += a.part_hg[j]; }
+  for (int j = threadIdx.x; j < gn; j += kCloseBlock) t_node += a.part_dtn[j];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    t_kin += __shfl_down_sync(0xffffffffu, t_kin, o);
+    t_node += __shfl_down_sync(0xffffffffu, t_node, o);
+    t_hg += __shfl_down_sync(0xffffffffu, t_hg, o);
+  }
+  __shared__ double wsum[3][kCloseBlock / 32];
+  const int w = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { wsum[0][w] = t_kin; wsum[1][w] = t_node; wsum[2][w] = t_hg; }
+  __syncthreads();
   if (threadIdx.x != 0) return;
+  double s_kin = wsum[0][0], s_node = wsum[1][0], s_hg = wsum[2][0];
+#pragma unroll
+  for (int k = 1; k < kCloseBlock / 32; ++k) { s_kin += wsum[0][k]; s_node += wsum[1][k]; s_hg += wsum[2][k]; }
   const CycleRec r = *rec;
   AdjScal v = *sc;
   v.Lhg += s_hg;
