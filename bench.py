@@ -302,6 +302,21 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
     res = adj.result
     ge, ghg = adj.grad("e"), res.grad_hgcoef
     hg0 = snap[1]["hgcoef"]
+    # the same gradient with each segment's recompute and transpose in turn
+    # (one tape) instead of overlapped (two tapes)
+    adj.set_overlap(False)
+    restore()
+    adj.gradient(cycles)  # warm-up (graphs)
+    seq = []
+    for _ in range(2):
+        restore()
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        adj.gradient(cycles)
+        torch.cuda.synchronize(dev)
+        seq.append(time.perf_counter() - t0)
+    seq_same = bool(np.array_equal(adj.grad("e"), ge)) and adj.result.grad_hgcoef == ghg
+    adj.set_overlap(True)
 
     def loss_at(e, hg):
         restore(e, hg)
@@ -319,8 +334,8 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
         errs.append(abs(an - fd) / max(abs(fd), 1e-12 * abs(loss)))
     adj.close()
     # the same gradient with the whole run taped in HBM (no recompute): one
-    # segment of `cycles` cycles, about 8 * (238 E + 3 N) bytes per cycle
-    tape_gb = 8.0 * (238 * g.numElem + 3 * g.numNode) * cycles / 1e9
+    # segment of `cycles` cycles, about 8 * (241 E + 9 N) bytes per cycle
+    tape_gb = 8.0 * (241 * g.numElem + 9 * g.numNode) * cycles / 1e9
     full = None
     try:
         adj2 = L.Adjoint(g, radius=0.3, checkpoint_every=cycles)
@@ -347,6 +362,9 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
             "nx": nx, "cycles": int(res.cycles), "checkpoints": int(res.checkpoints),
             "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
             "adjoint_sweep_ms": {"checkpointed_forward": res.forward_ms, "reverse": res.reverse_ms},
+            "reverse_sweep": "recompute of each segment overlapped with the transpose of the next (two tapes)",
+            "sequential": {"adjoint_s": min(seq), "adjoint_over_forward": min(seq) / fwd_s,
+                           "gradient_bitwise_equal": seq_same},
             "loss": loss, "grad_hgcoef": ghg, "grad_e_origin": float(ge[0]),
             "fd": {"directions": dirs, "step": h, "max_rel_err": max(errs),
                    "median_rel_err": float(np.median(errs))},

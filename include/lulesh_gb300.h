@@ -312,8 +312,11 @@ int lulesh_calc_force_for_nodes_static(const lulesh_force_args* args, void* stre
  * v ss (element); the gradient w.r.t. the run's initial value of each is
  * returned (lulesh_adj_get_gradient), with dL/dhgcoef in the result.
  * Memory: one state per checkpoint plus checkpoint_every cycles of tape
- * (about 8*(12*E + 5*N) bytes per taped cycle). The derivative is that of the
- * branches the forward run took (dt minima, clamps, limiter cases). */
+ * (about 8*(241*E + 9*N) bytes per taped cycle); a second tape of the same
+ * size, allocated at the first gradient that has two or more segments if it
+ * fits, lets the recompute of one segment overlap the transpose of the next
+ * (lulesh_adj_set_overlap). The derivative is that of the branches the
+ * forward run took (dt minima, clamps, limiter cases). */
 typedef struct lulesh_adjoint lulesh_adjoint;
 
 typedef struct {
@@ -340,6 +343,11 @@ int lulesh_adj_loss(lulesh_adjoint* adj, double* loss);
  * w.r.t. the initial state and hgcoef. result->cycles is the number run. */
 int lulesh_adj_gradient(lulesh_adjoint* adj, int64_t num_cycles, lulesh_adj_result* result);
 int lulesh_adj_get_gradient(lulesh_adjoint* adj, int32_t field, double* host, int64_t count);
+/* enable = 0: one tape, each segment recomputed and then transposed on the
+ * domain's stream (frees the second tape). enable = 1 (the default): the
+ * second tape is allocated now; LULESH_ERR_MEMORY (and the sequential sweep)
+ * if it does not fit. Gradients are bitwise the same either way. */
+int lulesh_adj_set_overlap(lulesh_adjoint* adj, int32_t enable);
 
 /* Human-readable text of a status code. */
 const char* lulesh_status_string(int32_t status);

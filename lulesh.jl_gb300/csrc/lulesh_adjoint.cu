@@ -14,7 +14,9 @@
 //      element that attained them.
 // The forward sweep runs as lulesh_run does (CUDA graphs, dt on the device);
 // the recompute and the transpose of a segment are queued without any host
-// synchronisation.
+// synchronisation. With two tape sets (when they fit), segment k-1 is
+// recomputed on a second stream while segment k is transposed: the FP64-bound
+// forward kernels fill the SMs the latency-bound transposes leave idle.
 // The handle is left at its final state. Every derivative is that of the
 // branches the forward run took.
 #include <cuda_runtime.h>
@@ -76,14 +78,26 @@ double** state_ptr(DevDomain& d, int k) {
 
 }  // namespace
 
+// What one segment's recompute leaves for its transpose: the K+1 states, the
+// K cycles' tape and their device records.
+struct TapeSet {
+  std::vector<StateBuf> slots;
+  std::vector<CycleTape> tape;
+  CycleRec* rec = nullptr;
+  bool ready = false;
+};
+
 struct lulesh_adjoint {
   lulesh_domain* dom = nullptr;
   double radius = 0.3;
   int K = 20;
   int E = 0, N = 0;
   std::vector<void*> allocs;
-  std::vector<StateBuf> slots;   // K+1 states of the current segment
-  std::vector<CycleTape> tape;   // K cycles
+  TapeSet sets[2];               // set 1 only for the overlapped reverse sweep
+  std::vector<void*> set1_allocs;
+  bool overlap = true;           // overlap recompute and transpose when set 1 fits
+  cudaStream_t rstream = nullptr;  // recompute stream of the overlapped sweep
+  cudaEvent_t ev_start = nullptr, ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   std::vector<StateBuf> ckpts;   // segment start states
   std::vector<int> seg_len;      // cycles of each segment
   DevState* ckpt_st = nullptr;   // device: step state at each checkpoint
@@ -94,7 +108,6 @@ struct lulesh_adjoint {
   double *fx_s = nullptr, *fy_s = nullptr, *fz_s = nullptr;  // force scratch of taped cycles
   AdjDev ad{};
   double* scal = nullptr;       // device: sums of partials (objective)
-  CycleRec* rec = nullptr;      // device: K cycle records of the current segment
   AdjScal* dsc = nullptr;       // device: carried scalar adjoints
   std::map<int32_t, double*> seeds;  // linear-objective weights per state field
   // graph of K forward cycles for the checkpointed sweep, with what it bakes in
@@ -102,28 +115,91 @@ struct lulesh_adjoint {
   Params fwd_prm{};
   Tuning fwd_tuning{};
   bool fwd_aux = false;
-  // graph of one full segment's recompute and transpose
-  cudaGraphExec_t rev_graph = nullptr;
+  // graphs of one full segment's recompute (into set X) and transpose (of
+  // set X), with what they bake in
+  cudaGraphExec_t rec_graph[2] = {nullptr, nullptr}, tr_graph[2] = {nullptr, nullptr};
   Params rev_prm{};
   Tuning rev_tuning{};
 };
 
-static int dmalloc(lulesh_adjoint* a, void** p, size_t bytes) {
+static int dmalloc_to(std::vector<void*>& list, void** p, size_t bytes) {
   if (cudaMalloc(p, bytes ? bytes : 8) != cudaSuccess) { cudaGetLastError(); return LULESH_ERR_MEMORY; }
-  a->allocs.push_back(*p);
+  list.push_back(*p);
   return LULESH_OK;
 }
+static int dmalloc(lulesh_adjoint* a, void** p, size_t bytes) { return dmalloc_to(a->allocs, p, bytes); }
 template <class T>
 static int dalloc(lulesh_adjoint* a, T** p, size_t n) {
   return dmalloc(a, reinterpret_cast<void**>(p), n * sizeof(T));
 }
+template <class T>
+static int dalloc_to(std::vector<void*>& list, T** p, size_t n) {
+  return dmalloc_to(list, reinterpret_cast<void**>(p), n * sizeof(T));
+}
 
-static int alloc_state(lulesh_adjoint* a, StateBuf& s) {
+static int alloc_state_to(lulesh_adjoint* a, std::vector<void*>& list, StateBuf& s) {
   for (int k = 0; k < kStateFields; ++k) {
-    int rc = dalloc(a, &s.f[k], k < 6 ? a->N : a->E);
+    int rc = dalloc_to(list, &s.f[k], k < 6 ? a->N : a->E);
     if (rc) return rc;
   }
   return LULESH_OK;
+}
+static int alloc_state(lulesh_adjoint* a, StateBuf& s) { return alloc_state_to(a, a->allocs, s); }
+
+// The K+1 states, K cycles of tape and K records of one tape set.
+static int alloc_set(lulesh_adjoint* a, std::vector<void*>& list, TapeSet& t) {
+  const int E = a->E, N = a->N, K = a->K;
+  int rc;
+  t.slots.assign(K + 1, StateBuf{});
+  for (auto& st : t.slots)
+    if ((rc = alloc_state_to(a, list, st))) return rc;
+  t.tape.assign(K, CycleTape{});
+  for (auto& c : t.tape) {
+    if ((rc = dalloc_to(list, &c.ax, N)) || (rc = dalloc_to(list, &c.ay, N)) || (rc = dalloc_to(list, &c.az, N)) ||
+        (rc = dalloc_to(list, &c.vnew, E)) || (rc = dalloc_to(list, &c.delv, E)) ||
+        (rc = dalloc_to(list, &c.arealg, E)) || (rc = dalloc_to(list, &c.vdov, E)) ||
+        (rc = dalloc_to(list, &c.flags, E)) || (rc = dalloc_to(list, &c.dtc, E)) || (rc = dalloc_to(list, &c.dth, E)) ||
+        (rc = dalloc_to(list, &c.geo, 102 * (size_t)E)) || (rc = dalloc_to(list, &c.kin, 90 * (size_t)E)) ||
+        (rc = dalloc_to(list, &c.mat, 31 * (size_t)E)))
+      return rc;
+    for (int k = 0; k < 3; ++k)
+      if ((rc = dalloc_to(list, &c.dv[k], E)) || (rc = dalloc_to(list, &c.dx[k], E))) return rc;
+  }
+  if ((rc = dalloc_to(list, &t.rec, K))) return rc;
+  t.ready = true;
+  return LULESH_OK;
+}
+
+static void free_set1(lulesh_adjoint* a) {
+  if (a->rec_graph[1]) { cudaGraphExecDestroy(a->rec_graph[1]); a->rec_graph[1] = nullptr; }
+  if (a->tr_graph[1]) { cudaGraphExecDestroy(a->tr_graph[1]); a->tr_graph[1] = nullptr; }
+  for (void* p : a->set1_allocs) cudaFree(p);
+  a->set1_allocs.clear();
+  a->sets[1] = TapeSet{};
+}
+
+// Set 1, the stream and the events of the overlapped reverse sweep; false
+// (sequential sweep) when they do not fit.
+static bool ensure_overlap(lulesh_adjoint* a) {
+  if (!a->overlap) return false;
+  if (a->sets[1].ready) return true;
+  if (!a->rstream && cudaStreamCreateWithFlags(&a->rstream, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    a->rstream = nullptr;
+    return false;
+  }
+  cudaEvent_t* evs[5] = {&a->ev_start, &a->ev_ready[0], &a->ev_ready[1], &a->ev_free[0], &a->ev_free[1]};
+  for (cudaEvent_t* e : evs)
+    if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      *e = nullptr;
+      return false;
+    }
+  if (alloc_set(a, a->set1_allocs, a->sets[1]) != LULESH_OK) {
+    free_set1(a);
+    return false;
+  }
+  return true;
 }
 
 static StateSet domain_set(lulesh_adjoint* a) {
@@ -136,12 +212,16 @@ static StateSet buf_set(const StateBuf& b) {
   for (int k = 0; k < kStateFields; ++k) t.f[k] = b.f[k];
   return t;
 }
-static void copy_state(lulesh_adjoint* a, const StateSet& src, const StateSet& dst) {
+static void copy_state(lulesh_adjoint* a, const StateSet& src, const StateSet& dst, cudaStream_t s) {
   const int n = std::max(a->E, a->N);
-  ka_copy_state<<<(n + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, a->dom->stream>>>(src, dst, a->E, a->N);
+  ka_copy_state<<<(n + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(src, dst, a->E, a->N);
 }
-static void copy_state_from_domain(lulesh_adjoint* a, StateBuf& s) { copy_state(a, domain_set(a), buf_set(s)); }
-static void copy_state_to_domain(lulesh_adjoint* a, const StateBuf& s) { copy_state(a, buf_set(s), domain_set(a)); }
+static void copy_state_from_domain(lulesh_adjoint* a, StateBuf& b, cudaStream_t s) {
+  copy_state(a, domain_set(a), buf_set(b), s);
+}
+static void copy_state_to_domain(lulesh_adjoint* a, const StateBuf& b, cudaStream_t s) {
+  copy_state(a, buf_set(b), domain_set(a), s);
+}
 
 static Scalars5 get_scalars(const lulesh_domain* d) {
   return Scalars5{d->sc[LULESH_S_TIME], d->sc[LULESH_S_DELTATIME], d->sc[LULESH_S_DTCOURANT],
@@ -159,10 +239,9 @@ static void set_scalars(lulesh_domain* d, const Scalars5& s) {
 // timeIncrement! on the device (recorded), the step kernels with the cycle's
 // intermediate values, accelerations, branch flags and dt candidates going to
 // the tape, then the arg-min elements of the Courant and hydro minima.
-static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, CycleRec* rec) {
+static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, CycleRec* rec, cudaStream_t s) {
   lulesh_domain* d = a->dom;
   const Params prm = make_params(d);
-  cudaStream_t s = d->stream;
   const int nmax = std::max(a->E, a->N);
   ka_tape_begin<<<(nmax + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(domain_set(a), buf_set(slot), a->E, a->N,
                                                                         d->dd.st, rec, prm);
@@ -199,9 +278,8 @@ static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const Stat
 // Transpose of one recorded cycle, queued on the stream: the adjoint state
 // goes from the cycle's end to its start, and the carried scalar adjoints
 // through timeIncrement!.
-static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec) {
+static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec, cudaStream_t s) {
   lulesh_domain* d = a->dom;
-  cudaStream_t s = d->stream;
   const Params prm = make_params(d);
   const int ge = (a->E + kAdjBlock - 1) / kAdjBlock, gn = (a->N + kAdjBlock - 1) / kAdjBlock;
   const int mode = d->dd.mode;
@@ -306,20 +384,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
   const int E = a->E, N = a->N, K = a->K;
   auto fail = [&](int rc) { lulesh_adj_destroy(a); return rc; };
   int rc;
-  a->slots.resize(K + 1);
-  for (auto& s : a->slots)
-    if ((rc = alloc_state(a, s))) return fail(rc);
-  a->tape.resize(K);
-  for (auto& t : a->tape) {
-    if ((rc = dalloc(a, &t.ax, N)) || (rc = dalloc(a, &t.ay, N)) || (rc = dalloc(a, &t.az, N)) ||
-        (rc = dalloc(a, &t.vnew, E)) || (rc = dalloc(a, &t.delv, E)) || (rc = dalloc(a, &t.arealg, E)) ||
-        (rc = dalloc(a, &t.vdov, E)) || (rc = dalloc(a, &t.flags, E)) || (rc = dalloc(a, &t.dtc, E)) ||
-        (rc = dalloc(a, &t.dth, E)) || (rc = dalloc(a, &t.geo, 102 * (size_t)E)) ||
-        (rc = dalloc(a, &t.kin, 90 * (size_t)E)) || (rc = dalloc(a, &t.mat, 31 * (size_t)E)))
-      return fail(rc);
-    for (int k = 0; k < 3; ++k)
-      if ((rc = dalloc(a, &t.dv[k], E)) || (rc = dalloc(a, &t.dx[k], E))) return fail(rc);
-  }
+  if ((rc = alloc_set(a, a->allocs, a->sets[0]))) return fail(rc);
   if ((rc = alloc_state(a, a->final_state))) return fail(rc);
   AdjDev& ad = a->ad;
   const int ge = (E + kAdjBlock - 1) / kAdjBlock, gn = (N + kAdjBlock - 1) / kAdjBlock;
@@ -334,7 +399,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
       (rc = dalloc(a, &ad.fX, 24 * (size_t)E)) || (rc = dalloc(a, &ad.fV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
       (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
       (rc = dalloc(a, &ad.part_dtn, gn)) || (rc = dalloc(a, &ad.part_hg, ge)) || (rc = dalloc(a, &a->scal, 4)) ||
-      (rc = dalloc(a, &a->rec, K)) || (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
+      (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
       (rc = dalloc(a, &a->fx_s, N)) || (rc = dalloc(a, &a->fy_s, N)) || (rc = dalloc(a, &a->fz_s, N)))
     return fail(rc);
   for (int k = 0; k < 3; ++k)
@@ -429,9 +494,32 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   cudaSetDevice(a->dom->params.device);
   cudaStreamSynchronize(a->dom->stream);
   if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
-  if (a->rev_graph) cudaGraphExecDestroy(a->rev_graph);
+  if (a->rec_graph[0]) cudaGraphExecDestroy(a->rec_graph[0]);
+  if (a->tr_graph[0]) cudaGraphExecDestroy(a->tr_graph[0]);
+  if (a->rstream) cudaStreamSynchronize(a->rstream);
+  free_set1(a);
+  for (cudaEvent_t e : {a->ev_start, a->ev_ready[0], a->ev_ready[1], a->ev_free[0], a->ev_free[1]})
+    if (e) cudaEventDestroy(e);
+  if (a->rstream) cudaStreamDestroy(a->rstream);
   for (void* p : a->allocs) cudaFree(p);
   delete a;
+  return LULESH_OK;
+}
+
+int lulesh_adj_set_overlap(lulesh_adjoint* a, int32_t enable) {
+  if (!a) return LULESH_ERR_ARGUMENT;
+  ACK(cudaSetDevice(a->dom->params.device));
+  ACK(cudaStreamSynchronize(a->dom->stream));
+  if (a->rstream) ACK(cudaStreamSynchronize(a->rstream));
+  a->overlap = enable != 0;
+  if (!a->overlap) {
+    free_set1(a);
+    return LULESH_OK;
+  }
+  if (!ensure_overlap(a)) {
+    a->overlap = false;
+    return LULESH_ERR_MEMORY;
+  }
   return LULESH_OK;
 }
 
@@ -490,6 +578,9 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   }
   const Params prm = make_params(d);
   const bool aux = d->params.keep_aux != 0;
+  // segment k's tape set: k & 1 when recompute and transpose overlap
+  const bool pipe = nplan > 1 && ensure_overlap(a);
+  auto set_of = [&](int k) -> TapeSet& { return a->sets[pipe ? (k & 1) : 0]; };
   if (nplan > 1 && (!a->fwd_graph || std::memcmp(&a->fwd_prm, &prm, sizeof(Params)) != 0 ||
                     std::memcmp(&a->fwd_tuning, &d->tuning, sizeof(Tuning)) != 0 || a->fwd_aux != aux)) {
     if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
@@ -515,13 +606,14 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   state_to_device_mirror(d);  // no cycle limit: the segments count the cycles
   ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
   for (int k = 0; k < nplan; ++k) {
-    copy_state_from_domain(a, a->ckpts[k]);
+    copy_state_from_domain(a, a->ckpts[k], s);
     ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
     if (k < nplan - 1) {
       ACK(cudaGraphLaunch(a->fwd_graph, s));
     } else {
-      for (int j = 0; j < last_len; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
-      copy_state_from_domain(a, a->slots[last_len]);
+      TapeSet& ts = set_of(k);
+      for (int j = 0; j < last_len; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], ts.rec + j, s);
+      copy_state_from_domain(a, ts.slots[last_len], s);
     }
   }
   ACK(cudaGetLastError());
@@ -544,54 +636,89 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   out.cycles = done;
   out.checkpoints = nseg;
   if ((rc = objective(a, true, &out.loss))) return rc;
-  copy_state_from_domain(a, a->final_state);
+  copy_state_from_domain(a, a->final_state, s);
   const Scalars5 final_sc = get_scalars(d);
   // ---- reverse sweep ----
   ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
   ACK(cudaMemsetAsync(a->ad.fX, 0, 24 * sizeof(double) * (size_t)a->E, s));
   ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
-  // a full segment's recompute and transpose read and write the same slots,
-  // tape and records whichever segment it is: one captured graph serves all
-  // (rebuilt when the parameters it bakes in change)
-  auto queue_segment = [&](int n, bool recompute) {
-    if (recompute) {
-      for (int j = 0; j < n; ++j) tape_cycle(a, a->slots[j], a->tape[j], a->rec + j);
-      copy_state_from_domain(a, a->slots[n]);
-    }
+  // Recompute R(k) (checkpoint k restored into the domain, its cycles taped
+  // into set_of(k)) and transpose T(k) (the adjoint state through those
+  // cycles, in reverse). T runs on the domain's stream in order k = nseg-1..0.
+  // Overlapped, R runs on its own stream one segment ahead: R(k-1) is queued
+  // before T(k), waits until T(k+1) has released its set, and T(k) waits for
+  // R(k). Sequential, R(k) runs right before T(k) on the domain's stream.
+  // Full segments run as captured graphs (one per set and phase, rebuilt
+  // when the parameters they bake in change).
+  cudaStream_t rs = pipe ? a->rstream : s;
+  auto queue_recompute = [&](TapeSet& ts, int n, cudaStream_t st) {
+    for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], ts.rec + j, st);
+    copy_state_from_domain(a, ts.slots[n], st);
+  };
+  auto queue_transpose = [&](TapeSet& ts, int n, cudaStream_t st) {
     for (int j = n - 1; j >= 0; --j) {
-      set_cycle_pointers(a, a->slots[j], a->slots[j + 1], a->tape[j]);
-      reverse_cycle(a, a->rec + j);
+      set_cycle_pointers(a, ts.slots[j], ts.slots[j + 1], ts.tape[j]);
+      reverse_cycle(a, ts.rec + j, st);
     }
   };
-  const bool full_recomputed = nseg > 1 || (nseg == 1 && !last_taped);
-  if (full_recomputed && (!a->rev_graph || std::memcmp(&a->rev_prm, &prm, sizeof(Params)) != 0 ||
-                          std::memcmp(&a->rev_tuning, &d->tuning, sizeof(Tuning)) != 0)) {
-    if (a->rev_graph) cudaGraphExecDestroy(a->rev_graph);
-    a->rev_graph = nullptr;
-    cudaGraph_t g;
-    ACK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    queue_segment(K, true);
-    ACK(cudaStreamEndCapture(s, &g));
-    const cudaError_t ge = cudaGraphInstantiate(&a->rev_graph, g, 0);
-    cudaGraphDestroy(g);
-    ACK(ge);
+  const int nsets = pipe ? 2 : 1;
+  if (std::memcmp(&a->rev_prm, &prm, sizeof(Params)) != 0 || std::memcmp(&a->rev_tuning, &d->tuning, sizeof(Tuning)) != 0) {
+    for (int x = 0; x < 2; ++x) {
+      if (a->rec_graph[x]) { cudaGraphExecDestroy(a->rec_graph[x]); a->rec_graph[x] = nullptr; }
+      if (a->tr_graph[x]) { cudaGraphExecDestroy(a->tr_graph[x]); a->tr_graph[x] = nullptr; }
+    }
     a->rev_prm = prm;
     a->rev_tuning = d->tuning;
   }
+  auto capture = [&](cudaGraphExec_t* out, cudaStream_t st, auto&& body) -> int {
+    cudaGraph_t g;
+    ACK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    body();
+    ACK(cudaStreamEndCapture(st, &g));
+    const cudaError_t ge = cudaGraphInstantiate(out, g, 0);
+    cudaGraphDestroy(g);
+    ACK(ge);
+    return LULESH_OK;
+  };
+  const bool any_full = std::count(a->seg_len.begin(), a->seg_len.end(), K) > 0;
+  for (int x = 0; x < nsets && any_full; ++x) {
+    TapeSet& ts = a->sets[x];
+    if (!a->rec_graph[x] && (rc = capture(&a->rec_graph[x], rs, [&] { queue_recompute(ts, K, rs); }))) return rc;
+    if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], s, [&] { queue_transpose(ts, K, s); }))) return rc;
+  }
+  auto recomputed = [&](int k) { return !(k == nseg - 1 && last_taped); };
+  auto enqueue_R = [&](int k) -> int {
+    const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
+    if (pipe && k + 2 <= nseg - 1) ACK(cudaStreamWaitEvent(rs, a->ev_free[x], 0));
+    copy_state_to_domain(a, a->ckpts[k], rs);
+    ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, rs));
+    if (n == K) ACK(cudaGraphLaunch(a->rec_graph[x], rs));
+    else queue_recompute(a->sets[x], n, rs);
+    if (pipe) ACK(cudaEventRecord(a->ev_ready[x], rs));
+    return LULESH_OK;
+  };
+  if (pipe) {
+    // the recompute stream starts once the objective and the final state are taken
+    ACK(cudaEventRecord(a->ev_start, s));
+    ACK(cudaStreamWaitEvent(rs, a->ev_start, 0));
+    if (recomputed(nseg - 1) && (rc = enqueue_R(nseg - 1))) return rc;
+  }
   for (int k = nseg - 1; k >= 0; --k) {
-    const int n = a->seg_len[k];
-    const bool recompute = !(k == nseg - 1 && last_taped);
-    if (recompute) {
-      copy_state_to_domain(a, a->ckpts[k]);
-      ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+    const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
+    if (pipe) {
+      if (k >= 1 && (rc = enqueue_R(k - 1))) return rc;
+      if (recomputed(k)) ACK(cudaStreamWaitEvent(s, a->ev_ready[x], 0));
+    } else if (recomputed(k) && (rc = enqueue_R(k))) {
+      return rc;
     }
-    if (recompute && n == K) ACK(cudaGraphLaunch(a->rev_graph, s));
-    else queue_segment(n, recompute);
+    if (n == K) ACK(cudaGraphLaunch(a->tr_graph[x], s));
+    else queue_transpose(a->sets[x], n, s);
+    if (pipe) ACK(cudaEventRecord(a->ev_free[x], s));
     ACK(cudaGetLastError());
   }
   // the first cycle's force transpose is still in the force corner buffers
   ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
-  copy_state_to_domain(a, a->final_state);
+  copy_state_to_domain(a, a->final_state, s);
   AdjScal hsc;
   ACK(cudaMemcpyAsync(&hsc, a->dsc, sizeof(AdjScal), cudaMemcpyDeviceToHost, s));
   ACK(cudaStreamSynchronize(s));

@@ -21,7 +21,7 @@ module LULESHGB300
 
 using LULESH
 
-export GPUDomain, LuleshGPUError, GPUAdjoint, energy_gradient!, save_state, load_state!
+export GPUDomain, LuleshGPUError, GPUAdjoint, energy_gradient!, save_state, load_state!, set_overlap!
 
 const libpath = get(ENV, "LULESH_GB300_LIB",
                     joinpath(@__DIR__, "..", "lib", "liblulesh_gb300.so"))
@@ -225,6 +225,18 @@ function set_seed!(a::GPUAdjoint, field::Symbol, w::Vector{Float64})
 end
 
 clear_seeds!(a::GPUAdjoint) = (ccall((:lulesh_adj_clear_seeds, libpath), Cint, (Ptr{Cvoid},), a.handle); a)
+
+"""
+    set_overlap!(a, enable::Bool)
+
+Overlap each checkpoint segment's recompute with the transpose of the
+segment after it (two tapes, the default), or run them in turn on one tape.
+"""
+function set_overlap!(a::GPUAdjoint, enable::Bool)
+    rc = ccall((:lulesh_adj_set_overlap, libpath), Cint, (Ptr{Cvoid}, Int32), a.handle, Int32(enable))
+    rc == 0 || throw(LuleshGPUError("overlap: status $rc", rc))
+    return a
+end
 
 """
     gradient!(a, num_cycles) -> AdjResult

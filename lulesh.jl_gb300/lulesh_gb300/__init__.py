@@ -183,6 +183,7 @@ def load_library():
         "lulesh_adj_loss": (ctypes.c_int, [P, ctypes.POINTER(dbl)]),
         "lulesh_adj_gradient": (ctypes.c_int, [P, i64, ctypes.POINTER(AdjResult)]),
         "lulesh_adj_get_gradient": (ctypes.c_int, [P, i32, P, i64]),
+        "lulesh_adj_set_overlap": (ctypes.c_int, [P, i32]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -569,6 +570,12 @@ class Adjoint:
 
     def clear_seeds(self):
         _check(self._L.lulesh_adj_clear_seeds(self._h), "clear seeds")
+
+    def set_overlap(self, enable):
+        """Overlap each segment's recompute with the next segment's transpose
+        (two tapes; the default) or run them in turn on one tape. Raises if
+        the second tape does not fit."""
+        _check(self._L.lulesh_adj_set_overlap(self._h, 1 if enable else 0), "overlap")
 
     def loss(self):
         x = ctypes.c_double()

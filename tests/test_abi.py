@@ -56,6 +56,7 @@ def test_calls_that_need_no_gpu(gpu_lib):
     p.nx, p.mode = 8, 9
     assert L.lulesh_create(ctypes.byref(p), ctypes.byref(h)) == 6
     assert L.lulesh_destroy(None) == 6
+    assert L.lulesh_adj_set_overlap(None, 1) == 6
 
 
 def test_python_ids_match_header(gpu_lib):

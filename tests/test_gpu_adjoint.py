@@ -179,6 +179,46 @@ def test_checkpoint_interval_and_final_state(gpu_lib):
             assert np.array_equal(other[2][f], grads[0][2][f]), f
 
 
+@pytest.mark.parametrize("stop_early", [False, True])
+def test_overlapped_and_sequential_sweeps_agree(gpu_lib, stop_early):
+    """The reverse sweep that recomputes one segment while it transposes the
+    next (two tapes) gives bitwise the gradients of the sequential sweep (one
+    tape): 27 cycles in segments of 7 (a partial last one), and a run that
+    reaches stoptime after about 17 cycles (its last segment recomputed, not
+    taped during the forward sweep)."""
+    L = gpu_lib
+    nx, cycles, every = 8, 27, 7
+    g = developed(L, nx, 0, 0, 0xC7)
+    snap = snapshot(g)
+    stoptime = g.stoptime
+    if stop_early:
+        ref = L.Domain(L.LuleshProblem(nx=nx))
+        restore(ref, snap)
+        for _ in range(17):
+            L.timeIncrement(ref)
+            L.lagrangeLeapFrog(ref)
+        stoptime = ref.time
+    out = []
+    for overlap in (True, False, True):
+        restore(g, snap)
+        g.stoptime = stoptime
+        adj = L.Adjoint(g, checkpoint_every=every)
+        adj.set_overlap(overlap)
+        loss = adj.gradient(cycles)
+        if stop_early:
+            assert 17 <= adj.result.cycles < cycles
+        else:
+            assert adj.result.cycles == cycles and adj.result.checkpoints == 4
+        out.append((loss, adj.result.grad_hgcoef, {f: adj.grad(f) for f in STATE},
+                    {f: g.field(f) for f in STATE}))
+        adj.close()
+    for other in out[1:]:
+        assert other[0] == out[0][0] and other[1] == out[0][1]
+        for f in STATE:
+            assert np.array_equal(other[2][f], out[0][2][f]), f
+            assert np.array_equal(other[3][f], out[0][3][f]), f
+
+
 def test_gradient_matches_central_fd(gpu_lib):
     L = gpu_lib
     nx, cycles, h = 12, 40, 1e-6
