@@ -487,7 +487,10 @@ def run_ours(args):
     force_bytes = FORCE_BYTES_PER_ELEM * E + FORCE_BYTES_PER_NODE * N
     achieved = force_bytes / (force_ms * 1e-3) / 1e9
     prof = _profile_numbers()
-    traffic = prof.get("dram_bytes_per_launch") if prof else None
+    # the committed capture's per-launch figures are of the 150^3 problem
+    # (3,375,000 elements); both grow with the elements of the run's problem
+    prof_scale = E / 3375000.0
+    traffic = prof["dram_bytes_per_launch"] * prof_scale if prof and prof.get("dram_bytes_per_launch") else None
     roofline = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
@@ -496,10 +499,11 @@ def run_ours(args):
     step_gbs = step_bytes * cycles / (ms * 1e-3) / 1e9
     fp64 = {"bound": "fp64", "peak_fma_per_s": fma_s.value, "peak_add_per_s": add_s.value,
             "peak_source": "lulesh_measure_fp64_peak (this run, this GPU)"}
-    if prof and prof.get("fp64_inst_per_launch"):
-        rate = prof["fp64_inst_per_launch"] / (force_ms * 1e-3)
+    if prof and prof.get("fp64_inst_per_element"):
+        inst = prof["fp64_inst_per_element"] * E
+        rate = inst / (force_ms * 1e-3)
         fp64.update({"kernel": "k_force", "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
-                     "fp64_inst_per_launch": prof["fp64_inst_per_launch"]})
+                     "fp64_inst_per_launch": inst, "fp64_inst_per_element": prof["fp64_inst_per_element"]})
 
     g.close()  # the remaining legs build their own problems
     c3 = None
