@@ -859,33 +859,47 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
       hvp(U, d61, d50, dU, gd(6, 1), gd(5, 0), 1, 4, 2, 5, 6, 1, 5, 0);
     }
   }
-  // stress part: f = s8 * B with B the sum of the node's three face cross products
+  // stress part: f = s8 * B. The forward forms B0..B3 from faces 0-4 (node
+  // n's three face cross products) and the opposite corners as B6 = -B0,
+  // B7 = -B1, B4 = -B2, B5 = -B3 (the face normals of a closed surface sum to
+  // zero), so face 5 carries no adjoint.
   {
     const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
     const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
-    constexpr int nf[8][3] = {{0, 1, 4}, {0, 1, 2}, {0, 2, 3}, {0, 3, 4},
-                              {1, 4, 5}, {1, 2, 5}, {2, 3, 5}, {3, 4, 5}};
-    // face normals (the forward's cross products, from the tape)
-    V3 N[6];
+    // face normals 0..4 (the forward's cross products, from the tape)
+    V3 N[5];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) N[f] = v3(a.geo[(48 + f) * E + e], a.geo[(54 + f) * E + e], a.geo[(60 + f) * E + e]);
-    // sum_n lf_n . B_n = sum_f N_f . LU_f with LU_f the sum of lf over the
-    // face's nodes (node 1's quirk included); the normals' adjoints are s8 LU_f
-    V3 LU[6] = {v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0), v3(0, 0, 0)};
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      const V3 lf = v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]);
-      if (n == 0 && !(MODE & 1)) {
-        // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice and no areaZ
-        vadd(LU[0], lf); vadd(LU[1], lf);
-        LU[4].x += lf.x; LU[4].y = fma(2.0, lf.y, LU[4].y);
-      } else {
-        vadd(LU[nf[n][0]], lf); vadd(LU[nf[n][1]], lf); vadd(LU[nf[n][2]], lf);
-      }
+    for (int f = 0; f < 5; ++f) N[f] = v3(a.geo[(48 + f) * E + e], a.geo[(54 + f) * E + e], a.geo[(60 + f) * E + e]);
+    auto lfv = [&](int n) { return v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]); };
+    // w_n = lf_n - lf_opposite(n) for the corners 0..3 (opposites 6, 7, 4, 5)
+    const V3 lf0 = lfv(0);
+    V3 w0 = lf0, w1 = lfv(1), w2 = lfv(2), w3 = lfv(3);
+    {
+      const V3 o0 = lfv(6), o1 = lfv(7), o2 = lfv(4), o3 = lfv(5);
+      w0.x -= o0.x; w0.y -= o0.y; w0.z -= o0.z;
+      w1.x -= o1.x; w1.y -= o1.y; w1.z -= o1.z;
+      w2.x -= o2.x; w2.y -= o2.y; w2.z -= o2.z;
+      w3.x -= o3.x; w3.y -= o3.y; w3.z -= o3.z;
+    }
+    // sum_n lf_n . B_n = sum_f N_f . LU_f: corners 0..3 touch faces
+    // {0,1,4} {0,1,2} {0,2,3} {0,3,4}
+    V3 w01 = w0; vadd(w01, w1);
+    V3 w23 = w2; vadd(w23, w3);
+    V3 LU[5];
+    LU[0] = w01; vadd(LU[0], w23);
+    LU[1] = w01;
+    LU[2] = w1; vadd(LU[2], w2);
+    LU[3] = w23;
+    LU[4] = w0; vadd(LU[4], w3);
+    if (!(MODE & 1)) {
+      // src/domain.jl:1050-1055: node 1 (corner 0) takes face 5's areaY twice
+      // and no areaZ; its opposite corner has the plain sum
+      LU[4].y += lf0.y;
+      LU[4].z -= lf0.z;
     }
     double Ls8 = 0.0;
 #pragma unroll
-    for (int f = 0; f < 6; ++f) Ls8 += vdot(N[f], LU[f]);
+    for (int f = 0; f < 5; ++f) Ls8 += vdot(N[f], LU[f]);
     const double Lpq = -0.125 * Ls8;
     a.lp[e] += Lpq;
     a.lq[e] += Lpq;
@@ -900,7 +914,6 @@ __global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
     face_t(2, d61, d25, 6, 1, 2, 5);
     face_t(3, d72, d36, 7, 2, 3, 6);
     face_t(4, d43, d07, 4, 3, 0, 7);
-    face_t(5, d64, d57, 6, 4, 5, 7);
   }
 #pragma unroll
   for (int k = 0; k < 3; ++k)

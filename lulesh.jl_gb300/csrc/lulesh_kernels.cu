@@ -91,12 +91,16 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
 
   // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
   // face-diagonal cross products; true B = -Bc/8. The face normals are scaled
-  // by s8 here, so Bx..Bz hold the stress forces s8*Bc.
+  // by s8 here, so Bx..Bz hold the stress forces s8*Bc. The six face normals
+  // are the area vectors of a closed surface and sum to zero, and opposite
+  // corners touch complementary faces (node 0: faces 0,1,4; node 6: 2,3,5),
+  // so B6 = -B0, B7 = -B1, B4 = -B2, B5 = -B3 and face 5's normal is not
+  // needed (the taping variant still forms it for the transpose).
   double Bx[8], By[8], Bz[8];
   {
     double nx[6], ny[6], nz[6];
 #pragma unroll
-    for (int f = 0; f < 6; ++f) {
+    for (int f = 0; f < (TAPE ? 6 : 5); ++f) {
       const double* d1 = g[2 * f];
       const double* d2 = g[2 * f + 1];
       cross(d1[0], d1[1], d1[2], d2[0], d2[1], d2[2], nx[f], ny[f], nz[f]);
@@ -108,19 +112,21 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
       nx[f] *= s8; ny[f] *= s8; nz[f] *= s8;
     }
     // node -> its three faces (faces numbered 0..5 = reference faces 1..6)
-    Bx[0] = (nx[0] + nx[1]) + nx[4]; By[0] = (ny[0] + ny[1]) + ny[4]; Bz[0] = (nz[0] + nz[1]) + nz[4];
+    const double px01 = nx[0] + nx[1], py01 = ny[0] + ny[1], pz01 = nz[0] + nz[1];
+    Bx[0] = px01 + nx[4]; By[0] = py01 + ny[4]; Bz[0] = pz01 + nz[4];
+    Bx[1] = px01 + nx[2]; By[1] = py01 + ny[2]; Bz[1] = pz01 + nz[2];
+    Bx[2] = (nx[0] + nx[2]) + nx[3]; By[2] = (ny[0] + ny[2]) + ny[3]; Bz[2] = (nz[0] + nz[2]) + nz[3];
+    Bx[3] = (nx[0] + nx[3]) + nx[4]; By[3] = (ny[0] + ny[3]) + ny[4]; Bz[3] = (nz[0] + nz[3]) + nz[4];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) {
+      const int o = n < 2 ? n + 6 : n + 2;  // the opposite corner
+      Bx[o] = -Bx[n]; By[o] = -By[n]; Bz[o] = -Bz[n];
+    }
     if (!(MODE & 1)) {
       // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice, no areaZ
       By[0] = By[0] + ny[4];
-      Bz[0] = nz[0] + nz[1];
+      Bz[0] = pz01;
     }
-    Bx[1] = (nx[0] + nx[1]) + nx[2]; By[1] = (ny[0] + ny[1]) + ny[2]; Bz[1] = (nz[0] + nz[1]) + nz[2];
-    Bx[2] = (nx[0] + nx[2]) + nx[3]; By[2] = (ny[0] + ny[2]) + ny[3]; Bz[2] = (nz[0] + nz[2]) + nz[3];
-    Bx[3] = (nx[0] + nx[3]) + nx[4]; By[3] = (ny[0] + ny[3]) + ny[4]; Bz[3] = (nz[0] + nz[3]) + nz[4];
-    Bx[4] = (nx[1] + nx[4]) + nx[5]; By[4] = (ny[1] + ny[4]) + ny[5]; Bz[4] = (nz[1] + nz[4]) + nz[5];
-    Bx[5] = (nx[1] + nx[2]) + nx[5]; By[5] = (ny[1] + ny[2]) + ny[5]; Bz[5] = (nz[1] + nz[2]) + nz[5];
-    Bx[6] = (nx[2] + nx[3]) + nx[5]; By[6] = (ny[2] + ny[3]) + ny[5]; Bz[6] = (nz[2] + nz[3]) + nz[5];
-    Bx[7] = (nx[3] + nx[4]) + nx[5]; By[7] = (ny[3] + ny[4]) + ny[5]; Bz[7] = (nz[3] + nz[4]) + nz[5];
   }
 
   // calcElemVolumeDerivative (src/domain.jl:1178-1256), times 12: its eight
