@@ -28,7 +28,9 @@ typedef enum {
   LULESH_ERR_CUDA = 4,       /* a CUDA runtime call failed */
   LULESH_ERR_TIMEOUT = 5,    /* a bounded device wait ran out */
   LULESH_ERR_ARGUMENT = 6,   /* bad argument (null pointer, unknown id, size mismatch) */
-  LULESH_ERR_MEMORY = 7      /* device allocation failed */
+  LULESH_ERR_MEMORY = 7,     /* device allocation failed */
+  LULESH_ERR_INDEX = 8       /* a build with -DLULESH_CHECK met an index outside its range
+                                (the access was skipped); never raised by a normal build */
 } lulesh_status;
 
 /* Which reference check raised a LULESH_ERR_VOLUME (finer than the code). */

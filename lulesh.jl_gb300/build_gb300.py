@@ -41,26 +41,31 @@ def _run(cmd):
     return r.stderr
 
 
-def build(verbose=False):
+def build(verbose=False, defines=(), lib=LIB):
+    """Builds the library at `lib` (objects in a _build folder beside it
+    unless it is the in-tree default). `defines` adds -D macros, e.g.
+    ("LULESH_CHECK",) for the index-checked debug build."""
     nvcc = _nvcc()
-    os.makedirs(OBJ, exist_ok=True)
-    os.makedirs(LIB_DIR, exist_ok=True)
+    obj = OBJ if lib == LIB else os.path.join(os.path.dirname(os.path.abspath(lib)), "_build")
+    os.makedirs(obj, exist_ok=True)
+    os.makedirs(os.path.dirname(os.path.abspath(lib)), exist_ok=True)
+    dflags = ["-D" + m for m in defines]
     cu, cpp = _sources()
     jobs = []
     for f in cu:
-        o = os.path.join(OBJ, f + ".o")
-        jobs.append([nvcc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, f), "-o", o])
+        o = os.path.join(obj, f + ".o")
+        jobs.append([nvcc] + ARCH + NVCC_FLAGS + dflags + ["-c", os.path.join(CSRC, f), "-o", o])
     for f in cpp:
-        o = os.path.join(OBJ, f + ".o")
-        jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off",
-                     "-c", os.path.join(CSRC, f), "-o", o])
+        o = os.path.join(obj, f + ".o")
+        jobs.append([os.environ.get("CXX", "g++"), "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off"] + dflags +
+                    ["-c", os.path.join(CSRC, f), "-o", o])
     with ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
         for msg in ex.map(_run, jobs):
             if verbose and msg:
                 print(msg)
-    objs = [os.path.join(OBJ, f + ".o") for f in cu + cpp]
-    _run([nvcc] + ARCH + ["-shared", "-o", LIB] + objs)
-    return LIB
+    objs = [os.path.join(obj, f + ".o") for f in cu + cpp]
+    _run([nvcc] + ARCH + ["-shared", "-o", lib] + objs)
+    return lib
 
 
 if __name__ == "__main__":

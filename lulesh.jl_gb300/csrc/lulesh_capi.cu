@@ -71,6 +71,7 @@ void lulesh::decode_status(unsigned bits, int32_t* status, int32_t* site) {
   *status = LULESH_OK;
   *site = LULESH_SITE_NONE;
   if (!bits) return;
+  if (bits & ST_INDEX) { *status = LULESH_ERR_INDEX; return; }
   if (bits & ST_EARLY) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_EARLY; return; }
   if (bits & ST_HOURGLASS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_HOURGLASS; return; }
   if (bits & ST_KINEMATICS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_KINEMATICS; return; }
@@ -255,6 +256,7 @@ const char* lulesh_status_string(int32_t status) {
     case LULESH_ERR_TIMEOUT: return "device wait timed out";
     case LULESH_ERR_ARGUMENT: return "bad argument";
     case LULESH_ERR_MEMORY: return "device allocation failed";
+    case LULESH_ERR_INDEX: return "index out of range (checked build)";
     default: return "unknown status";
   }
 }

@@ -34,6 +34,17 @@ namespace lulesh {
 
 #define LDG(p) __ldg(p)
 
+// Index guard of the checked build (-DLULESH_CHECK, a debug build the tests
+// run small cases with): an index outside [0, n) records ST_INDEX in the
+// problem's status word and is replaced by 0, so the access stays in bounds.
+// A normal build passes the index through.
+#ifdef LULESH_CHECK
+#define LULESH_IDX(i, n, st) \
+  (((unsigned)(i) < (unsigned)(n)) ? (i) : (atomicOr(&(st)->status, ST_INDEX), 0))
+#else
+#define LULESH_IDX(i, n, st) (i)
+#endif
+
 // gamma[n][m] of calcFBHourglassForceForElems, src/domain.jl:1490-1499.
 __device__ __forceinline__ double gamma_nm(int n, int m) {
   // column m is the Walsh function eta*zeta, xi*zeta, xi*eta, xi*eta*zeta

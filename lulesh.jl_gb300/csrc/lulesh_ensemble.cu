@@ -24,6 +24,7 @@
 #include "../../include/lulesh_gb300.h"
 #include "lulesh_arena.h"
 #include "lulesh_device.cuh"
+#include "lulesh_handle.h"
 #include "lulesh_internal.h"
 #include "lulesh_kernels.h"
 #include "lulesh_setup.h"
@@ -55,18 +56,7 @@ Params reference_params() {
   return p;
 }
 
-void decode(unsigned bits, int32_t* status, int32_t* site) {
-  *status = LULESH_OK;
-  *site = LULESH_SITE_NONE;
-  if (!bits) return;
-  if (bits & ST_EARLY) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_EARLY; }
-  else if (bits & ST_HOURGLASS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_HOURGLASS; }
-  else if (bits & ST_KINEMATICS) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_KINEMATICS; }
-  else if (bits & ST_BAD_BC) *status = LULESH_ERR_BAD_BC;
-  else if (bits & ST_QSTOP) *status = LULESH_ERR_QSTOP;
-  else if (bits & ST_MATERIAL) { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_MATERIAL; }
-  else { *status = LULESH_ERR_VOLUME; *site = LULESH_SITE_UPDATE; }
-}
+void decode(unsigned bits, int32_t* status, int32_t* site) { lulesh::decode_status(bits, status, site); }
 
 // The mutable per-run fields, snapshotted at creation for reset().
 struct Mutable {

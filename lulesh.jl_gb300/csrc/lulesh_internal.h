@@ -27,6 +27,7 @@ enum : uint32_t {
   ST_QSTOP = 1u << 4,       // q > qstop, src/domain.jl:2567-2580
   ST_MATERIAL = 1u << 5,    // clamped v <= 0, src/domain.jl:2905
   ST_UPDATE = 1u << 6,      // new v <= 0, src/domain.jl:2926
+  ST_INDEX = 1u << 7,       // checked build (LULESH_CHECK): an index outside its range
 };
 
 // Which value a monotonic-Q limiter returned (src/domain.jl:2357-2376).

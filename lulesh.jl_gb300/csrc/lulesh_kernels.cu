@@ -34,14 +34,14 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
-  const int inst = ENS ? LDG(&d.elemInst[e]) : 0;
+  const int inst = ENS ? LULESH_IDX(LDG(&d.elemInst[e]), d.ninst, d.st) : 0;
   DevState* const st = d.st + inst;
   if (step_off(st)) return;
   const double hgcoef = ENS ? LDG(&d.instHg[inst]) : prm.hgcoef;
 
   int nd[8];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) nd[c] = LDG(&d.nodelist[c * E + e]);
+  for (int c = 0; c < 8; ++c) nd[c] = LULESH_IDX(LDG(&d.nodelist[c * E + e]), d.N, st);
   double x[8], y[8], z[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
@@ -258,16 +258,21 @@ template <bool AUX, bool ENS>
 __global__ void __launch_bounds__(kMaxNodeBlock) k_node(DevDomain d, Params prm) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= d.N) return;
-  const DevState* st = d.st + (ENS ? LDG(&d.nodeInst[i]) : 0);
+  DevState* const st = d.st + (ENS ? LULESH_IDX(LDG(&d.nodeInst[i]), d.ninst, d.st) : 0);
   if (step_off(st)) return;
   const double dt = st->deltatime;
-  const int s = LDG(&d.nodeElemStart[i]), t = LDG(&d.nodeElemStart[i + 1]);
+  const int s = LDG(&d.nodeElemStart[i]);
+  int t = LDG(&d.nodeElemStart[i + 1]);
+#ifdef LULESH_CHECK
+  // the node's corner range must lie within [0, 8E]; an empty one reads nothing
+  if (s < 0 || t < s || t > 8 * d.E) { atomicOr(&st->status, ST_INDEX); t = s; }
+#endif
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (s < t) {
-    const int c0 = LDG(&d.cornerList[s]);
+    const int c0 = LULESH_IDX(LDG(&d.cornerList[s]), 8 * d.E, st);
     fx = LDG(&d.fcx[c0]); fy = LDG(&d.fcy[c0]); fz = LDG(&d.fcz[c0]);
     for (int j = s + 1; j < t; ++j) {
-      const int c = LDG(&d.cornerList[j]);
+      const int c = LULESH_IDX(LDG(&d.cornerList[j]), 8 * d.E, st);
       fx += LDG(&d.fcx[c]); fy += LDG(&d.fcy[c]); fz += LDG(&d.fcz[c]);
     }
   }
@@ -301,13 +306,13 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
-  DevState* const st = d.st + (ENS ? LDG(&d.elemInst[e]) : 0);
+  DevState* const st = d.st + (ENS ? LULESH_IDX(LDG(&d.elemInst[e]), d.ninst, d.st) : 0);
   if (step_off(st)) return;
   const double dt = st->deltatime;
 
   int nd[8];
 #pragma unroll
-  for (int c = 0; c < 8; ++c) nd[c] = LDG(&d.nodelist[c * E + e]);
+  for (int c = 0; c < 8; ++c) nd[c] = LULESH_IDX(LDG(&d.nodelist[c * E + e]), d.N, st);
   double x[8], y[8], z[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
@@ -616,10 +621,10 @@ template <int MODE, bool AUX, bool ENS, bool TAPE, bool REGION>
 __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params prm) {
   const int E = d.E;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  const int i = REGION ? (t < E ? LDG(&d.regOrder[t]) : E) : t;
+  const int i = REGION ? (t < E ? LULESH_IDX(LDG(&d.regOrder[t]), E, d.st) : E) : t;
   // every thread of the block takes part in the dt reduction
   unsigned long long courant = kInfBits, hydro = kInfBits;
-  const int inst = (ENS && i < E) ? LDG(&d.elemInst[i]) : 0;
+  const int inst = (ENS && i < E) ? LULESH_IDX(LDG(&d.elemInst[i]), d.ninst, d.st) : 0;
   DevState* const st = d.st + inst;
   const bool live = (i < E) && !step_off(st);
   if (live) {

@@ -219,6 +219,27 @@ def test_error_stops_device_run(gpu_lib):
     assert g.cycle == 11  # the failing cycle's timeIncrement ran, nothing after
 
 
+# ---- smallest meshes: every element on the boundary ------------------------------
+
+@pytest.mark.parametrize("nx", [1, 2, 3])
+@pytest.mark.parametrize("mode", [0, 7])
+def test_tiny_meshes_match_oracle(gpu_lib, oracle_mod, nx, mode):
+    """nx = 1 (one element, eight nodes, every face on a symmetry plane or free
+    surface) to 3, stepwise to stoptime with the auxiliary fields."""
+    g, o = pair(gpu_lib, oracle_mod, nx, mode=mode, keep_aux=True)
+    steps = 0
+    while o.get("time") < o.get("stoptime") and steps < 100:
+        gpu_lib.timeIncrement(g)
+        o.time_increment()
+        gpu_lib.lagrangeLeapFrog(g)
+        assert o.lagrange_leapfrog() == 0
+        assert_scalars(g, o)
+        assert_fields(g, o, STATE_F64, tol=1e-10, where=f"step {steps}")
+        assert_fields(g, o, STEP_F64 + AUX_F64, where=f"step {steps}")
+        steps += 1
+    assert o.get("time") >= o.get("stoptime") and g.time == pytest.approx(o.get("time"), rel=1e-12)
+
+
 # ---- full-size checks -----------------------------------------------------------
 
 def test_full_size_s150_matches_oracle(gpu_lib, oracle_mod):
@@ -239,3 +260,19 @@ def test_full_size_s150_is_deterministic(gpu_lib):
         assert np.array_equal(a.field(n), b.field(n)), n
     a.close()
     b.close()
+
+
+def test_largest_configuration_matches_oracle(gpu_lib, oracle_mod):
+    """The unbalanced-regions problem at its full size (256^3 = 16.8 M
+    elements, 11 regions, balance 4, cost 2) for 2 cycles, with the region
+    cost model on in the GPU run (results unchanged by it)."""
+    L = gpu_lib
+    g = L.Domain(L.LuleshProblem(nx=256, nr=11, balance=4, cost=2, region_reps=True))
+    o = oracle_mod.OracleDomain(256, nr=11, balance=4, cost=2)
+    for n in ["regNumList", "regElemSize", "regReps"]:
+        assert np.array_equal(g.field(n), o.field(n)), n
+    L.run(g, 2)
+    assert o.run(2) == 0
+    assert_scalars(g, o)
+    assert_fields(g, o, STATE_F64 + ["vdov", "arealg"])
+    g.close()
