@@ -96,7 +96,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   // corners touch complementary faces (node 0: faces 0,1,4; node 6: 2,3,5),
   // so B6 = -B0, B7 = -B1, B4 = -B2, B5 = -B3 and face 5's normal is not
   // needed (the taping variant still forms it for the transpose).
-  double Bx[8], By[8], Bz[8];
+  double Bx[4], By[4], Bz[4];  // corners 0..3; corner 6, 7, 4, 5 is minus corner 0, 1, 2, 3
+  double b6y, b6z;             // corner 0's y and z before its quirk (corner 6 is minus them)
   {
     double nx[6], ny[6], nz[6];
 #pragma unroll
@@ -117,17 +118,21 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     Bx[1] = px01 + nx[2]; By[1] = py01 + ny[2]; Bz[1] = pz01 + nz[2];
     Bx[2] = (nx[0] + nx[2]) + nx[3]; By[2] = (ny[0] + ny[2]) + ny[3]; Bz[2] = (nz[0] + nz[2]) + nz[3];
     Bx[3] = (nx[0] + nx[3]) + nx[4]; By[3] = (ny[0] + ny[3]) + ny[4]; Bz[3] = (nz[0] + nz[3]) + nz[4];
-#pragma unroll
-    for (int n = 0; n < 4; ++n) {
-      const int o = n < 2 ? n + 6 : n + 2;  // the opposite corner
-      Bx[o] = -Bx[n]; By[o] = -By[n]; Bz[o] = -Bz[n];
-    }
+    b6y = By[0]; b6z = Bz[0];
     if (!(MODE & 1)) {
       // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice, no areaZ
       By[0] = By[0] + ny[4];
       Bz[0] = pz01;
     }
   }
+  // s8*Bc of corner n, component k (n and k are constants after unrolling, so
+  // the sign folds into the instruction that consumes it)
+  auto bstress = [&](int k, int n) -> double {
+    const double* b = k == 0 ? Bx : k == 1 ? By : Bz;
+    if (n < 4) return b[n];
+    if (n == 6) return -(k == 0 ? Bx[0] : k == 1 ? b6y : b6z);
+    return -b[n == 4 ? 2 : n == 5 ? 3 : 1];
+  };
 
   // calcElemVolumeDerivative (src/domain.jl:1178-1256), times 12: its eight
   // voluDer calls are the gradient of 12*volume, and 12*volume is
@@ -218,7 +223,6 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     // calcElemFBHourglassForce (src/domain.jl:1258-1460), one velocity
     // component at a time to bound register use.
     const double* vel[3] = {d.xd, d.yd, d.zd};
-    const double* Bc[3] = {Bx, By, Bz};
     double* fo[3] = {fx, fy, fz};
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -236,12 +240,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
       }
 #pragma unroll
       for (int n = 0; n < 8; ++n) {
-        fo[k][n] = fma(hg[n][0], h[0], fma(hg[n][1], h[1], fma(hg[n][2], h[2], fma(hg[n][3], h[3], Bc[k][n]))));
+        fo[k][n] = fma(hg[n][0], h[0], fma(hg[n][1], h[1], fma(hg[n][2], h[2], fma(hg[n][3], h[3], bstress(k, n)))));
       }
     }
   } else {
 #pragma unroll
-    for (int n = 0; n < 8; ++n) { fx[n] = Bx[n]; fy[n] = By[n]; fz[n] = Bz[n]; }
+    for (int n = 0; n < 8; ++n) { fx[n] = bstress(0, n); fy[n] = bstress(1, n); fz[n] = bstress(2, n); }
   }
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
