@@ -50,24 +50,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     z[c] = LDG(&d.z[nd[c]]);
   }
 
-  // Walsh coefficients: W1 = Jacobian columns (xi, eta, zeta), HM = modes.
-  double wx[3], wy[3], wz[3], hmx[4], hmy[4], hmz[4];
-  walsh7(x, wx, hmx);
-  walsh7(y, wy, hmy);
-  walsh7(z, wz, hmz);
-
-  // integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
-  // sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
-  {
-    const double cxet = fma(wz[0], wy[2], -(wy[0] * wz[2]));
-    const double cyet = fma(wx[0], wz[2], -(wz[0] * wx[2]));
-    const double czet = fma(wy[0], wx[2], -(wx[0] * wy[2]));
-    const double det = fma(wx[1], cxet, fma(wy[1], cyet, wz[1] * czet));
-    if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
-  }
-
   // The 12 face diagonals (two per face, in calcElemNodeNormals' argument
-  // order p2 - p0, p3 - p1) serve the node normals and the volume derivatives.
+  // order p2 - p0, p3 - p1) serve the node normals, the volume derivatives
+  // and three of the four hourglass modes.
   // Face f: (2,0,3,1) (5,0,1,4) (6,1,2,5) (7,2,3,6) (4,3,0,7) (6,4,5,7).
   double g[12][3];
   {
@@ -84,6 +69,45 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
         d.tapeGeo[(68 + 3 * q) * E + e] = g[q][2];
       }
     }
+  }
+
+  // Walsh coefficients: W1 = Jacobian columns (xi, eta, zeta), HM = the
+  // hourglass modes (eta*zeta, xi*zeta, xi*eta, xi*eta*zeta). Face diagonals
+  // join corners of one parity, so the three even modes are sums of four
+  // of them: eta*zeta = (d64 - d57) - (d20 + d31), xi*zeta = (d07 + d61) -
+  // (d43 + d25), xi*eta = (d07 + d61) + (d43 + d25); W1 and xi*eta*zeta come
+  // from the four body diagonals a = p6 - p0, b = p5 - p3, c = p7 - p1,
+  // d = p4 - p2: (a+b) - (c+d), (a-b) + (c-d), (a+b) + (c+d) and
+  // (a-b) - (c-d). 19 adds per coordinate instead of a 23-add butterfly.
+  double wx[3], wy[3], wz[3], hmx[4], hmy[4], hmz[4];
+  {
+    const double* P[3] = {x, y, z};
+    double* W[3] = {wx, wy, wz};
+    double* H[3] = {hmx, hmy, hmz};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      const double* v = P[k];
+      const double a = v[6] - v[0], b = v[5] - v[3], c = v[7] - v[1], dd = v[4] - v[2];
+      const double apb = a + b, cpd = c + dd, amb = a - b, cmd = c - dd;
+      W[k][0] = apb - cpd;
+      W[k][1] = amb + cmd;
+      W[k][2] = apb + cpd;
+      H[k][3] = amb - cmd;
+      H[k][0] = (g[10][k] - g[11][k]) - (g[0][k] + g[1][k]);
+      const double pp = g[9][k] + g[4][k], qq = g[8][k] + g[5][k];
+      H[k][1] = pp - qq;
+      H[k][2] = pp + qq;
+    }
+  }
+
+  // integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
+  // sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
+  {
+    const double cxet = fma(wz[0], wy[2], -(wy[0] * wz[2]));
+    const double cyet = fma(wx[0], wz[2], -(wz[0] * wx[2]));
+    const double czet = fma(wy[0], wx[2], -(wx[0] * wy[2]));
+    const double det = fma(wx[1], cxet, fma(wy[1], cyet, wz[1] * czet));
+    if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
   }
 
   // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
@@ -166,14 +190,16 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     double gr[8][3];
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
+      // corners 1 and 2, 3 and 7, 4 and 5 share a difference of the U gradients
+      const double t12 = gU[2][k] - gU[0][k], t37 = gU[0][k] - gU[1][k], t45 = gU[1][k] - gU[2][k];
       gr[0][k] = -((gW[0][k] + gW[1][k]) + gW[2][k]);
-      gr[1][k] = (gU[2][k] - gU[0][k]) - gV[2][k];
-      gr[2][k] = (gW[0][k] - gU[0][k]) + gU[2][k];
-      gr[3][k] = (gU[0][k] - gV[0][k]) - gU[1][k];
-      gr[4][k] = (gU[1][k] - gV[1][k]) - gU[2][k];
-      gr[5][k] = (gU[1][k] - gU[2][k]) + gW[2][k];
+      gr[1][k] = t12 - gV[2][k];
+      gr[2][k] = t12 + gW[0][k];
+      gr[3][k] = t37 - gV[0][k];
+      gr[4][k] = t45 - gV[1][k];
+      gr[5][k] = t45 + gW[2][k];
       gr[6][k] = (gV[0][k] + gV[1][k]) + gV[2][k];
-      gr[7][k] = (gU[0][k] - gU[1][k]) + gW[1][k];
+      gr[7][k] = t37 + gW[1][k];
     }
 #pragma unroll
     for (int n = 0; n < 8; ++n) {
