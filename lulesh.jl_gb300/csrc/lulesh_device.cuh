@@ -11,7 +11,11 @@
 //    diagonals; power-of-two scale factors (0.125, 0.25, 8) are dropped where
 //    they cancel or only scale a sign test, which is exact;
 //  * the hourglass modes x8n*gamma (src/domain.jl:1510-1525) are the
-//    second/third-order Walsh coefficients, found by a 3-stage butterfly;
+//    second/third-order Walsh coefficients, found by a 3-stage butterfly or,
+//    where the face diagonals exist anyway, as sums of four of them (face
+//    diagonals join corners of one parity) plus the body diagonals;
+//  * the node normals of a corner and its opposite corner are negatives of
+//    each other (the face normals of a closed surface sum to zero);
 //  * a face's area vector (sumElemFaceNormal, src/domain.jl:971-989) is
 //    -(d1 x d2)/8 for the face's two diagonals d1, d2;
 //  * voluDer (src/domain.jl:1178-1211) only ever sums the 12 hex edges, so
