@@ -151,16 +151,46 @@ __device__ __forceinline__ double inv_cbrt(double x) {
   return fma(y0, e * fma(e, 2.0 / 9.0, 1.0 / 3.0), y0);
 }
 
-// 1/a, 1/b, 1/c from one division: r = 1/(a b c), 1/c = r (a b),
-// 1/a = (r c) b, 1/b = (r c) a. For a, b, c > 0 whose product is a normal
-// double; each result is within a few ulps of the quotient.
-__device__ __forceinline__ void recip3(double a, double b, double c, double& ia, double& ib, double& ic) {
+// True when |v| is a normal finite double (exponent field neither 0 nor all
+// ones), tested on the integer pipe.
+__device__ __forceinline__ bool normal_finite(double v) {
+  const unsigned long long m = (unsigned long long)__double_as_longlong(v) & 0x7FFFFFFFFFFFFFFFull;
+  return m - 0x0010000000000000ull < 0x7FE0000000000000ull;
+}
+
+// 1/a and 1/b from one division, r = 1/(a b): 1/a = r b, 1/b = r a; the
+// two quotients one by one when a b is not a normal finite double.
+__device__ __forceinline__ void recip2(double a, double b, double& ia, double& ib) {
   const double ab = a * b;
-  const double r = 1.0 / (ab * c);
-  const double rc = r * c;
-  ic = r * ab;
-  ia = rc * b;
-  ib = rc * a;
+  if (normal_finite(ab)) {
+    const double r = 1.0 / ab;
+    ia = r * b;
+    ib = r * a;
+  } else {
+    ia = 1.0 / a;
+    ib = 1.0 / b;
+  }
+}
+
+// 1/a, 1/b, 1/c from one division: r = 1/(a b c), 1/c = r (a b),
+// 1/a = (r c) b, 1/b = (r c) a; each result is within a few ulps of the
+// quotient. When a b or a b c is not a normal finite double (a state far
+// outside the physical ranges, or a zero operand) the three quotients are
+// formed one by one, so the results are those of the divisions. The range
+// test runs on the integer pipe.
+__device__ __forceinline__ void recip3(double a, double b, double c, double& ia, double& ib, double& ic) {
+  const double ab = a * b, abc = ab * c;
+  if (normal_finite(ab) && normal_finite(abc)) {
+    const double r = 1.0 / abc;
+    const double rc = r * c;
+    ic = r * ab;
+    ia = rc * b;
+    ib = rc * a;
+  } else {
+    ia = 1.0 / a;
+    ib = 1.0 / b;
+    ic = 1.0 / c;
+  }
 }
 
 // timeIncrement!, src/domain.jl:920-961, shared by the host API and the

@@ -480,11 +480,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     const double d1 = fma(Cxxi, vxw[0], fma(Cxet, vxw[1], Cxze * vxw[2]));
     const double d2 = fma(Cyxi, vyw[0], fma(Cyet, vyw[1], Cyze * vyw[2]));
     const double d3 = fma(Czxi, vzw[0], fma(Czet, vzw[1], Czze * vzw[2]));
-    {
-      const double r = 1.0 / (det * q64);
-      inv = r * q64;
-      norm64 = r * det;
-    }
+    recip2(det, q64, inv, norm64);
     const double vdov = ((d1 + d2) + d3) * inv;
     d.vdov[e] = vdov;
     if (TAPE) {
@@ -670,17 +666,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
     double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
     double tl[9];  // limiter terms per direction: norm, dm/norm, dp/norm (TAPE)
-    // the three 1/(delv + ptiny) from one division: r = 1/(sx sy sz)
+    // the three 1/(delv + ptiny) from one division
     double inx, iny, inz;
-    {
-      const double sx = dvxi + 1.e-36, sy = dveta + 1.e-36, sz = dvzeta + 1.e-36;
-      const double sxy = sx * sy;
-      const double r = 1.0 / (sxy * sz);
-      const double rz = r * sz;  // 1/(sx sy)
-      inz = r * sxy;
-      inx = rz * sy;
-      iny = rz * sx;
-    }
+    recip3(dvxi + 1.e-36, dveta + 1.e-36, dvzeta + 1.e-36, inx, iny, inz);
     const double phixi = monoq_phi(inx, dm, dp, prm, src0, tl[0], tl[3], tl[6]);
     dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
     dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);

@@ -46,6 +46,12 @@ int main() {
     a[i] = std::pow(10.0, -9.0 + 18.0 * u01());   // relative volumes within eosvmin..eosvmax
     b[i] = std::pow(10.0, -9.0 + 18.0 * u01());
     c[i] = std::pow(10.0, -20.0 + 23.0 * u01());  // |vdov| + 1e-20
+    if (i % 64 == 0) {
+      // operands whose products leave the normal range (the division fallback)
+      a[i] = std::pow(10.0, -300.0 + 600.0 * u01());
+      b[i] = std::pow(10.0, -300.0 + 600.0 * u01());
+      c[i] = std::pow(10.0, -300.0 + 600.0 * u01());
+    }
   }
   double *dx, *da, *db, *dc, *dout;
   const size_t bytes = (size_t)n * sizeof(double);
