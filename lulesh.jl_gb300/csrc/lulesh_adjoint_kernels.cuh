@@ -794,7 +794,7 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
 //    products (the reference's face-5 quirk unless corrected).
 // All three use the 12 face diagonals of the element.
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_force_geo(AdjDev a) {
+__global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= E) return;
