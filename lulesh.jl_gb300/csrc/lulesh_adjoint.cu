@@ -235,11 +235,22 @@ static void set_scalars(lulesh_domain* d, const Scalars5& s) {
   d->sc[LULESH_S_CYCLE] = (double)s.cycle;
 }
 
+// The start of a taped segment: the force kernel's geometry of the current
+// positions, with the first cycle's face diagonals and normals on its tape.
+static void tape_segment_begin(lulesh_adjoint* a, const CycleTape& first, cudaStream_t s) {
+  DevDomain gd = a->dom->dd;
+  gd.tapeGeoNext = first.geo;
+  launch_geometry(gd, s);
+}
+
 // One taped cycle, queued on the stream: the start state to its slot and
 // timeIncrement! on the device (recorded), the step kernels with the cycle's
 // intermediate values, accelerations, branch flags and dt candidates going to
-// the tape, then the arg-min elements of the Courant and hydro minima.
-static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, CycleRec* rec, cudaStream_t s) {
+// the tape (the kinematics kernel also writes the next cycle's face diagonals
+// and normals to `next`, if there is one), then the arg-min elements of the
+// Courant and hydro minima.
+static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, const CycleTape* next, CycleRec* rec,
+                       cudaStream_t s) {
   lulesh_domain* d = a->dom;
   const Params prm = make_params(d);
   const int nmax = std::max(a->E, a->N);
@@ -253,6 +264,7 @@ static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, C
   td.fx = a->fx_s; td.fy = a->fy_s; td.fz = a->fz_s;
   td.tapeFlags = tp.flags; td.tapeDtc = tp.dtc; td.tapeDth = tp.dth; td.tapeGeo = tp.geo;
   td.tapeKin = tp.kin; td.tapeMat = tp.mat;
+  td.tapeGeoNext = next ? next->geo : nullptr;
   launch_force(td, prm, d->tuning, s);
   launch_node(td, prm, true, d->tuning, s);  // aux: the node kernel stores the accelerations
   launch_kinematics(td, prm, false, d->tuning, s);
@@ -605,6 +617,11 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
   state_to_device_mirror(d);  // no cycle limit: the segments count the cycles
   ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
+  // the plain segments read the force geometry the kinematics kernel stores;
+  // the taping kernels form their own, so after the gradient (the domain left
+  // at the final state) it has to be formed again
+  ensure_geometry(d);
+  d->geo_valid = false;
   for (int k = 0; k < nplan; ++k) {
     copy_state_from_domain(a, a->ckpts[k], s);
     ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
@@ -612,7 +629,9 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
       ACK(cudaGraphLaunch(a->fwd_graph, s));
     } else {
       TapeSet& ts = set_of(k);
-      for (int j = 0; j < last_len; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], ts.rec + j, s);
+      tape_segment_begin(a, ts.tape[0], s);
+      for (int j = 0; j < last_len; ++j)
+        tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < last_len ? &ts.tape[j + 1] : nullptr, ts.rec + j, s);
       copy_state_from_domain(a, ts.slots[last_len], s);
     }
   }
@@ -652,7 +671,8 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   // when the parameters they bake in change).
   cudaStream_t rs = pipe ? a->rstream : s;
   auto queue_recompute = [&](TapeSet& ts, int n, cudaStream_t st) {
-    for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], ts.rec + j, st);
+    tape_segment_begin(a, ts.tape[0], st);
+    for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < n ? &ts.tape[j + 1] : nullptr, ts.rec + j, st);
     copy_state_from_domain(a, ts.slots[n], st);
   };
   auto queue_transpose = [&](TapeSet& ts, int n, cudaStream_t st) {

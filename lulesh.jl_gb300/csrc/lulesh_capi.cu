@@ -66,6 +66,12 @@ Params lulesh::make_params(const lulesh_domain* d) {
   return p;
 }
 
+void lulesh::ensure_geometry(lulesh_domain* d) {
+  if (d->geo_valid) return;
+  launch_geometry(d->dd, d->stream);
+  d->geo_valid = true;
+}
+
 // Maps kernel status bits to (status, site) in the reference's check order.
 void lulesh::decode_status(unsigned bits, int32_t* status, int32_t* site) {
   *status = LULESH_OK;
@@ -402,11 +408,14 @@ int lulesh_lagrange_leapfrog(lulesh_domain* d) {
   state_to_device_mirror(d);
   int rc;
   if ((rc = h2d(d->dd.st, d->hst, 1, d->stream))) return rc;
+  ensure_geometry(d);
   if ((rc = launch_step(d, prm, false, d->timing))) return rc;
   if ((rc = d2h(d->hst, d->dd.st, 1, d->stream))) return rc;
   CK(cudaStreamSynchronize(d->stream));
   if (d->timing && (rc = collect_times(d))) return rc;
   state_from_device_mirror(d);
+  // a step that stopped early may leave the stored geometry behind the positions
+  if (d->status) d->geo_valid = false;
   return d->status;
 }
 
@@ -419,6 +428,7 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
   int rc;
   cudaStream_t s = d->stream;
   if ((rc = h2d(d->dd.st, d->hst, 1, s))) return rc;
+  ensure_geometry(d);
   // cycles the loop can still take: the first always runs, later ones while cycle < num_iters
   const int64_t cyc0 = d->cycle_i();
   const int64_t budget = std::max<int64_t>(1, num_iters - cyc0);
@@ -462,6 +472,7 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
   if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
   CK(cudaStreamSynchronize(s));
   state_from_device_mirror(d);
+  if (d->status) d->geo_valid = false;
   if (out) lulesh_get_scalars(d, out);
   return d->status;
 }
@@ -681,6 +692,8 @@ int lulesh_upload_field(lulesh_domain* d, int32_t f, const void* host, int64_t c
   cudaStream_t s = d->stream;
   const int64_t E = d->E, N = d->N;
   int rc;
+  // the force kernel's stored geometry depends on the positions and the connectivity
+  if (f == LULESH_F_X || f == LULESH_F_Y || f == LULESH_F_Z || f == LULESH_F_NODELIST) d->geo_valid = false;
   if (f < LULESH_F_NODELIST) {
     Kind k;
     double* p = f64_ptr(d, f, &k);
@@ -810,12 +823,16 @@ int lulesh_autotune(lulesh_domain* d, int32_t cycles, lulesh_tuning* chosen) {
     d->hst->first = 0;
     err = cudaMemcpyAsync(dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s);
   }
-  if (err == cudaSuccess) err = autotune_blocks(dd, make_params(d), d->params.keep_aux != 0, 1, s, cycles, d->tuning);
+  if (err == cudaSuccess) {
+    ensure_geometry(d);
+    err = autotune_blocks(dd, make_params(d), d->params.keep_aux != 0, 1, s, cycles, d->tuning);
+  }
   if (err == cudaSuccess) err = copy_all(false);
   if (err == cudaSuccess) err = cudaStreamSynchronize(s);
   cudaFree(save);
   std::memcpy(d->sc, sc_saved, sizeof(sc_saved));
   drop_graph(d);
+  d->geo_valid = false;  // the tuning cycles moved the positions the geometry describes
   CK(err);
   return chosen ? lulesh_get_tuning(d, chosen) : LULESH_OK;
 }

@@ -81,6 +81,7 @@ struct lulesh_ensemble {
   std::vector<DevState> init_state;
   cudaGraphExec_t graph = nullptr;
   int64_t graph_key = -1;
+  bool geo_valid = false;  // dd.nextGeo holds the force geometry of the current positions
 };
 
 static double** mutable_node_fields(DevDomain& d, int k) {
@@ -311,6 +312,7 @@ int lulesh_ens_reset(lulesh_ensemble* s) {
   ECK(cudaSetDevice(s->device));
   int rc = snapshot_copy(s, false);
   if (rc) return rc;
+  s->geo_valid = false;
   return upload_states(s);
 }
 
@@ -332,6 +334,12 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
     budget = std::max<int64_t>(budget, num_iters - d.cycle);
   }
   ECK(cudaMemcpyAsync(s->dd.st, s->hst, sizeof(DevState) * s->n, cudaMemcpyHostToDevice, st));
+  // the force kernel's stored geometry (an instance that stopped on an error
+  // keeps its positions until a reset, which clears this)
+  if (!s->geo_valid) {
+    launch_geometry(s->dd, st);
+    s->geo_valid = true;
+  }
   // the run limit lives in the device state, so one graph serves every call
   if (!s->graph) {
     drop_graph(s);
@@ -482,6 +490,7 @@ int lulesh_ens_autotune(lulesh_ensemble* s, int32_t cycles, lulesh_tuning* chose
   if (rc) return rc;
   for (int i = 0; i < s->n; ++i) { s->hst[i] = s->init_state[i]; s->hst[i].first = 0; }
   ECK(cudaMemcpyAsync(s->dd.st, s->hst, sizeof(DevState) * s->n, cudaMemcpyHostToDevice, s->stream));
+  launch_geometry(s->dd, s->stream);
   ECK(autotune_blocks(s->dd, s->prm, false, s->n, s->stream, cycles, s->tuning));
   drop_graph(s);
   if ((rc = lulesh_ens_reset(s))) return rc;

@@ -27,6 +27,9 @@ struct lulesh_domain {
   lulesh::DevState* hst = nullptr;  // pinned mirror of the device state
   cudaGraphExec_t graph = nullptr;
   int64_t graph_key = -1;
+  // dd.nextGeo holds the force kernel's geometry of the current positions
+  // (cleared when the host changes positions or a step stops early)
+  bool geo_valid = false;
   // host copies of what only the host uses
   std::vector<int> symmX, symmY, symmZ;
   std::vector<int64_t> regNumList, regElemlist, regCSR, regReps, regSorted, regElemSize;
@@ -43,6 +46,8 @@ struct lulesh_domain {
 namespace lulesh {
 // Kernel parameters from the handle's Domain scalars.
 Params make_params(const lulesh_domain* d);
+// Forms the force kernel's geometry on the handle's stream unless it is valid.
+void ensure_geometry(lulesh_domain* d);
 // Status bits of a step -> (lulesh_status, lulesh_site) in the reference's order.
 void decode_status(unsigned bits, int32_t* status, int32_t* site);
 // Host scalars -> pinned device-state mirror (fresh accumulators, first = 1).

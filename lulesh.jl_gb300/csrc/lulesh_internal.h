@@ -113,6 +113,9 @@ struct DevState {
 
 constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
 
+// doubles per element of DevDomain::nextGeo
+constexpr int kGeoSlots = 51;
+
 // Pointers of one problem's device fields. Element arrays have E entries,
 // node arrays N; corner arrays 8E in corner-major order (c*E + e).
 struct DevDomain {
@@ -136,6 +139,12 @@ struct DevDomain {
   // region batching (cost model only)
   int* regElemlist0;                          // E, 0-based element ids grouped by region
   int* regOfSlot;                             // E, region rep count per slot
+  // the force kernel's geometry of the current positions, [kGeoSlots][E]
+  // (formed by the kinematics kernel of the cycle before, or by k_geometry)
+  double* nextGeo;
+  // taped runs: the next cycle's force tape, where the kinematics kernel (or
+  // k_geometry) writes the face diagonals and normals of these positions
+  double* tapeGeoNext;
   // corner forces [8][E]
   double *fcx, *fcy, *fcz;
   // step state: one entry, or one per instance of an ensemble

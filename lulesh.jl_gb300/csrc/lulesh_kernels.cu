@@ -27,8 +27,213 @@ __device__ __forceinline__ bool step_off(const DevState* st) {
 }
 
 // ---------------------------------------------------------------------------
+// Element geometry at one set of positions
+// ---------------------------------------------------------------------------
+// The force kernel of a cycle sees the positions the kinematics kernel of
+// the cycle before it saw. So the kinematics kernel (or k_geometry, at the
+// start of a run and after the host changed the positions) forms what the
+// force kernel needs from the positions alone and stores it in d.nextGeo
+// ([kGeoSlots][E]), and the force kernel loads it instead of forming it
+// again. Both sides use the functions below, so a stored value is bitwise
+// the one the force kernel would form (the taping force kernel still forms
+// them, for its tape).
+//
+// d.nextGeo slots: 0..23 the volume derivatives of corner n, coordinate k
+// (8k + n, in corner order); 24..35 the hourglass modes of coordinate k
+// (24 + 4k + m, before the 1/(12 determ) scale); 36..47 the node normals of
+// corners 0..3 (36 + 4k + n, before node 0's quirk and the stress scale);
+// 48 and 49 face 0 + face 1's z normal and face 4's y normal (node 0's
+// quirk); 50 the Jacobian determinant of the detJ check.
+
+// The 12 face diagonals, two per face in calcElemNodeNormals' argument order
+// p2 - p0, p3 - p1 (src/domain.jl:991-1067). Face f: (2,0,3,1) (5,0,1,4)
+// (6,1,2,5) (7,2,3,6) (4,3,0,7) (6,4,5,7), so g = d20 d31 d50 d14 d61 d25
+// d72 d36 d43 d07 d64 d57.
+__device__ __forceinline__ void face_diagonals(const double x[8], const double y[8], const double z[8],
+                                               double g[12][3]) {
+  constexpr int pa[12] = {2, 3, 5, 1, 6, 2, 7, 3, 4, 0, 6, 5};
+  constexpr int pb[12] = {0, 1, 0, 4, 1, 5, 2, 6, 3, 7, 4, 7};
+#pragma unroll
+  for (int q = 0; q < 12; ++q) {
+    g[q][0] = x[pa[q]] - x[pb[q]];
+    g[q][1] = y[pa[q]] - y[pb[q]];
+    g[q][2] = z[pa[q]] - z[pb[q]];
+  }
+}
+
+// Walsh coefficients of the positions: w[k] = the Jacobian columns (xi, eta,
+// zeta) of coordinate k, hm[k] = its hourglass modes (eta*zeta, xi*zeta,
+// xi*eta, xi*eta*zeta; src/domain.jl:1510-1525 without the gamma sums).
+// Face diagonals join corners of one parity, so the three even modes are
+// sums of four of them: eta*zeta = (d64 - d57) - (d20 + d31), xi*zeta =
+// (d07 + d61) - (d43 + d25), xi*eta = (d07 + d61) + (d43 + d25); w and
+// xi*eta*zeta come from the four body diagonals a = p6 - p0, b = p5 - p3,
+// c = p7 - p1, d = p4 - p2: (a+b) - (c+d), (a-b) + (c-d), (a+b) + (c+d) and
+// (a-b) - (c-d). 19 adds per coordinate instead of a 23-add butterfly.
+__device__ __forceinline__ void position_walsh(const double x[8], const double y[8], const double z[8],
+                                               const double g[12][3], double w[3][3], double hm[3][4]) {
+  const double* P[3] = {x, y, z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double* v = P[k];
+    const double a = v[6] - v[0], b = v[5] - v[3], c = v[7] - v[1], dd = v[4] - v[2];
+    const double apb = a + b, cpd = c + dd, amb = a - b, cmd = c - dd;
+    w[k][0] = apb - cpd;
+    w[k][1] = amb + cmd;
+    w[k][2] = apb + cpd;
+    hm[k][3] = amb - cmd;
+    hm[k][0] = (g[10][k] - g[11][k]) - (g[0][k] + g[1][k]);
+    const double pp = g[9][k] + g[4][k], qq = g[8][k] + g[5][k];
+    hm[k][1] = pp - qq;
+    hm[k][2] = pp + qq;
+  }
+}
+
+// integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
+// sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
+__device__ __forceinline__ double jacobian_det(const double w[3][3]) {
+  const double cxet = fma(w[2][0], w[1][2], -(w[1][0] * w[2][2]));
+  const double cyet = fma(w[0][0], w[2][2], -(w[2][0] * w[0][2]));
+  const double czet = fma(w[1][0], w[0][2], -(w[0][0] * w[1][2]));
+  return fma(w[0][1], cxet, fma(w[1][1], cyet, w[2][1] * czet));
+}
+
+// Face f's area vector times -8: the cross product of its two diagonals.
+__device__ __forceinline__ void face_normal(const double g[12][3], int f, double n[3]) {
+  cross(g[2 * f][0], g[2 * f][1], g[2 * f][2], g[2 * f + 1][0], g[2 * f + 1][1], g[2 * f + 1][2], n[0], n[1], n[2]);
+}
+
+// Node normals (calcElemNodeNormals, src/domain.jl:991-1067) of corners 0..3
+// as sums of their three faces' cross products (true B = -Bc/8); node 0
+// without its quirk, for which pz01 and ny4 are returned. The six face
+// normals are the area vectors of a closed surface and sum to zero, and
+// opposite corners touch complementary faces (node 0: faces 0,1,4; node 6:
+// 2,3,5), so corners 6, 7, 4, 5 are minus corners 0, 1, 2, 3 and face 5's
+// normal is never needed.
+__device__ __forceinline__ void node_normals(const double n[6][3], double B[3][4], double& pz01, double& ny4) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    const double p01 = n[0][k] + n[1][k];
+    B[k][0] = p01 + n[4][k];
+    B[k][1] = p01 + n[2][k];
+    B[k][2] = (n[0][k] + n[2][k]) + n[3][k];
+    B[k][3] = (n[0][k] + n[3][k]) + n[4][k];
+    if (k == 2) pz01 = p01;
+  }
+  ny4 = n[4][1];
+}
+
+// calcElemVolume's three triple products U.(V x W) of face diagonals
+// (src/utils.jl:36-116): (d31+d72).(d63 x d20), (d43+d57).(d64 x d70),
+// (d14+d25).(d61 x d50); U[t] and the gradients V x W, W x U, U x V.
+__device__ __forceinline__ void volume_terms(const double g[12][3], double U[3][3], double gU[3][3], double gV[3][3],
+                                             double gW[3][3]) {
+  auto grads = [&](int t, const double V[3], const double W[3]) {
+    cross(V[0], V[1], V[2], W[0], W[1], W[2], gU[t][0], gU[t][1], gU[t][2]);
+    cross(W[0], W[1], W[2], U[t][0], U[t][1], U[t][2], gV[t][0], gV[t][1], gV[t][2]);
+    cross(U[t][0], U[t][1], U[t][2], V[0], V[1], V[2], gW[t][0], gW[t][1], gW[t][2]);
+  };
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    U[0][k] = g[1][k] + g[6][k];
+    U[1][k] = g[8][k] + g[11][k];
+    U[2][k] = g[3][k] + g[5][k];
+  }
+  const double V1[3] = {-g[7][0], -g[7][1], -g[7][2]};
+  grads(0, V1, g[0]);
+  const double W2[3] = {-g[9][0], -g[9][1], -g[9][2]};
+  grads(1, g[10], W2);
+  grads(2, g[4], g[2]);
+}
+
+// calcElemVolumeDerivative (src/domain.jl:1178-1256), times 12, in corner
+// order: its voluDer values are the gradient of 12*volume, the triple
+// products' gradients scattered to their corners (U1 = +3 -1 +7 -2,
+// V1 = +6 -3, W1 = +2 -0; U2 = +4 -3 +5 -7, V2 = +6 -4, W2 = +7 -0;
+// U3 = +1 -4 +2 -5, V3 = +6 -1, W3 = +5 -0). The reference's n-th call
+// stores node owner[n]'s derivative in slot n (slots 1 and 3 exchanged)
+// unless corrected; the force kernel applies that when it reads them.
+__device__ __forceinline__ void volume_derivatives(const double gU[3][3], const double gV[3][3],
+                                                   const double gW[3][3], double gr[3][8]) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    // corners 1 and 2, 3 and 7, 4 and 5 share a difference of the U gradients
+    const double t12 = gU[2][k] - gU[0][k], t37 = gU[0][k] - gU[1][k], t45 = gU[1][k] - gU[2][k];
+    gr[k][0] = -((gW[0][k] + gW[1][k]) + gW[2][k]);
+    gr[k][1] = t12 - gV[2][k];
+    gr[k][2] = t12 + gW[0][k];
+    gr[k][3] = t37 - gV[0][k];
+    gr[k][4] = t45 - gV[1][k];
+    gr[k][5] = t45 + gW[2][k];
+    gr[k][6] = (gV[0][k] + gV[1][k]) + gV[2][k];
+    gr[k][7] = t37 + gW[1][k];
+  }
+}
+
+__device__ __forceinline__ void store_geometry(double* geo, int E, int e, const double gr[3][8], const double hm[3][4],
+                                               const double B[3][4], double pz01, double ny4, double det) {
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+#pragma unroll
+    for (int n = 0; n < 8; ++n) geo[(8 * k + n) * E + e] = gr[k][n];
+#pragma unroll
+    for (int m = 0; m < 4; ++m) geo[(24 + 4 * k + m) * E + e] = hm[k][m];
+#pragma unroll
+    for (int n = 0; n < 4; ++n) geo[(36 + 4 * k + n) * E + e] = B[k][n];
+  }
+  geo[48 * E + e] = pz01;
+  geo[49 * E + e] = ny4;
+  geo[50 * E + e] = det;
+}
+
+// The force tape's face diagonals (slots 66 + 3q + k) and face normals 0..4
+// (48 + f, 54 + f, 60 + f) of these positions, for the transpose.
+__device__ __forceinline__ void tape_force_geometry(double* tape, int E, int e, const double g[12][3],
+                                                    const double n[6][3]) {
+#pragma unroll
+  for (int q = 0; q < 12; ++q)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tape[(66 + 3 * q + k) * E + e] = g[q][k];
+#pragma unroll
+  for (int f = 0; f < 5; ++f) {
+    tape[(48 + f) * E + e] = n[f][0];
+    tape[(54 + f) * E + e] = n[f][1];
+    tape[(60 + f) * E + e] = n[f][2];
+  }
+}
+
+// The stored geometry of the current positions (see above): at the start of
+// a run, after the host changed the positions, and for the ensemble's reset;
+// in a taped run also the first cycle's face diagonals and normals.
+__global__ void __launch_bounds__(kMaxElemBlock) k_geometry(DevDomain d) {
+  const int E = d.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  double x[8], y[8], z[8];
+#pragma unroll
+  for (int c = 0; c < 8; ++c) {
+    const int nd = LULESH_IDX(LDG(&d.nodelist[c * E + e]), d.N, d.st);
+    x[c] = LDG(&d.x[nd]); y[c] = LDG(&d.y[nd]); z[c] = LDG(&d.z[nd]);
+  }
+  double g[12][3], w[3][3], hm[3][4], n[6][3], B[3][4], pz01, ny4;
+  double U[3][3], gU[3][3], gV[3][3], gW[3][3], gr[3][8];
+  face_diagonals(x, y, z, g);
+  position_walsh(x, y, z, g, w, hm);
+#pragma unroll
+  for (int f = 0; f < 5; ++f) face_normal(g, f, n[f]);
+  node_normals(n, B, pz01, ny4);
+  volume_terms(g, U, gU, gV, gW);
+  volume_derivatives(gU, gV, gW, gr);
+  store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w));
+  if (d.tapeGeoNext) tape_force_geometry(d.tapeGeoNext, E, e, g, n);
+}
+
+// ---------------------------------------------------------------------------
 // k_force
 // ---------------------------------------------------------------------------
+// Every variant loads the geometry of the cycle's positions from d.nextGeo;
+// the taping variant adds the volume derivatives, scaled modes and mode
+// sums to the force tape (the diagonals and normals are there already).
 template <int MODE, bool ENS, bool TAPE>
 __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm) {
   const int E = d.E;
@@ -42,172 +247,55 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   int nd[8];
 #pragma unroll
   for (int c = 0; c < 8; ++c) nd[c] = LULESH_IDX(LDG(&d.nodelist[c * E + e]), d.N, st);
-  double x[8], y[8], z[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) {
-    x[c] = LDG(&d.x[nd[c]]);
-    y[c] = LDG(&d.y[nd[c]]);
-    z[c] = LDG(&d.z[nd[c]]);
-  }
 
-  // The 12 face diagonals (two per face, in calcElemNodeNormals' argument
-  // order p2 - p0, p3 - p1) serve the node normals, the volume derivatives
-  // and three of the four hourglass modes.
-  // Face f: (2,0,3,1) (5,0,1,4) (6,1,2,5) (7,2,3,6) (4,3,0,7) (6,4,5,7).
-  double g[12][3];
+  double gr[3][8], hm[3][4], B[3][4], pz01, ny4, det;
   {
-    constexpr int pa[12] = {2, 3, 5, 1, 6, 2, 7, 3, 4, 0, 6, 5};
-    constexpr int pb[12] = {0, 1, 0, 4, 1, 5, 2, 6, 3, 7, 4, 7};
-#pragma unroll
-    for (int q = 0; q < 12; ++q) {
-      g[q][0] = x[pa[q]] - x[pb[q]];
-      g[q][1] = y[pa[q]] - y[pb[q]];
-      g[q][2] = z[pa[q]] - z[pb[q]];
-      if (TAPE) {
-        d.tapeGeo[(66 + 3 * q) * E + e] = g[q][0];
-        d.tapeGeo[(67 + 3 * q) * E + e] = g[q][1];
-        d.tapeGeo[(68 + 3 * q) * E + e] = g[q][2];
-      }
-    }
-  }
-
-  // Walsh coefficients: W1 = Jacobian columns (xi, eta, zeta), HM = the
-  // hourglass modes (eta*zeta, xi*zeta, xi*eta, xi*eta*zeta). Face diagonals
-  // join corners of one parity, so the three even modes are sums of four
-  // of them: eta*zeta = (d64 - d57) - (d20 + d31), xi*zeta = (d07 + d61) -
-  // (d43 + d25), xi*eta = (d07 + d61) + (d43 + d25); W1 and xi*eta*zeta come
-  // from the four body diagonals a = p6 - p0, b = p5 - p3, c = p7 - p1,
-  // d = p4 - p2: (a+b) - (c+d), (a-b) + (c-d), (a+b) + (c+d) and
-  // (a-b) - (c-d). 19 adds per coordinate instead of a 23-add butterfly.
-  double wx[3], wy[3], wz[3], hmx[4], hmy[4], hmz[4];
-  {
-    const double* P[3] = {x, y, z};
-    double* W[3] = {wx, wy, wz};
-    double* H[3] = {hmx, hmy, hmz};
+    const double* geo = d.nextGeo;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      const double* v = P[k];
-      const double a = v[6] - v[0], b = v[5] - v[3], c = v[7] - v[1], dd = v[4] - v[2];
-      const double apb = a + b, cpd = c + dd, amb = a - b, cmd = c - dd;
-      W[k][0] = apb - cpd;
-      W[k][1] = amb + cmd;
-      W[k][2] = apb + cpd;
-      H[k][3] = amb - cmd;
-      H[k][0] = (g[10][k] - g[11][k]) - (g[0][k] + g[1][k]);
-      const double pp = g[9][k] + g[4][k], qq = g[8][k] + g[5][k];
-      H[k][1] = pp - qq;
-      H[k][2] = pp + qq;
-    }
-  }
-
-  // integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
-  // sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
-  {
-    const double cxet = fma(wz[0], wy[2], -(wy[0] * wz[2]));
-    const double cyet = fma(wx[0], wz[2], -(wz[0] * wx[2]));
-    const double czet = fma(wy[0], wx[2], -(wx[0] * wy[2]));
-    const double det = fma(wx[1], cxet, fma(wy[1], cyet, wz[1] * czet));
-    if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
-  }
-
-  // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q
-  const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
-
-  // Node normals (calcElemNodeNormals, src/domain.jl:991-1067) as sums of
-  // face-diagonal cross products; true B = -Bc/8. The face normals are scaled
-  // by s8 here, so Bx..Bz hold the stress forces s8*Bc. The six face normals
-  // are the area vectors of a closed surface and sum to zero, and opposite
-  // corners touch complementary faces (node 0: faces 0,1,4; node 6: 2,3,5),
-  // so B6 = -B0, B7 = -B1, B4 = -B2, B5 = -B3 and face 5's normal is not
-  // needed (the taping variant still forms it for the transpose).
-  double Bx[4], By[4], Bz[4];  // corners 0..3; corner 6, 7, 4, 5 is minus corner 0, 1, 2, 3
-  double b6y, b6z;             // corner 0's y and z before its quirk (corner 6 is minus them)
-  {
-    double nx[6], ny[6], nz[6];
 #pragma unroll
-    for (int f = 0; f < (TAPE ? 6 : 5); ++f) {
-      const double* d1 = g[2 * f];
-      const double* d2 = g[2 * f + 1];
-      cross(d1[0], d1[1], d1[2], d2[0], d2[1], d2[2], nx[f], ny[f], nz[f]);
-      if (TAPE) {
-        d.tapeGeo[(48 + f) * E + e] = nx[f];
-        d.tapeGeo[(54 + f) * E + e] = ny[f];
-        d.tapeGeo[(60 + f) * E + e] = nz[f];
-      }
-      nx[f] *= s8; ny[f] *= s8; nz[f] *= s8;
+      for (int n = 0; n < 8; ++n) gr[k][n] = LDG(&geo[(8 * k + n) * E + e]);
+#pragma unroll
+      for (int m = 0; m < 4; ++m) hm[k][m] = LDG(&geo[(24 + 4 * k + m) * E + e]);
+#pragma unroll
+      for (int n = 0; n < 4; ++n) B[k][n] = LDG(&geo[(36 + 4 * k + n) * E + e]);
     }
-    // node -> its three faces (faces numbered 0..5 = reference faces 1..6)
-    const double px01 = nx[0] + nx[1], py01 = ny[0] + ny[1], pz01 = nz[0] + nz[1];
-    Bx[0] = px01 + nx[4]; By[0] = py01 + ny[4]; Bz[0] = pz01 + nz[4];
-    Bx[1] = px01 + nx[2]; By[1] = py01 + ny[2]; Bz[1] = pz01 + nz[2];
-    Bx[2] = (nx[0] + nx[2]) + nx[3]; By[2] = (ny[0] + ny[2]) + ny[3]; Bz[2] = (nz[0] + nz[2]) + nz[3];
-    Bx[3] = (nx[0] + nx[3]) + nx[4]; By[3] = (ny[0] + ny[3]) + ny[4]; Bz[3] = (nz[0] + nz[3]) + nz[4];
-    b6y = By[0]; b6z = Bz[0];
-    if (!(MODE & 1)) {
-      // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice, no areaZ
-      By[0] = By[0] + ny[4];
-      Bz[0] = pz01;
-    }
+    pz01 = LDG(&geo[48 * E + e]);
+    ny4 = LDG(&geo[49 * E + e]);
+    det = LDG(&geo[50 * E + e]);
+  }
+  if (le_zero(det)) atomicOr(&st->status, ST_EARLY);
+
+  // the reference's slots of the volume derivatives: node 3's in slot 1 and
+  // node 1's in slot 3 unless corrected
+  double dvx[8], dvy[8], dvz[8];
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const int src = (MODE & 2) ? n : (n == 1 ? 3 : n == 3 ? 1 : n);
+    dvx[n] = gr[0][src]; dvy[n] = gr[1][src]; dvz[n] = gr[2][src];
+  }
+
+  // stress: f = (-sig) * B = (sig/8) * Bc with sig = -p - q; corners 4..7
+  // are minus corners 2, 3, 0, 1, formed before node 0's quirk
+  const double s8 = ((-LDG(&d.p[e])) - LDG(&d.q[e])) * 0.125;
+  double SB[3][4];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+#pragma unroll
+    for (int n = 0; n < 4; ++n) SB[k][n] = s8 * B[k][n];
+  double q0y = SB[1][0], q0z = SB[2][0];
+  if (!(MODE & 1)) {
+    // src/domain.jl:1050-1055: node 1 takes face 5's areaY twice, no areaZ
+    q0y = s8 * (B[1][0] + ny4);
+    q0z = s8 * pz01;
   }
   // s8*Bc of corner n, component k (n and k are constants after unrolling, so
   // the sign folds into the instruction that consumes it)
   auto bstress = [&](int k, int n) -> double {
-    const double* b = k == 0 ? Bx : k == 1 ? By : Bz;
-    if (n < 4) return b[n];
-    if (n == 6) return -(k == 0 ? Bx[0] : k == 1 ? b6y : b6z);
-    return -b[n == 4 ? 2 : n == 5 ? 3 : 1];
+    if (n == 0) return k == 0 ? SB[0][0] : k == 1 ? q0y : q0z;
+    if (n < 4) return SB[k][n];
+    return -SB[k][n == 4 ? 2 : n == 5 ? 3 : n == 6 ? 0 : 1];
   };
-
-  // calcElemVolumeDerivative (src/domain.jl:1178-1256), times 12: its eight
-  // voluDer calls are the gradient of 12*volume, and 12*volume is
-  // calcElemVolume's sum of three triple products U.(V x W) of face
-  // diagonals (src/utils.jl:36-116): (d31+d72).(d63 x d20),
-  // (d43+d57).(d64 x d70), (d14+d25).(d61 x d50). The gradient w.r.t. U, V,
-  // W is V x W, W x U, U x V, scattered to their corners. The n-th reference
-  // call differentiates w.r.t. node owner[n] and stores in slot n (slots 1
-  // and 3 exchanged) unless corrected.
-  double dvx[8], dvy[8], dvz[8];
-  {
-    double gU[3][3], gV[3][3], gW[3][3];
-    auto grads = [&](int t, const double U[3], const double V[3], const double W[3]) {
-      cross(V[0], V[1], V[2], W[0], W[1], W[2], gU[t][0], gU[t][1], gU[t][2]);
-      cross(W[0], W[1], W[2], U[0], U[1], U[2], gV[t][0], gV[t][1], gV[t][2]);
-      cross(U[0], U[1], U[2], V[0], V[1], V[2], gW[t][0], gW[t][1], gW[t][2]);
-    };
-    {
-      // diagonals: 0 d20, 1 d31, 2 d50, 3 d14, 4 d61, 5 d25, 6 d72, 7 d36, 8 d43, 9 d07, 10 d64, 11 d57
-      const double U1[3] = {g[1][0] + g[6][0], g[1][1] + g[6][1], g[1][2] + g[6][2]};
-      const double V1[3] = {-g[7][0], -g[7][1], -g[7][2]};
-      grads(0, U1, V1, g[0]);
-      const double U2[3] = {g[8][0] + g[11][0], g[8][1] + g[11][1], g[8][2] + g[11][2]};
-      const double W2[3] = {-g[9][0], -g[9][1], -g[9][2]};
-      grads(1, U2, g[10], W2);
-      const double U3[3] = {g[3][0] + g[5][0], g[3][1] + g[5][1], g[3][2] + g[5][2]};
-      grads(2, U3, g[4], g[2]);
-    }
-    // corners: U1 = +3 -1 +7 -2, V1 = +6 -3, W1 = +2 -0; U2 = +4 -3 +5 -7,
-    // V2 = +6 -4, W2 = +7 -0; U3 = +1 -4 +2 -5, V3 = +6 -1, W3 = +5 -0
-    double gr[8][3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      // corners 1 and 2, 3 and 7, 4 and 5 share a difference of the U gradients
-      const double t12 = gU[2][k] - gU[0][k], t37 = gU[0][k] - gU[1][k], t45 = gU[1][k] - gU[2][k];
-      gr[0][k] = -((gW[0][k] + gW[1][k]) + gW[2][k]);
-      gr[1][k] = t12 - gV[2][k];
-      gr[2][k] = t12 + gW[0][k];
-      gr[3][k] = t37 - gV[0][k];
-      gr[4][k] = t45 - gV[1][k];
-      gr[5][k] = t45 + gW[2][k];
-      gr[6][k] = (gV[0][k] + gV[1][k]) + gV[2][k];
-      gr[7][k] = t37 + gW[1][k];
-    }
-#pragma unroll
-    for (int n = 0; n < 8; ++n) {
-      // faithful slots: node 3's derivative in slot 1 and node 1's in slot 3
-      const int src = (MODE & 2) ? n : (n == 1 ? 3 : n == 3 ? 1 : n);
-      dvx[n] = gr[src][0]; dvy[n] = gr[src][1]; dvz[n] = gr[src][2];
-    }
-  }
 
   // calcHourglassControlForElems (src/domain.jl:1696-1736): determ = volo*v.
   const double v = LDG(&d.v[e]);
@@ -220,8 +308,9 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
     // determ^(-1/3) serves the coefficient, its cube the modes' 1/(12 determ)
     const double rc = inv_cbrt(determ);
     const double vi12 = (rc * rc) * (rc * (1.0 / 12.0));
+    double hmx[4], hmy[4], hmz[4];
 #pragma unroll
-    for (int m = 0; m < 4; ++m) { hmx[m] *= vi12; hmy[m] *= vi12; hmz[m] *= vi12; }
+    for (int m = 0; m < 4; ++m) { hmx[m] = hm[0][m] * vi12; hmy[m] = hm[1][m] * vi12; hmz[m] = hm[2][m] * vi12; }
     if (TAPE) {
 #pragma unroll
       for (int n = 0; n < 8; ++n) {
@@ -351,75 +440,69 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     z[c] = LDG(&d.z[nd[c]]);
   }
 
-  // calcElemVolume (src/utils.jl:36-116); its 12 differences are the face
-  // diagonals that calcElemCharacteristicLength needs too.
+  // calcElemVolume (src/utils.jl:36-116) and calcElemCharacteristicLength
+  // (src/domain.jl:1874-1930) from the face diagonals; the next force
+  // kernel's geometry of these positions is stored too.
   double volume, charLength = 0.0;
-  double wx[3], wy[3], wz[3];  // first-order Walsh vectors (xi, eta, zeta) of x, y, z
+  double w[3][3];  // first-order Walsh vectors (xi, eta, zeta) of x, y, z
   {
-    double d61[3], d70[3], d63[3], d20[3], d50[3], d64[3], d31[3], d72[3], d43[3], d57[3], d14[3], d25[3];
-    const double* P[3] = {x, y, z};
-    double* W[3] = {wx, wy, wz};
+    double g[12][3], hm[3][4], n[6][3], U[3][3], gU[3][3], gV[3][3], gW[3][3];
+    face_diagonals(x, y, z, g);
+    position_walsh(x, y, z, g, w, hm);
+    volume_terms(g, U, gU, gV, gW);
+    auto triple_t = [&](int t) { return fma(U[t][0], gU[t][0], fma(U[t][1], gU[t][1], U[t][2] * gU[t][2])); };
+    volume = ((triple_t(0) + triple_t(1)) + triple_t(2)) * (1.0 / 12.0);
 #pragma unroll
-    for (int k = 0; k < 3; ++k) {
-      const double* p = P[k];
-      d61[k] = p[6] - p[1]; d70[k] = p[7] - p[0]; d63[k] = p[6] - p[3]; d20[k] = p[2] - p[0];
-      d50[k] = p[5] - p[0]; d64[k] = p[6] - p[4]; d31[k] = p[3] - p[1]; d72[k] = p[7] - p[2];
-      d43[k] = p[4] - p[3]; d57[k] = p[5] - p[7]; d14[k] = p[1] - p[4]; d25[k] = p[2] - p[5];
-      // the Walsh vectors from the face diagonals (9 adds instead of 11):
-      // xi = (d20 - d31) + (d64 + d57), eta = (d20 + d31) + (d64 - d57),
-      // zeta = (d50 - d14) + (d72 + d63)
-      W[k][0] = (d20[k] - d31[k]) + (d64[k] + d57[k]);
-      W[k][1] = (d20[k] + d31[k]) + (d64[k] - d57[k]);
-      W[k][2] = (d50[k] - d14[k]) + (d72[k] + d63[k]);
-    }
-    double gu[3][3];  // V x W of each triple product (kept for the tape)
-    const double v12 =
-        triple(d31[0] + d72[0], d63[0], d20[0], d31[1] + d72[1], d63[1], d20[1], d31[2] + d72[2], d63[2], d20[2],
-               gu[0]) +
-        triple(d43[0] + d57[0], d64[0], d70[0], d43[1] + d57[1], d64[1], d70[1], d43[2] + d57[2], d64[2], d70[2],
-               gu[1]) +
-        triple(d14[0] + d25[0], d61[0], d50[0], d14[1] + d25[1], d61[1], d50[1], d14[2] + d25[2], d61[2], d50[2],
-               gu[2]);
-    volume = v12 * (1.0 / 12.0);
+    for (int f = 0; f < 6; ++f) face_normal(g, f, n[f]);
     if (TAPE) {
-      // the 12 diagonals d61 d70 d63 d20 d50 d64 d31 d72 d43 d57 d14 d25 and the crosses
-      const double* dgl[12] = {d61, d70, d63, d20, d50, d64, d31, d72, d43, d57, d14, d25};
+      // the 12 diagonals in the order d61 d70 d63 d20 d50 d64 d31 d72 d43 d57
+      // d14 d25 (force-order index, sign) and the V x W factors
+      constexpr int gi[12] = {4, 9, 7, 0, 2, 10, 1, 6, 8, 11, 3, 5};
+      constexpr int gs[12] = {1, -1, -1, 1, 1, 1, 1, 1, 1, 1, 1, 1};
 #pragma unroll
       for (int q = 0; q < 12; ++q)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) d.tapeKin[(45 + 3 * q + k) * E + e] = dgl[q][k];
+        for (int k = 0; k < 3; ++k) d.tapeKin[(45 + 3 * q + k) * E + e] = gs[q] < 0 ? -g[gi[q]][k] : g[gi[q]][k];
 #pragma unroll
       for (int t = 0; t < 3; ++t)
 #pragma unroll
-        for (int k = 0; k < 3; ++k) d.tapeKin[(81 + 3 * t + k) * E + e] = gu[t][k];
+        for (int k = 0; k < 3; ++k) d.tapeKin[(81 + 3 * t + k) * E + e] = gU[t][k];
     }
     // areaFace (src/domain.jl:1874-1891): with f, g = a -/+ b for the face
     // diagonals a, b, |f|^2|g|^2 - (f.g)^2 = |f x g|^2 = 4 |a x b|^2; the 4
-    // is folded into arealg below.
+    // is folded into arealg below. The reference's faces in order are the
+    // force order's 0, 5, 1, 2, 3, 4, the last two with reversed diagonals
+    // (so minus those cross products).
     int fidx = 0;
     double fcx = 0.0, fcy = 0.0, fcz = 0.0;  // the largest face's cross product (TAPE)
-    auto face = [&](const double* a, const double* b, int f) {
-      double cx, cy, cz;
-      cross(a[0], a[1], a[2], b[0], b[1], b[2], cx, cy, cz);
+    constexpr int ff[6] = {0, 5, 1, 2, 3, 4};
+#pragma unroll
+    for (int q = 0; q < 6; ++q) {
+      const double* c = n[ff[q]];
       // area4 >= +0 and charLength too: their bit patterns order them
-      const double area4 = fma(cx, cx, fma(cy, cy, cz * cz));
-      if (TAPE && (f == 0 || __double_as_longlong(area4) > __double_as_longlong(charLength))) {
-        fidx = f;
-        fcx = cx; fcy = cy; fcz = cz;
+      const double area4 = fma(c[0], c[0], fma(c[1], c[1], c[2] * c[2]));
+      if (TAPE && (q == 0 || __double_as_longlong(area4) > __double_as_longlong(charLength))) {
+        const bool neg = q >= 4;
+        fidx = q;
+        fcx = neg ? -c[0] : c[0]; fcy = neg ? -c[1] : c[1]; fcz = neg ? -c[2] : c[2];
       }
       charLength = max_nonneg(area4, charLength);
-    };
-    face(d20, d31, 0);   // nodes 1,2,3,4
-    face(d64, d57, 1);   // 5,6,7,8
-    face(d50, d14, 2);   // 1,2,6,5
-    face(d61, d25, 3);   // 2,3,7,6
-    face(d72, d63, 4);   // 3,4,8,7
-    face(d43, d70, 5);   // 4,1,5,8
+    }
     if (TAPE) {
       d.tapeFlags[e] = (unsigned long long)fidx << TF_FACE_SHIFT;
       d.tapeKin[41 * E + e] = fcx; d.tapeKin[42 * E + e] = fcy; d.tapeKin[43 * E + e] = fcz;
+      if (d.tapeGeoNext) tape_force_geometry(d.tapeGeoNext, E, e, g, n);
+    }
+    {
+      double B[3][4], pz01, ny4, gr[3][8];
+      node_normals(n, B, pz01, ny4);
+      volume_derivatives(gU, gV, gW, gr);
+      store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w));
     }
   }
+  const double* wx = w[0];
+  const double* wy = w[1];
+  const double* wz = w[2];
   const double vnew = volume * LDG(&d.inv_volo[e]);
   if (le_zero(vnew)) atomicOr(&st->status, ST_KINEMATICS);
   d.vnew[e] = vnew;
@@ -917,6 +1000,11 @@ __global__ void k_time_increment(DevState* st, int n, Params prm) {
 // ---------------------------------------------------------------------------
 // An ensemble (d.elemInst set) runs the ENS instantiations, which read each
 // element's or node's instance; the plain path runs ENS = false.
+void launch_geometry(const DevDomain& d, cudaStream_t s) {
+  const int bs = 128;
+  k_geometry<<<(d.E + bs - 1) / bs, bs, 0, s>>>(d);
+}
+
 void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaStream_t s) {
   const int bs = t.force;
   const int grid = (d.E + bs - 1) / bs;

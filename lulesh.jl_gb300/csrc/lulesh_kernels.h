@@ -22,6 +22,9 @@ struct Tuning {
   int mat = 128;
 };
 
+// k_geometry: the force kernel's geometry of the current positions (needed
+// before a step whenever the positions did not come from the last step).
+void launch_geometry(const DevDomain& d, cudaStream_t s);
 void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaStream_t s);
 void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
 void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s);
