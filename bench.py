@@ -32,10 +32,13 @@ UNIT = "zones*cycles/s"
 NX = 150
 # Algorithmic bytes (minimal HBM traffic of the method, FP64 fields, int32
 # connectivity): 364 B per element + 152 B per node per cycle for the whole
-# step; the force kernel's share is 80 B per element (nodelist, p, q, ss, v,
-# volo, elemMass) + 48 B per node (x, y, z, xd, yd, zd).
+# step. Per kernel, (bytes per element, bytes per node): the force pass reads
+# nodelist, p, q, ss, v, volo, elemMass and x..zd; the kinematics pass reads
+# nodelist, volo, v and x..zd and writes its nine outputs; the material pass
+# reads those nine, e, p, q, v, volo, elemMass, elemBC and writes e, p, q, ss,
+# v; the node pass reads x..zd and nodalMass and writes x..zd.
 STEP_BYTES_PER_ELEM, STEP_BYTES_PER_NODE = 364, 152
-FORCE_BYTES_PER_ELEM, FORCE_BYTES_PER_NODE = 80, 48
+KERNEL_BYTES = {"k_force": (80, 48), "k_kinematics": (120, 48), "k_material": (164, 0), "k_node": (0, 104)}
 STATE_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"]
 
 
@@ -48,12 +51,13 @@ def _measured_peaks():
 
 
 def _profile_numbers():
-    """Per-launch ncu figures of k_force at 150^3, if a profile summary was committed."""
-    path = os.path.join(ROOT, "profiles", "k_force_s150_ncu.json")
+    """Per-kernel ncu figures of the step kernels at 150^3 (per launch and per
+    element), if the profile summary was committed."""
+    path = os.path.join(ROOT, "profiles", "step_kernels_s150_ncu.json")
     if os.path.exists(path):
         with open(path) as f:
             return json.load(f)
-    return None
+    return {}
 
 
 class ClockSampler:
@@ -482,27 +486,29 @@ def run_ours(args):
 
     peaks, peak_kind = _measured_peaks()
     hbm = float(peaks.get("hbm_gbs", 6800.0))
-    force_ms = ktimes.get("k_force", 0.0) / cycles
-    dominant = max(ktimes, key=ktimes.get)
-    force_bytes = FORCE_BYTES_PER_ELEM * E + FORCE_BYTES_PER_NODE * N
-    achieved = force_bytes / (force_ms * 1e-3) / 1e9
-    prof = _profile_numbers()
+    # the roofline of the dominant step kernel (the one with the most time)
+    dominant = max((k for k in ktimes if k in KERNEL_BYTES), key=ktimes.get)
+    dom_ms = ktimes[dominant] / cycles
+    be, bn = KERNEL_BYTES[dominant]
+    dom_bytes = be * E + bn * N
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    prof = _profile_numbers().get(dominant, {})
     # the committed capture's per-launch figures are of the 150^3 problem
-    # (3,375,000 elements); both grow with the elements of the run's problem
+    # (3,375,000 elements); they grow with the elements of the run's problem
     prof_scale = E / 3375000.0
-    traffic = prof["dram_bytes_per_launch"] * prof_scale if prof and prof.get("dram_bytes_per_launch") else None
-    roofline = {"bound": "hbm", "kernel": "k_force", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+    traffic = prof["dram_bytes_per_launch"] * prof_scale if prof.get("dram_bytes_per_launch") else None
+    roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
                 "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
-                "algorithmic_bytes_per_launch": force_bytes}
+                "algorithmic_bytes_per_launch": dom_bytes}
     step_bytes = STEP_BYTES_PER_ELEM * E + STEP_BYTES_PER_NODE * N
     step_gbs = step_bytes * cycles / (ms * 1e-3) / 1e9
     fp64 = {"bound": "fp64", "peak_fma_per_s": fma_s.value, "peak_add_per_s": add_s.value,
             "peak_source": "lulesh_measure_fp64_peak (this run, this GPU)"}
-    if prof and prof.get("fp64_inst_per_element"):
+    if prof.get("fp64_inst_per_element"):
         inst = prof["fp64_inst_per_element"] * E
-        rate = inst / (force_ms * 1e-3)
-        fp64.update({"kernel": "k_force", "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
+        rate = inst / (dom_ms * 1e-3)
+        fp64.update({"kernel": dominant, "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
                      "fp64_inst_per_launch": inst, "fp64_inst_per_element": prof["fp64_inst_per_element"]})
 
     g.close()  # the remaining legs build their own problems
