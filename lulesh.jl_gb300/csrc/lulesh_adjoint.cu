@@ -97,7 +97,9 @@ struct lulesh_adjoint {
   std::vector<void*> set1_allocs;
   bool overlap = true;           // overlap recompute and transpose when set 1 fits
   cudaStream_t rstream = nullptr;  // recompute stream of the overlapped sweep
-  cudaEvent_t ev_start = nullptr, ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  cudaStream_t tstream = nullptr;  // transpose stream of the overlapped sweep (high priority)
+  cudaEvent_t ev_start = nullptr, ev_done = nullptr;
+  cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
   std::vector<StateBuf> ckpts;   // segment start states
   std::vector<int> seg_len;      // cycles of each segment
   DevState* ckpt_st = nullptr;   // device: step state at each checkpoint
@@ -178,8 +180,11 @@ static void free_set1(lulesh_adjoint* a) {
   a->sets[1] = TapeSet{};
 }
 
-// Set 1, the stream and the events of the overlapped reverse sweep; false
-// (sequential sweep) when they do not fit.
+// Set 1, the streams and the events of the overlapped reverse sweep; false
+// (sequential sweep) when they do not fit. The transposes are the sweep's
+// critical path, so their stream takes the device's highest priority: the
+// block scheduler gives them the SMs first and the recompute fills what they
+// leave idle (partial waves, latency-bound phases).
 static bool ensure_overlap(lulesh_adjoint* a) {
   if (!a->overlap) return false;
   if (a->sets[1].ready) return true;
@@ -188,7 +193,16 @@ static bool ensure_overlap(lulesh_adjoint* a) {
     a->rstream = nullptr;
     return false;
   }
-  cudaEvent_t* evs[5] = {&a->ev_start, &a->ev_ready[0], &a->ev_ready[1], &a->ev_free[0], &a->ev_free[1]};
+  if (!a->tstream) {
+    int least = 0, greatest = 0;
+    if (cudaDeviceGetStreamPriorityRange(&least, &greatest) != cudaSuccess ||
+        cudaStreamCreateWithPriority(&a->tstream, cudaStreamNonBlocking, greatest) != cudaSuccess) {
+      cudaGetLastError();
+      a->tstream = nullptr;
+      return false;
+    }
+  }
+  cudaEvent_t* evs[6] = {&a->ev_start, &a->ev_done, &a->ev_ready[0], &a->ev_ready[1], &a->ev_free[0], &a->ev_free[1]};
   for (cudaEvent_t* e : evs)
     if (!*e && cudaEventCreateWithFlags(e, cudaEventDisableTiming) != cudaSuccess) {
       cudaGetLastError();
@@ -509,10 +523,12 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   if (a->rec_graph[0]) cudaGraphExecDestroy(a->rec_graph[0]);
   if (a->tr_graph[0]) cudaGraphExecDestroy(a->tr_graph[0]);
   if (a->rstream) cudaStreamSynchronize(a->rstream);
+  if (a->tstream) cudaStreamSynchronize(a->tstream);
   free_set1(a);
-  for (cudaEvent_t e : {a->ev_start, a->ev_ready[0], a->ev_ready[1], a->ev_free[0], a->ev_free[1]})
+  for (cudaEvent_t e : {a->ev_start, a->ev_done, a->ev_ready[0], a->ev_ready[1], a->ev_free[0], a->ev_free[1]})
     if (e) cudaEventDestroy(e);
   if (a->rstream) cudaStreamDestroy(a->rstream);
+  if (a->tstream) cudaStreamDestroy(a->tstream);
   for (void* p : a->allocs) cudaFree(p);
   delete a;
   return LULESH_OK;
@@ -523,6 +539,7 @@ int lulesh_adj_set_overlap(lulesh_adjoint* a, int32_t enable) {
   ACK(cudaSetDevice(a->dom->params.device));
   ACK(cudaStreamSynchronize(a->dom->stream));
   if (a->rstream) ACK(cudaStreamSynchronize(a->rstream));
+  if (a->tstream) ACK(cudaStreamSynchronize(a->tstream));
   a->overlap = enable != 0;
   if (!a->overlap) {
     free_set1(a);
@@ -570,11 +587,12 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   int rc;
   // ---- forward sweep with checkpoints ----
   // Segments of K cycles: each starts by copying the state and the device step
-  // state to its checkpoint; every segment but the last then runs as a
-  // captured graph of exactly K cycles (dt on the device; once time reaches
-  // stoptime, as in the examples/benchmark.jl loop, the remaining cycles are
-  // no-ops), and the last runs taped so that the reverse sweep need not
-  // recompute it. Nothing waits on the host until the sweep ends.
+  // state to its checkpoint; the segments then run as captured graphs of
+  // exactly K cycles (dt on the device; once time reaches stoptime, as in the
+  // examples/benchmark.jl loop, the remaining cycles are no-ops), except the
+  // last one (the last two when the sweep overlaps and has both tape sets),
+  // which run taped so that the reverse sweep need not recompute them.
+  // Nothing waits on the host until the sweep ends.
   auto t0 = std::chrono::steady_clock::now();
   const int nplan = (int)((num_cycles + K - 1) / K);
   const int last_len = (int)(num_cycles - (int64_t)(nplan - 1) * K);
@@ -593,6 +611,8 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   // segment k's tape set: k & 1 when recompute and transpose overlap
   const bool pipe = nplan > 1 && ensure_overlap(a);
   auto set_of = [&](int k) -> TapeSet& { return a->sets[pipe ? (k & 1) : 0]; };
+  // segments k >= first_taped are taped by the forward sweep itself
+  const int first_taped = nplan - (pipe ? std::min(2, nplan) : 1);
   if (nplan > 1 && (!a->fwd_graph || std::memcmp(&a->fwd_prm, &prm, sizeof(Params)) != 0 ||
                     std::memcmp(&a->fwd_tuning, &d->tuning, sizeof(Tuning)) != 0 || a->fwd_aux != aux)) {
     if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
@@ -625,14 +645,14 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   for (int k = 0; k < nplan; ++k) {
     copy_state_from_domain(a, a->ckpts[k], s);
     ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
-    if (k < nplan - 1) {
+    if (k < first_taped) {
       ACK(cudaGraphLaunch(a->fwd_graph, s));
     } else {
       TapeSet& ts = set_of(k);
+      const int n = k < nplan - 1 ? K : last_len;
       tape_segment_begin(a, ts.tape[0], s);
-      for (int j = 0; j < last_len; ++j)
-        tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < last_len ? &ts.tape[j + 1] : nullptr, ts.rec + j, s);
-      copy_state_from_domain(a, ts.slots[last_len], s);
+      for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < n ? &ts.tape[j + 1] : nullptr, ts.rec + j, s);
+      copy_state_from_domain(a, ts.slots[n], s);
     }
   }
   ACK(cudaGetLastError());
@@ -649,7 +669,6 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     a->seg_len.push_back((int)len);
   }
   const int nseg = (int)a->seg_len.size();
-  const bool last_taped = nseg == nplan;
   if (d->status) { out.status = d->status; out.cycles = done; if (res) *res = out; return d->status; }
   auto t1 = std::chrono::steady_clock::now();
   out.cycles = done;
@@ -663,13 +682,15 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
   // Recompute R(k) (checkpoint k restored into the domain, its cycles taped
   // into set_of(k)) and transpose T(k) (the adjoint state through those
-  // cycles, in reverse). T runs on the domain's stream in order k = nseg-1..0.
-  // Overlapped, R runs on its own stream one segment ahead: R(k-1) is queued
-  // before T(k), waits until T(k+1) has released its set, and T(k) waits for
-  // R(k). Sequential, R(k) runs right before T(k) on the domain's stream.
-  // Full segments run as captured graphs (one per set and phase, rebuilt
-  // when the parameters they bake in change).
+  // cycles, in reverse), in order k = nseg-1..0; segments the forward sweep
+  // taped skip R. Overlapped, T runs on the high-priority transpose stream
+  // and R on its own stream one segment ahead: R(k-1) is queued before T(k),
+  // waits until T(k+1) has released its set, and T(k) waits for R(k); the
+  // domain's stream joins both at the end. Sequential, R(k) runs right before
+  // T(k) on the domain's stream. Full segments run as captured graphs (one
+  // per set and phase, rebuilt when the parameters they bake in change).
   cudaStream_t rs = pipe ? a->rstream : s;
+  cudaStream_t tst = pipe ? a->tstream : s;
   auto queue_recompute = [&](TapeSet& ts, int n, cudaStream_t st) {
     tape_segment_begin(a, ts.tape[0], st);
     for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < n ? &ts.tape[j + 1] : nullptr, ts.rec + j, st);
@@ -704,9 +725,9 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   for (int x = 0; x < nsets && any_full; ++x) {
     TapeSet& ts = a->sets[x];
     if (!a->rec_graph[x] && (rc = capture(&a->rec_graph[x], rs, [&] { queue_recompute(ts, K, rs); }))) return rc;
-    if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], s, [&] { queue_transpose(ts, K, s); }))) return rc;
+    if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], tst, [&] { queue_transpose(ts, K, tst); }))) return rc;
   }
-  auto recomputed = [&](int k) { return !(k == nseg - 1 && last_taped); };
+  auto recomputed = [&](int k) { return k < first_taped; };
   auto enqueue_R = [&](int k) -> int {
     const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
     if (pipe && k + 2 <= nseg - 1) ACK(cudaStreamWaitEvent(rs, a->ev_free[x], 0));
@@ -718,23 +739,28 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     return LULESH_OK;
   };
   if (pipe) {
-    // the recompute stream starts once the objective and the final state are taken
+    // both streams start once the objective and the final state are taken
     ACK(cudaEventRecord(a->ev_start, s));
     ACK(cudaStreamWaitEvent(rs, a->ev_start, 0));
+    ACK(cudaStreamWaitEvent(tst, a->ev_start, 0));
     if (recomputed(nseg - 1) && (rc = enqueue_R(nseg - 1))) return rc;
   }
   for (int k = nseg - 1; k >= 0; --k) {
     const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
     if (pipe) {
-      if (k >= 1 && (rc = enqueue_R(k - 1))) return rc;
-      if (recomputed(k)) ACK(cudaStreamWaitEvent(s, a->ev_ready[x], 0));
+      if (k >= 1 && recomputed(k - 1) && (rc = enqueue_R(k - 1))) return rc;
+      if (recomputed(k)) ACK(cudaStreamWaitEvent(tst, a->ev_ready[x], 0));
     } else if (recomputed(k) && (rc = enqueue_R(k))) {
       return rc;
     }
-    if (n == K) ACK(cudaGraphLaunch(a->tr_graph[x], s));
-    else queue_transpose(a->sets[x], n, s);
-    if (pipe) ACK(cudaEventRecord(a->ev_free[x], s));
+    if (n == K) ACK(cudaGraphLaunch(a->tr_graph[x], tst));
+    else queue_transpose(a->sets[x], n, tst);
+    if (pipe) ACK(cudaEventRecord(a->ev_free[x], tst));
     ACK(cudaGetLastError());
+  }
+  if (pipe) {
+    ACK(cudaEventRecord(a->ev_done, tst));
+    ACK(cudaStreamWaitEvent(s, a->ev_done, 0));
   }
   // the first cycle's force transpose is still in the force corner buffers
   ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);

@@ -90,12 +90,19 @@ __device__ __forceinline__ void position_walsh(const double x[8], const double y
 }
 
 // integrateStressForElems' detJ <= 0 check (src/domain.jl:1101-1105): the
-// sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019).
+// sign of 8*(fjxet*cjxet + fjyet*cjyet + fjzet*cjzet) (src/domain.jl:2019),
+// with the eta cofactor column c = W_zeta x W_xi (also the monotonic-Q
+// gradient's eta direction).
+__device__ __forceinline__ void eta_cofactors(const double w[3][3], double c[3]) {
+  cross(w[0][2], w[1][2], w[2][2], w[0][0], w[1][0], w[2][0], c[0], c[1], c[2]);
+}
+__device__ __forceinline__ double jacobian_det(const double w[3][3], const double c[3]) {
+  return fma(w[0][1], c[0], fma(w[1][1], c[1], w[2][1] * c[2]));
+}
 __device__ __forceinline__ double jacobian_det(const double w[3][3]) {
-  const double cxet = fma(w[2][0], w[1][2], -(w[1][0] * w[2][2]));
-  const double cyet = fma(w[0][0], w[2][2], -(w[2][0] * w[0][2]));
-  const double czet = fma(w[1][0], w[0][2], -(w[0][0] * w[1][2]));
-  return fma(w[0][1], cxet, fma(w[1][1], cyet, w[2][1] * czet));
+  double c[3];
+  eta_cofactors(w, c);
+  return jacobian_det(w, c);
 }
 
 // Face f's area vector times -8: the cross product of its two diagonals.
@@ -445,6 +452,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
   // kernel's geometry of these positions is stored too.
   double volume, charLength = 0.0;
   double w[3][3];  // first-order Walsh vectors (xi, eta, zeta) of x, y, z
+  double cet[3];   // W_zeta x W_xi
   {
     double g[12][3], hm[3][4], n[6][3], U[3][3], gU[3][3], gV[3][3], gW[3][3];
     face_diagonals(x, y, z, g);
@@ -497,7 +505,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
       double B[3][4], pz01, ny4, gr[3][8];
       node_normals(n, B, pz01, ny4);
       volume_derivatives(gU, gV, gW, gr);
-      store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w));
+      eta_cofactors(w, cet);
+      store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w, cet));
     }
   }
   const double* wx = w[0];
@@ -609,8 +618,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     d.delx_xi[e] = vol16 * rs;
     d.delv_xi[e] = norm64 * fma(ax, vxw[0], fma(ay, vyw[0], az * vzw[0]));
     tape_a(0);
-    // eta: zeta x xi
-    cross(wx[2], wy[2], wz[2], wx[0], wy[0], wz[0], ax, ay, az);
+    // eta: zeta x xi (formed for the detJ check)
+    ax = cet[0]; ay = cet[1]; az = cet[2];
     rs = rsqrt(fma(ax, ax, fma(ay, ay, fma(az, az, 256.0 * ptiny))));
     d.delx_eta[e] = vol16 * rs;
     d.delv_eta[e] = norm64 * fma(ax, vxw[1], fma(ay, vyw[1], az * vzw[1]));
