@@ -469,7 +469,7 @@ def run_ours(args):
         L.timeIncrement(g)
         L.lagrangeLeapFrog(g)
     for f in STATE_FIELDS:
-        host[f][:] = g.field(f)
+        g.field(f, out=host[f])
     e2e_s = max_over_ranks(time.perf_counter() - t0, world)
     e2e = {"value": world * E * cycles / e2e_s, "unit": UNIT,
            "h2d_bytes_per_step": scalar_bytes + state_bytes / cycles,

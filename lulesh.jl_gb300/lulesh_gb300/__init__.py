@@ -267,11 +267,18 @@ class Domain:
         except Exception:
             pass
 
-    def field(self, name):
+    def field(self, name, out=None):
+        """A copy of the field on the host; with `out` (a C-contiguous array of
+        the field's dtype and length, e.g. in pinned memory) the copy lands
+        there directly and `out` is returned."""
         fid, dt = FIELDS[name]
         n = ctypes.c_int64()
         _check(self._L.lulesh_field_length(self._h, fid, ctypes.byref(n)), f"length of {name}")
-        out = np.empty(n.value, dtype=dt)
+        if out is None:
+            out = np.empty(n.value, dtype=dt)
+        elif (not isinstance(out, np.ndarray) or out.dtype != np.dtype(dt) or out.size != n.value
+              or not out.flags.c_contiguous or not out.flags.writeable):
+            raise ValueError(f"out must be a writeable C-contiguous {np.dtype(dt)} array of {n.value} values")
         _check(self._L.lulesh_download_field(self._h, fid, out.ctypes.data_as(ctypes.c_void_p), n.value),
                f"download {name}")
         return out

@@ -179,15 +179,17 @@ def test_checkpoint_interval_and_final_state(gpu_lib):
             assert np.array_equal(other[2][f], grads[0][2][f]), f
 
 
-@pytest.mark.parametrize("stop_early", [False, True])
-def test_overlapped_and_sequential_sweeps_agree(gpu_lib, stop_early):
+@pytest.mark.parametrize("every,stop_early", [(7, False), (7, True), (14, False)])
+def test_overlapped_and_sequential_sweeps_agree(gpu_lib, every, stop_early):
     """The reverse sweep that recomputes one segment while it transposes the
-    next (two tapes) gives bitwise the gradients of the sequential sweep (one
-    tape): 27 cycles in segments of 7 (a partial last one), and a run that
-    reaches stoptime after about 17 cycles (its last segment recomputed, not
-    taped during the forward sweep)."""
+    next (two tapes, the forward sweep taping the last two segments) gives
+    bitwise the gradients of the sequential sweep (one tape, the last segment
+    taped): 27 cycles in segments of 7 (a partial last one); a run that
+    reaches stoptime after about 17 cycles, inside the third segment (taped
+    by the overlapped forward sweep, recomputed by the sequential one); and
+    segments of 14, both taped by the overlapped forward sweep."""
     L = gpu_lib
-    nx, cycles, every = 8, 27, 7
+    nx, cycles = 8, 27
     g = developed(L, nx, 0, 0, 0xC7)
     snap = snapshot(g)
     stoptime = g.stoptime
@@ -208,7 +210,7 @@ def test_overlapped_and_sequential_sweeps_agree(gpu_lib, stop_early):
         if stop_early:
             assert 17 <= adj.result.cycles < cycles
         else:
-            assert adj.result.cycles == cycles and adj.result.checkpoints == 4
+            assert adj.result.cycles == cycles and adj.result.checkpoints == -(-cycles // every)
         out.append((loss, adj.result.grad_hgcoef, {f: adj.grad(f) for f in STATE},
                     {f: g.field(f) for f in STATE}))
         adj.close()

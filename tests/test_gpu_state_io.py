@@ -53,3 +53,22 @@ def test_reader_and_rejections(gpu_lib, tmp_path):
     assert np.array_equal(fresh.field("x"), before) and fresh.cycle == 0
     with pytest.raises(ValueError):
         L.read_state(str(bad))
+
+
+def test_field_download_into_caller_buffer(gpu_lib):
+    """Domain.field(name, out=buf) copies into the caller's buffer (pinned
+    memory in the end-to-end timing) the values field(name) returns; a buffer
+    of the wrong dtype, length or layout is refused before any copy."""
+    torch = pytest.importorskip("torch")
+    L = gpu_lib
+    g = L.Domain(L.LuleshProblem(nx=10))
+    L.run(g, 5)
+    for f in STATE:
+        ref = g.field(f)
+        buf = torch.empty(ref.size, dtype=torch.float64, pin_memory=True).numpy()
+        assert g.field(f, out=buf) is buf
+        assert np.array_equal(buf, ref), f
+    n = g.field("e").size
+    for bad in (np.empty(n, np.float32), np.empty(n - 1), np.empty((n, 2))[:, 0]):
+        with pytest.raises(ValueError):
+            g.field("e", out=bad)
