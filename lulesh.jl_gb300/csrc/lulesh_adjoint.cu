@@ -292,6 +292,7 @@ static void set_cycle_pointers(lulesh_adjoint* a, const StateBuf& s0, const Stat
   ad.x0 = s0.f[0]; ad.y0 = s0.f[1]; ad.z0 = s0.f[2]; ad.xd0 = s0.f[3]; ad.yd0 = s0.f[4]; ad.zd0 = s0.f[5];
   ad.e0 = s0.f[6]; ad.p0 = s0.f[7]; ad.q0 = s0.f[8]; ad.v0 = s0.f[9]; ad.ss0 = s0.f[10];
   ad.x1 = s1.f[0]; ad.y1 = s1.f[1]; ad.z1 = s1.f[2]; ad.xd1 = s1.f[3]; ad.yd1 = s1.f[4]; ad.zd1 = s1.f[5];
+  ad.p1 = s1.f[7]; ad.q1 = s1.f[8];
   ad.ax = t.ax; ad.ay = t.ay; ad.az = t.az;
   ad.vnew = t.vnew; ad.delv = t.delv; ad.arealg = t.arealg; ad.vdov = t.vdov;
   for (int k = 0; k < 3; ++k) { ad.dvl[k] = t.dv[k]; ad.dxl[k] = t.dx[k]; }
@@ -312,20 +313,35 @@ static void reverse_cycle(lulesh_adjoint* a, const CycleRec* rec, cudaStream_t s
   const double irho0 = 1.0 / prm.refdens;
   if (mode & 4) ka_material<4><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, irho0, rec, a->dsc);
   else ka_material<0><<<ge, kAdjBlock, 0, s>>>(a->ad, prm, irho0, rec, a->dsc);
-  ka_kinematics<<<ge, kAdjBlock, 0, s>>>(a->ad, rec);  // also gathers the limiter's neighbour reads
-  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, rec);        // also gathers the kinematics corners
   const double hg = d->sc[LULESH_S_HGCOEF];
-#define LULESH_KA_FORCE(M)                                   \
-  ka_hourglass<M><<<ge, kAdjBlock, 0, s>>>(a->ad, hg);       \
-  ka_force_geo<M><<<ge, kAdjBlock, 0, s>>>(a->ad)
+  // ka_kinematics also gathers the limiter's neighbour reads and does the
+  // position transpose of the next cycle's k_force; ka_node gathers the
+  // corners; ka_hourglass leaves this cycle's force terms for the
+  // ka_kinematics of the cycle before (or ka_force_geo after the first cycle)
+#define LULESH_KA_CYCLE(M)                                            \
+  ka_kinematics<M><<<ge, kAdjBlock, 0, s>>>(a->ad, rec);              \
+  ka_node<<<gn, kAdjBlock, 0, s>>>(a->ad, rec);                       \
+  ka_hourglass<M><<<ge, kAdjBlock, 0, s>>>(a->ad, hg)
   switch (mode & 3) {
-    case 0: LULESH_KA_FORCE(0); break;
-    case 1: LULESH_KA_FORCE(1); break;
-    case 2: LULESH_KA_FORCE(2); break;
-    default: LULESH_KA_FORCE(3); break;
+    case 0: LULESH_KA_CYCLE(0); break;
+    case 1: LULESH_KA_CYCLE(1); break;
+    case 2: LULESH_KA_CYCLE(2); break;
+    default: LULESH_KA_CYCLE(3); break;
   }
-#undef LULESH_KA_FORCE
+#undef LULESH_KA_CYCLE
   ka_cycle_close<<<1, kCloseBlock, 0, s>>>(a->ad, ge, gn, rec, a->dsc, prm);
+}
+
+// Position transpose of the run's first cycle's k_force (the last one the
+// reverse sweep reaches), into the force corner buffer.
+static void first_cycle_force_geo(lulesh_adjoint* a, cudaStream_t s) {
+  const int ge = (a->E + kAdjBlock - 1) / kAdjBlock;
+  switch (a->dom->dd.mode & 3) {
+    case 0: ka_force_geo<0><<<ge, kAdjBlock, 0, s>>>(a->ad); break;
+    case 1: ka_force_geo<1><<<ge, kAdjBlock, 0, s>>>(a->ad); break;
+    case 2: ka_force_geo<2><<<ge, kAdjBlock, 0, s>>>(a->ad); break;
+    default: ka_force_geo<3><<<ge, kAdjBlock, 0, s>>>(a->ad); break;
+  }
 }
 
 static double* adj_field(lulesh_adjoint* a, int32_t f) {
@@ -422,7 +438,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
       (rc = dalloc(a, &ad.ldelv, E)) || (rc = dalloc(a, &ad.larealg, E)) || (rc = dalloc(a, &ad.lvdov, E)) ||
       (rc = dalloc(a, &ad.lnb, 6 * (size_t)E)) || (rc = dalloc(a, &ad.cX, 24 * (size_t)E)) ||
       (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) ||
-      (rc = dalloc(a, &ad.fX, 24 * (size_t)E)) || (rc = dalloc(a, &ad.fV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
+      (rc = dalloc(a, &ad.fX, 24 * (size_t)E)) || (rc = dalloc(a, &ad.fV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLU, 15 * (size_t)E)) ||
       (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
       (rc = dalloc(a, &ad.part_dtn, gn)) || (rc = dalloc(a, &ad.part_hg, ge)) || (rc = dalloc(a, &a->scal, 4)) ||
       (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
@@ -678,8 +694,12 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   const Scalars5 final_sc = get_scalars(d);
   // ---- reverse sweep ----
   ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
-  ACK(cudaMemsetAsync(a->ad.fX, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  // the force-transpose inputs the first transposed cycle's ka_kinematics
+  // reads (no cycle after it): zero
   ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLdv, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLhm, 0, 12 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLU, 0, 15 * sizeof(double) * (size_t)a->E, s));
   // Recompute R(k) (checkpoint k restored into the domain, its cycles taped
   // into set_of(k)) and transpose T(k) (the adjoint state through those
   // cycles, in reverse), in order k = nseg-1..0; segments the forward sweep
@@ -762,7 +782,10 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     ACK(cudaEventRecord(a->ev_done, tst));
     ACK(cudaStreamWaitEvent(s, a->ev_done, 0));
   }
-  // the first cycle's force transpose is still in the force corner buffers
+  // the first cycle's force transpose: its positions (segment 0's first
+  // tape, set 0), then both force corner buffers onto the node adjoints
+  set_cycle_pointers(a, a->sets[0].slots[0], a->sets[0].slots[1], a->sets[0].tape[0]);
+  first_cycle_force_geo(a, s);
   ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
   copy_state_to_domain(a, a->final_state, s);
   AdjScal hsc;

@@ -52,7 +52,7 @@ struct AdjDev {
   const int *nbStart, *nbList;  // inverse neighbour lists (entries slot*E + j)
   // cycle start state S0 and end positions/velocities S1
   const double *x0, *y0, *z0, *xd0, *yd0, *zd0, *e0, *p0, *q0, *v0, *ss0;
-  const double *x1, *y1, *z1, *xd1, *yd1, *zd1;
+  const double *x1, *y1, *z1, *xd1, *yd1, *zd1, *p1, *q1;
   // tape of the cycle
   const double *ax, *ay, *az;                 // accelerations (N)
   const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
@@ -60,7 +60,7 @@ struct AdjDev {
   const unsigned long long* flags;
   const double* geo;                          // [102][E] force-kernel tape (dv, hms, S, N, diagonals)
   const double* kin;                          // [90][E] kinematics-kernel tape
-  const double* mat;                          // [31][E] material-kernel tape                          // [48][E] force-kernel tape (dv, hms, S)
+  const double* mat;                          // [31][E] material-kernel tape
   // adjoints of the state (in place: S1 on entry, S0 on exit)
   double *lx, *ly, *lz, *lxd, *lyd, *lzd;     // N
   double *le, *lp, *lq, *lss, *lv;            // E
@@ -70,9 +70,11 @@ struct AdjDev {
   double *ldv[3], *ldx[3];                    // E
   double* lnb;                                // [6][E]: limiter neighbour slots
   double *cX, *cV;                            // [3][8][E] kinematics corner buffers
-  double *fX, *fV;                            // [3][8][E] force corner buffers (gathered one cycle later)
+  double *fX, *fV;                            // [3][8][E] force corner buffers: the first cycle's position
+                                              // transpose; each cycle's hourglass velocity corners
   double *part_dt, *part_dtn, *part_hg;       // per-block partial sums (kinematics, node, force)
   double *sLdv, *sLhm;                        // [3][8][E], [3][4][E]: hourglass -> geometry
+  double* sLU;                                // [5][3][E]: the stress force's face terms (hourglass -> geometry)
 };
 
 // Deterministic block sum (fixed tree order); thread 0 writes the block's sum.
@@ -347,11 +349,27 @@ __device__ __forceinline__ void walsh1_t(const double Lw[3], double L[8]) {
   L[4] += Ld; L[2] -= Ld;
 }
 
+// Transpose of the hourglass mode transform: out[n] = sum_m gamma[n][m] t[m]
+// (12 adds).
+__device__ __forceinline__ void walsh_modes_t(const double t[4], double out[8]) {
+  const double cm = t[2] - t[3], cp = t[2] + t[3];
+  const double s = t[0] + t[1], d = t[0] - t[1];
+  out[0] = s + cm; out[1] = d - cm; out[2] = cm - s; out[3] = -d - cm;
+  out[4] = cp - s; out[5] = -d - cp; out[6] = s + cp; out[7] = d - cp;
+}
+
 // ---------------------------------------------------------------------------
 // ka_kinematics: transpose of k_kinematics (volume, characteristic length,
 // velocity-gradient trace, monotonic-Q gradients), into the corner buffers.
+// The cycle's end positions are the next cycle's start positions, so the
+// position transpose of the next cycle's k_force (what force_geo_t does for
+// the first cycle) joins it here, from what that cycle's ka_hourglass left:
+// its modes' transpose starts the position corners, its volume-derivative
+// Hessian-vector product merges with this cycle's volume gradient, and its
+// stress terms add to the same face-diagonal adjoints, scattered once.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kAdjBlock, 4) ka_kinematics(AdjDev a, const CycleRec* rec) {
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock, 3) ka_kinematics(AdjDev a, const CycleRec* rec) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   const double dt = rec->dt;
@@ -359,11 +377,6 @@ __global__ void __launch_bounds__(kAdjBlock, 4) ka_kinematics(AdjDev a, const Cy
   if (e < E) {
     // forward values from the kinematics kernel's tape (slots: see tapeKin)
     auto tk = [&](int q) { return a.kin[q * E + e]; };
-    double LX[3][8], LV[3][8];
-#pragma unroll
-    for (int k = 0; k < 3; ++k)
-#pragma unroll
-      for (int c = 0; c < 8; ++c) { LX[k][c] = 0.0; LV[k][c] = 0.0; }
 
     const double vnew = a.vnew[e], volo = a.volo[e];
     double Lvnew = a.lvnew[e] + a.ldelv[e];
@@ -448,7 +461,18 @@ __global__ void __launch_bounds__(kAdjBlock, 4) ka_kinematics(AdjDev a, const Cy
         Ldt += -0.5 * vdot(LF[d], VW[d]);
       }
     }
-    // Walsh transposes
+    // Walsh transposes; the position corners start from the next cycle's
+    // hourglass-mode transpose Gamma^T dL/dhm
+    double LX[3][8], LV[3][8];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double t[4];
+#pragma unroll
+      for (int m = 0; m < 4; ++m) t[m] = a.sLhm[(k * 4 + m) * E + e];
+      walsh_modes_t(t, LX[k]);
+#pragma unroll
+      for (int c = 0; c < 8; ++c) LV[k][c] = 0.0;
+    }
     {
       const double lwx[3] = {LW[0].x, LW[1].x, LW[2].x}, lwy[3] = {LW[0].y, LW[1].y, LW[2].y},
                    lwz[3] = {LW[0].z, LW[1].z, LW[2].z};
@@ -457,67 +481,116 @@ __global__ void __launch_bounds__(kAdjBlock, 4) ka_kinematics(AdjDev a, const Cy
                    lvz[3] = {LVW[0].z, LVW[1].z, LVW[2].z};
       walsh1_t(lvx, LV[0]); walsh1_t(lvy, LV[1]); walsh1_t(lvz, LV[2]);
     }
-    // ---- volume and characteristic length ----
+    // the velocity corners, plus the hourglass velocity corners of the cycle
+    // after this one
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+#pragma unroll
+      for (int c = 0; c < 8; ++c) a.cV[(k * 8 + c) * E + e] = LV[k][c] + a.fV[(k * 8 + c) * E + e];
+    // ---- volume and characteristic length, and the position transpose of
+    //      the next cycle's k_force (same positions, same face diagonals) ----
     {
-      // the 12 diagonals of the new positions, from the tape
+      // the 12 diagonals of the new positions are on the tape in the order
+      // d61 d70 d63 d20 d50 d64 d31 d72 d43 d57 d14 d25
       auto dg = [&](int q) { return v3(tk(45 + 3 * q), tk(46 + 3 * q), tk(47 + 3 * q)); };
-      const V3 d61 = dg(0), d70 = dg(1), d63 = dg(2), d20 = dg(3), d50 = dg(4), d64 = dg(5);
-      const V3 d31 = dg(6), d72 = dg(7), d43 = dg(8), d57 = dg(9), d14 = dg(10), d25 = dg(11);
-      // the three triple products of calcElemVolume: U.(V x W)
-      V3 U1 = d31; vadd(U1, d72);
-      V3 U2 = d43; vadd(U2, d57);
-      V3 U3 = d14; vadd(U3, d25);
       const double volume = vnew * volo;  // vnew = volume / volo
-      // characteristic length from the face the tape recorded
-      // (selected without indexing, so the diagonals stay in registers)
+      // characteristic length from the face the tape recorded: its diagonals
+      // fa, fb (kinematics face order (d20, d31) (d64, d57) (d50, d14)
+      // (d61, d25) (d72, d63) (d43, d70))
       const int f = (int)((a.flags[e] >> TF_FACE_SHIFT) & 7ull);
-      V3 fa = d20, fb = d31;
-      if (f == 1) { fa = d64; fb = d57; }
-      else if (f == 2) { fa = d50; fb = d14; }
-      else if (f == 3) { fa = d61; fb = d25; }
-      else if (f == 4) { fa = d72; fb = d63; }
-      else if (f == 5) { fa = d43; fb = d70; }
+      const int qa = f == 0 ? 3 : f == 1 ? 5 : f == 2 ? 4 : f == 3 ? 0 : f == 4 ? 7 : 8;
+      const int qb = f == 0 ? 6 : f == 1 ? 9 : f == 2 ? 10 : f == 3 ? 11 : f == 4 ? 2 : 1;
       const V3 nf = v3(tk(41), tk(42), tk(43));  // fa x fb
       const double rsc = tk(44);                  // 1/|fa x fb|
       const double Lar = a.larealg[e];
       double Lvolume = Lar * 2.0 * rsc + Lvnew * a.inv_volo[e];
       const double Lcl = Lar * 2.0 * volume * (-0.5) * rsc * rsc * rsc;
       const V3 Ln = v3(2.0 * nf.x * Lcl, 2.0 * nf.y * Lcl, 2.0 * nf.z * Lcl);
-      const V3 Lfa = vcross(fb, Ln), Lfb = vcross(Ln, fa);
+      const V3 Lfa = vcross(dg(qb), Ln), Lfb = vcross(Ln, dg(qa));
       const double Lv12 = Lvolume * (1.0 / 12.0);
-      // gradients of the diagonals
-      V3 L61 = v3(0, 0, 0), L70 = v3(0, 0, 0), L63 = v3(0, 0, 0), L20 = v3(0, 0, 0), L50 = v3(0, 0, 0), L64 = v3(0, 0, 0);
-      V3 L31 = v3(0, 0, 0), L72 = v3(0, 0, 0), L43 = v3(0, 0, 0), L57 = v3(0, 0, 0), L14 = v3(0, 0, 0), L25 = v3(0, 0, 0);
-      {
-        // V x W of each triple product is taped; the other two factors are not
-        const V3 gU1 = v3(tk(81), tk(82), tk(83)), gV1 = vcross(d20, U1), gW1 = vcross(U1, d63);
-        vaxpy(L31, Lv12, gU1); vaxpy(L72, Lv12, gU1); vaxpy(L63, Lv12, gV1); vaxpy(L20, Lv12, gW1);
-        const V3 gU2 = v3(tk(84), tk(85), tk(86)), gV2 = vcross(d70, U2), gW2 = vcross(U2, d64);
-        vaxpy(L43, Lv12, gU2); vaxpy(L57, Lv12, gU2); vaxpy(L64, Lv12, gV2); vaxpy(L70, Lv12, gW2);
-        const V3 gU3 = v3(tk(87), tk(88), tk(89)), gV3 = vcross(d50, U3), gW3 = vcross(U3, d61);
-        vaxpy(L14, Lv12, gU3); vaxpy(L25, Lv12, gU3); vaxpy(L61, Lv12, gV3); vaxpy(L50, Lv12, gW3);
+      // The next cycle's force kernel used the gradient of 12*volume (its
+      // voluDer, dv): G = dL/ddv (zero before the first transposed cycle;
+      // the faithful slots 1 and 3 swapped back) makes its transpose the
+      // Hessian-vector product of the same triple products along G. With
+      // this cycle's Lv12 * gradient: dL/dU = Lv12 (V x W) + dV x W + V x dW,
+      // dL/dV = W x (Lv12 U + dU) + dW x U, dL/dW = (Lv12 U + dU) x V + U x dV,
+      // dU, dV, dW the differences of G along U, V, W (V x W is taped).
+      double G[3][8];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int c = 0; c < 8; ++c) G[j][c] = a.sLdv[(j * 8 + c) * E + e];
+      if (!(MODE & 2)) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) { const double t = G[j][1]; G[j][1] = G[j][3]; G[j][3] = t; }
       }
-      if (f == 0) { vadd(L20, Lfa); vadd(L31, Lfb); }
-      else if (f == 1) { vadd(L64, Lfa); vadd(L57, Lfb); }
-      else if (f == 2) { vadd(L50, Lfa); vadd(L14, Lfb); }
-      else if (f == 3) { vadd(L61, Lfa); vadd(L25, Lfb); }
-      else if (f == 4) { vadd(L72, Lfa); vadd(L63, Lfb); }
-      else { vadd(L43, Lfa); vadd(L70, Lfb); }
+      auto gd = [&](int p, int q) { return v3(G[0][p] - G[0][q], G[1][p] - G[1][q], G[2][p] - G[2][q]); };
+      auto triple_t = [&](const V3& U, const V3& V, const V3& W, const V3& gUt, const V3& dU, const V3& dV,
+                          const V3& dW, V3& LUa, V3& LUb, V3& LVd, V3& LWd) {
+        V3 A = dU; vaxpy(A, Lv12, U);
+        V3 gU = vcross(dV, W); vadd(gU, vcross(V, dW)); vaxpy(gU, Lv12, gUt);
+        V3 gV = vcross(W, A); vadd(gV, vcross(dW, U));
+        V3 gW = vcross(A, V); vadd(gW, vcross(U, dV));
+        vadd(LUa, gU); vadd(LUb, gU); vadd(LVd, gV); vadd(LWd, gW);
+      };
+      // The next cycle's stress force: face f's normal d1 x d2 (its
+      // diagonals, force order: faces (d20, d31) (d50, d14) (d61, d25)
+      // (d72, d36) (d43, d07), d36 = -d63, d07 = -d70) with LN = s8 LU_f
+      // gives d1 the adjoint d2 x LN and d2 the adjoint LN x d1; s8 from
+      // this cycle's end state.
+      const double s8 = ((-a.p1[e]) - a.q1[e]) * 0.125;
+      auto LN = [&](int fc) {
+        return v3(s8 * a.sLU[(fc * 3) * E + e], s8 * a.sLU[(fc * 3 + 1) * E + e], s8 * a.sLU[(fc * 3 + 2) * E + e]);
+      };
       auto put = [&](const V3& L, int p, int q) {
         LX[0][p] += L.x; LX[1][p] += L.y; LX[2][p] += L.z;
         LX[0][q] -= L.x; LX[1][q] -= L.y; LX[2][q] -= L.z;
       };
-      put(L61, 6, 1); put(L70, 7, 0); put(L63, 6, 3); put(L20, 2, 0); put(L50, 5, 0); put(L64, 6, 4);
-      put(L31, 3, 1); put(L72, 7, 2); put(L43, 4, 3); put(L57, 5, 7); put(L14, 1, 4); put(L25, 2, 5);
+      const V3 z0 = v3(0, 0, 0);
+      // Each triple product's four diagonals take adjoints from it, from two
+      // or one of the stress faces and possibly the characteristic face, and
+      // from nothing else: three disjoint groups, each scattered once.
+      {  // (d31 + d72).(d63 x d20), faces 0 and 3, characteristic faces 0 and 4
+        const V3 d63 = dg(2), d20 = dg(3), d31 = dg(6), d72 = dg(7);
+        V3 L63 = z0, L20 = z0, L31 = z0, L72 = z0;
+        V3 U = d31; vadd(U, d72);
+        V3 dU = gd(3, 1); vadd(dU, gd(7, 2));
+        triple_t(U, d63, d20, v3(tk(81), tk(82), tk(83)), dU, gd(6, 3), gd(2, 0), L31, L72, L63, L20);
+        { const V3 n = LN(0); vadd(L20, vcross(d31, n)); vadd(L31, vcross(n, d20)); }
+        { const V3 n = LN(3); vadd(L72, vcross(n, d63)); vadd(L63, vcross(d72, n)); }
+        if (f == 0) { vadd(L20, Lfa); vadd(L31, Lfb); }
+        else if (f == 4) { vadd(L72, Lfa); vadd(L63, Lfb); }
+        put(L63, 6, 3); put(L20, 2, 0); put(L31, 3, 1); put(L72, 7, 2);
+      }
+      {  // (d43 + d57).(d64 x d70), face 4, characteristic faces 1 and 5
+        const V3 d70 = dg(1), d64 = dg(5), d43 = dg(8), d57 = dg(9);
+        V3 L70 = z0, L64 = z0, L43 = z0, L57 = z0;
+        V3 U = d43; vadd(U, d57);
+        V3 dU = gd(4, 3); vadd(dU, gd(5, 7));
+        triple_t(U, d64, d70, v3(tk(84), tk(85), tk(86)), dU, gd(6, 4), gd(7, 0), L43, L57, L64, L70);
+        { const V3 n = LN(4); vadd(L43, vcross(n, d70)); vadd(L70, vcross(d43, n)); }
+        if (f == 1) { vadd(L64, Lfa); vadd(L57, Lfb); }
+        else if (f == 5) { vadd(L43, Lfa); vadd(L70, Lfb); }
+        put(L70, 7, 0); put(L64, 6, 4); put(L43, 4, 3); put(L57, 5, 7);
+      }
+      {  // (d14 + d25).(d61 x d50), faces 1 and 2, characteristic faces 2 and 3
+        const V3 d61 = dg(0), d50 = dg(4), d14 = dg(10), d25 = dg(11);
+        V3 L61 = z0, L50 = z0, L14 = z0, L25 = z0;
+        V3 U = d14; vadd(U, d25);
+        V3 dU = gd(1, 4); vadd(dU, gd(2, 5));
+        triple_t(U, d61, d50, v3(tk(87), tk(88), tk(89)), dU, gd(6, 1), gd(5, 0), L14, L25, L61, L50);
+        { const V3 n = LN(1); vadd(L50, vcross(d14, n)); vadd(L14, vcross(n, d50)); }
+        { const V3 n = LN(2); vadd(L61, vcross(d25, n)); vadd(L25, vcross(n, d61)); }
+        if (f == 2) { vadd(L50, Lfa); vadd(L14, Lfb); }
+        else if (f == 3) { vadd(L61, Lfa); vadd(L25, Lfb); }
+        put(L61, 6, 1); put(L50, 5, 0); put(L14, 1, 4); put(L25, 2, 5);
+      }
     }
+    // the position corners
 #pragma unroll
     for (int k = 0; k < 3; ++k)
 #pragma unroll
-      for (int c = 0; c < 8; ++c) {
-        // plus the pending force-transpose corners of the cycle after this one
-        a.cX[(k * 8 + c) * E + e] = LX[k][c] + a.fX[(k * 8 + c) * E + e];
-        a.cV[(k * 8 + c) * E + e] = LV[k][c] + a.fV[(k * 8 + c) * E + e];
-      }
+      for (int c = 0; c < 8; ++c) a.cX[(k * 8 + c) * E + e] = LX[k][c];
   }
   block_sum_to(Ldt, a.part_dt);
 }
@@ -597,15 +670,6 @@ __global__ void __launch_bounds__(kAdjBlock) ka_node(AdjDev a, const CycleRec* r
 // ka_force_geo (the stress force and those geometric factors onto the
 // positions).
 // ---------------------------------------------------------------------------
-
-// Transpose of the hourglass mode transform: out[n] = sum_m gamma[n][m] t[m]
-// (12 adds).
-__device__ __forceinline__ void walsh_modes_t(const double t[4], double out[8]) {
-  const double cm = t[2] - t[3], cp = t[2] + t[3];
-  const double s = t[0] + t[1], d = t[0] - t[1];
-  out[0] = s + cm; out[1] = d - cm; out[2] = cm - s; out[3] = -d - cm;
-  out[4] = cp - s; out[5] = -d - cp; out[6] = s + cp; out[7] = d - cp;
-}
 
 // The 8 volume derivatives (times 12) of one coordinate pair, in the forward
 // kernel's slot order: dv_x uses (ey, ez), dv_y (ex, ez), dv_z (ey, ex) with
@@ -780,32 +844,77 @@ __global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoe
       const double Ldeterm = (Lcoef * c0 * ss * mass * (-1.0 / 3.0) * r - Lvi12) * inv_det;
       a.lv[e] += Ldeterm * a.volo[e];
     }
+    // stress part of the force, f = s8 * B with s8 = (-p - q)/8. The forward
+    // forms B0..B3 from faces 0-4 (node n's three face cross products) and
+    // the opposite corners as B6 = -B0, B7 = -B1, B4 = -B2, B5 = -B3 (the face
+    // normals of a closed surface sum to zero), so face 5 carries no adjoint:
+    // sum_n lf_n . B_n = sum_f N_f . LU_f. The face terms LU go to sLU for
+    // the position transpose; p and q get -1/8 sum_f N_f . LU_f here, before
+    // the material transpose of the cycle before reads them.
+    {
+      const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
+      // face normals 0..4 (the forward's cross products, from the tape)
+      V3 N[5];
+#pragma unroll
+      for (int f = 0; f < 5; ++f) N[f] = v3(a.geo[(48 + f) * E + e], a.geo[(54 + f) * E + e], a.geo[(60 + f) * E + e]);
+      auto lfv = [&](int n) { return v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]); };
+      // w_n = lf_n - lf_opposite(n) for the corners 0..3 (opposites 6, 7, 4, 5)
+      const V3 lf0 = lfv(0);
+      V3 w0 = lf0, w1 = lfv(1), w2 = lfv(2), w3 = lfv(3);
+      {
+        const V3 o0 = lfv(6), o1 = lfv(7), o2 = lfv(4), o3 = lfv(5);
+        w0.x -= o0.x; w0.y -= o0.y; w0.z -= o0.z;
+        w1.x -= o1.x; w1.y -= o1.y; w1.z -= o1.z;
+        w2.x -= o2.x; w2.y -= o2.y; w2.z -= o2.z;
+        w3.x -= o3.x; w3.y -= o3.y; w3.z -= o3.z;
+      }
+      // corners 0..3 touch faces {0,1,4} {0,1,2} {0,2,3} {0,3,4}
+      V3 w01 = w0; vadd(w01, w1);
+      V3 w23 = w2; vadd(w23, w3);
+      V3 LU[5];
+      LU[0] = w01; vadd(LU[0], w23);
+      LU[1] = w01;
+      LU[2] = w1; vadd(LU[2], w2);
+      LU[3] = w23;
+      LU[4] = w0; vadd(LU[4], w3);
+      if (!(MODE & 1)) {
+        // src/domain.jl:1050-1055: node 1 (corner 0) takes face 5's areaY twice
+        // and no areaZ; its opposite corner has the plain sum
+        LU[4].y += lf0.y;
+        LU[4].z -= lf0.z;
+      }
+      double Ls8 = 0.0;
+#pragma unroll
+      for (int f = 0; f < 5; ++f) {
+        Ls8 += vdot(N[f], LU[f]);
+        a.sLU[(f * 3) * E + e] = LU[f].x;
+        a.sLU[(f * 3 + 1) * E + e] = LU[f].y;
+        a.sLU[(f * 3 + 2) * E + e] = LU[f].z;
+      }
+      const double Lpq = -0.125 * Ls8;
+      a.lp[e] += Lpq;
+      a.lq[e] += Lpq;
+    }
   }
   block_sum_to(Lhg_coef, a.part_hg);
 }
 
-// Position transpose of k_force, written to the position corner buffer:
+// Position transpose of one element's k_force, added into LX:
 //  * the hourglass modes: Gamma^T of dL/dhm;
 //  * the volume derivatives: the forward's dv is the gradient of 12*volume
 //    (calcElemVolume's three triple products U.(V x W) of face diagonals), so
 //    the transpose of G -> sum <G, dv> is the Hessian-vector product of those
 //    triple products along G (the faithful slots 1 and 3 swapped back);
 //  * the stress force f_n = s8 B_n with B_n the node's face-diagonal cross
-//    products (the reference's face-5 quirk unless corrected).
-// All three use the 12 face diagonals of the element.
+//    products, through the face terms LU (see ka_hourglass).
+// All three use the 12 face diagonals of the element (force order d20 d31
+// d50 d14 d61 d25 d72 d36 d43 d07 d64 d57); the hourglass transpose of the
+// same cycle left dL/dhm, dL/ddv and LU in sLhm, sLdv and sLU.
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
+__device__ __forceinline__ void force_geo_t(const AdjDev& a, int e, const V3 dgs[12], double s8, double LX[3][8]) {
   const int E = a.E;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= E) return;
-  int nd[8];
-#pragma unroll
-  for (int c = 0; c < 8; ++c) nd[c] = a.nodelist[c * E + e];
-  // the 12 face diagonals of the cycle's start positions, from the tape
-  auto dg = [&](int q) { return v3(a.geo[(66 + 3 * q) * E + e], a.geo[(67 + 3 * q) * E + e], a.geo[(68 + 3 * q) * E + e]); };
-  const V3 d20 = dg(0), d31 = dg(1), d50 = dg(2), d14 = dg(3), d61 = dg(4), d25 = dg(5);
-  const V3 d72 = dg(6), d36 = dg(7), d43 = dg(8), d07 = dg(9), d64 = dg(10), d57 = dg(11);
-  double LX[3][8];
+  const V3 d20 = dgs[0], d31 = dgs[1], d50 = dgs[2], d14 = dgs[3], d61 = dgs[4], d25 = dgs[5];
+  const V3 d72 = dgs[6], d36 = dgs[7], d43 = dgs[8], d07 = dgs[9], d64 = dgs[10], d57 = dgs[11];
   // hourglass modes hm_k = Gamma(X_k)
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
@@ -859,51 +968,12 @@ __global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
       hvp(U, d61, d50, dU, gd(6, 1), gd(5, 0), 1, 4, 2, 5, 6, 1, 5, 0);
     }
   }
-  // stress part: f = s8 * B. The forward forms B0..B3 from faces 0-4 (node
-  // n's three face cross products) and the opposite corners as B6 = -B0,
-  // B7 = -B1, B4 = -B2, B5 = -B3 (the face normals of a closed surface sum to
-  // zero), so face 5 carries no adjoint.
+  // stress part: with N_f = d1 x d2 for (d1, d2) = (p0 - p1, p2 - p3) of the
+  // face's corners, sum_n lf_n . f_n = s8 sum_f N_f . LU_f
   {
-    const double* Lf[3] = {a.lfx, a.lfy, a.lfz};
-    const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
-    // face normals 0..4 (the forward's cross products, from the tape)
-    V3 N[5];
-#pragma unroll
-    for (int f = 0; f < 5; ++f) N[f] = v3(a.geo[(48 + f) * E + e], a.geo[(54 + f) * E + e], a.geo[(60 + f) * E + e]);
-    auto lfv = [&](int n) { return v3(Lf[0][nd[n]], Lf[1][nd[n]], Lf[2][nd[n]]); };
-    // w_n = lf_n - lf_opposite(n) for the corners 0..3 (opposites 6, 7, 4, 5)
-    const V3 lf0 = lfv(0);
-    V3 w0 = lf0, w1 = lfv(1), w2 = lfv(2), w3 = lfv(3);
-    {
-      const V3 o0 = lfv(6), o1 = lfv(7), o2 = lfv(4), o3 = lfv(5);
-      w0.x -= o0.x; w0.y -= o0.y; w0.z -= o0.z;
-      w1.x -= o1.x; w1.y -= o1.y; w1.z -= o1.z;
-      w2.x -= o2.x; w2.y -= o2.y; w2.z -= o2.z;
-      w3.x -= o3.x; w3.y -= o3.y; w3.z -= o3.z;
-    }
-    // sum_n lf_n . B_n = sum_f N_f . LU_f: corners 0..3 touch faces
-    // {0,1,4} {0,1,2} {0,2,3} {0,3,4}
-    V3 w01 = w0; vadd(w01, w1);
-    V3 w23 = w2; vadd(w23, w3);
     V3 LU[5];
-    LU[0] = w01; vadd(LU[0], w23);
-    LU[1] = w01;
-    LU[2] = w1; vadd(LU[2], w2);
-    LU[3] = w23;
-    LU[4] = w0; vadd(LU[4], w3);
-    if (!(MODE & 1)) {
-      // src/domain.jl:1050-1055: node 1 (corner 0) takes face 5's areaY twice
-      // and no areaZ; its opposite corner has the plain sum
-      LU[4].y += lf0.y;
-      LU[4].z -= lf0.z;
-    }
-    double Ls8 = 0.0;
 #pragma unroll
-    for (int f = 0; f < 5; ++f) Ls8 += vdot(N[f], LU[f]);
-    const double Lpq = -0.125 * Ls8;
-    a.lp[e] += Lpq;
-    a.lq[e] += Lpq;
-    // N_f = d1 x d2 with (d1, d2) = (p0 - p1, p2 - p3) of the face's corners
+    for (int f = 0; f < 5; ++f) LU[f] = v3(a.sLU[(f * 3) * E + e], a.sLU[(f * 3 + 1) * E + e], a.sLU[(f * 3 + 2) * E + e]);
     auto face_t = [&](int f, const V3& d1, const V3& d2, int p0, int p1, int p2, int p3) {
       const V3 LN = v3(s8 * LU[f].x, s8 * LU[f].y, s8 * LU[f].z);
       const V3 L1 = vcross(d2, LN), L2 = vcross(LN, d1);
@@ -915,6 +985,22 @@ __global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
     face_t(3, d72, d36, 7, 2, 3, 6);
     face_t(4, d43, d07, 4, 3, 0, 7);
   }
+}
+
+// The position transpose of the first cycle's k_force (the other cycles'
+// is part of ka_kinematics of the cycle before), from the force tape's
+// diagonals, into the force corner buffer that ka_gather_corners sums.
+template <int MODE>
+__global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
+  const int E = a.E;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  V3 dgs[12];
+#pragma unroll
+  for (int q = 0; q < 12; ++q) dgs[q] = v3(a.geo[(66 + 3 * q) * E + e], a.geo[(67 + 3 * q) * E + e], a.geo[(68 + 3 * q) * E + e]);
+  const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
+  double LX[3][8];
+  force_geo_t<MODE>(a, e, dgs, s8, LX);
 #pragma unroll
   for (int k = 0; k < 3; ++k)
 #pragma unroll

@@ -166,8 +166,9 @@ struct DevDomain {
   // [102][E]: the force kernel's volume derivatives dv_j[n] (24, node
   // order), hourglass modes over 12*determ (12), mode sums S_k[m] of the
   // velocities (12), face-diagonal cross products (x, y, z of the 6 faces:
-  // 18) and the 12 face diagonals d20 d31 d50 d14 d61 d25 d72 d36 d43 d07
-  // d64 d57 (36)
+  // 18; faces 0..4 written) and the 12 face diagonals d20 d31 d50 d14 d61
+  // d25 d72 d36 d43 d07 d64 d57 (36; written at the start of a taped
+  // segment only)
   double* tapeGeo;
   // [90][E]: the kinematics kernel's Walsh vectors of positions (9) and
   // velocities (9), cofactor columns (9), 1/det (1), monotonic-Q cross

@@ -193,20 +193,29 @@ __device__ __forceinline__ void store_geometry(double* geo, int E, int e, const 
   geo[50 * E + e] = det;
 }
 
-// The force tape's face diagonals (slots 66 + 3q + k) and face normals 0..4
-// (48 + f, 54 + f, 60 + f) of these positions, for the transpose.
-__device__ __forceinline__ void tape_force_geometry(double* tape, int E, int e, const double g[12][3],
-                                                    const double n[6][3]) {
-#pragma unroll
-  for (int q = 0; q < 12; ++q)
-#pragma unroll
-    for (int k = 0; k < 3; ++k) tape[(66 + 3 * q + k) * E + e] = g[q][k];
+// The force tape's face normals 0..4 of these positions (slots 48 + f,
+// 54 + f, 60 + f), read by the hourglass transpose.
+__device__ __forceinline__ void tape_force_normals(double* tape, int E, int e, const double n[6][3]) {
 #pragma unroll
   for (int f = 0; f < 5; ++f) {
     tape[(48 + f) * E + e] = n[f][0];
     tape[(54 + f) * E + e] = n[f][1];
     tape[(60 + f) * E + e] = n[f][2];
   }
+}
+
+// The force tape's face diagonals (slots 66 + 3q + k) and face normals of
+// these positions: at the start of a taped segment, where the position
+// transpose of a segment's first cycle reads them (the other cycles' is
+// fused into the kinematics transpose of the cycle before, which reads the
+// kinematics tape).
+__device__ __forceinline__ void tape_force_geometry(double* tape, int E, int e, const double g[12][3],
+                                                    const double n[6][3]) {
+#pragma unroll
+  for (int q = 0; q < 12; ++q)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) tape[(66 + 3 * q + k) * E + e] = g[q][k];
+  tape_force_normals(tape, E, e, n);
 }
 
 // The stored geometry of the current positions (see above): at the start of
@@ -499,7 +508,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
     if (TAPE) {
       d.tapeFlags[e] = (unsigned long long)fidx << TF_FACE_SHIFT;
       d.tapeKin[41 * E + e] = fcx; d.tapeKin[42 * E + e] = fcy; d.tapeKin[43 * E + e] = fcz;
-      if (d.tapeGeoNext) tape_force_geometry(d.tapeGeoNext, E, e, g, n);
+      // the next cycle's face normals, for its hourglass transpose
+      if (d.tapeGeoNext) tape_force_normals(d.tapeGeoNext, E, e, n);
     }
     {
       double B[3][4], pz01, ny4, gr[3][8];
