@@ -72,7 +72,7 @@ def close(a, b, scale, tol):
     return abs(a - b) <= tol * max(scale, 1e-300)
 
 
-@pytest.mark.parametrize("mode", [0, 7])
+@pytest.mark.parametrize("mode", [0, 1, 2, 7])
 def test_one_cycle_block_dot_products(gpu_lib, oracle_mod, mode):
     L = gpu_lib
     nx = 6
@@ -118,11 +118,16 @@ def test_one_cycle_block_dot_products(gpu_lib, oracle_mod, mode):
     assert not bad, bad
 
 
-@pytest.mark.parametrize("mode", [0, 7])
-def test_run_gradient_matches_dual_oracle(gpu_lib, oracle_mod, mode):
+@pytest.mark.parametrize("mode,hgcoef", [(0, None), (1, None), (2, None), (7, None), (0, 0.0)])
+def test_run_gradient_matches_dual_oracle(gpu_lib, oracle_mod, mode, hgcoef):
+    """Modes 1 and 2 take the face-5 and volume-derivative corrections one
+    at a time (each changes the force transpose on its own); hgcoef 0 runs
+    without hourglass forces."""
     L = gpu_lib
     nx, cycles, radius = 8, 30, 0.3
     g = developed(L, nx, mode, 0, 0xB1)
+    if hgcoef is not None:
+        g.hgcoef = hgcoef
     snap = snapshot(g)
     rng = np.random.default_rng(0xB2)
     de = rng.standard_normal(g.numElem) * snap[0]["e"]
