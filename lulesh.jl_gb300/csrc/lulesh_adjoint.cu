@@ -439,7 +439,8 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
       (rc = dalloc(a, &ad.lnb, 6 * (size_t)E)) || (rc = dalloc(a, &ad.cX, 24 * (size_t)E)) ||
       (rc = dalloc(a, &ad.cV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.fX, 24 * (size_t)E)) ||
       (rc = dalloc(a, &ad.fV, 24 * (size_t)E)) || (rc = dalloc(a, &ad.sLdv, 24 * (size_t)E)) ||
-      (rc = dalloc(a, &ad.sLU, 15 * (size_t)E)) || (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) || (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
+      (rc = dalloc(a, &ad.sLU, 15 * (size_t)E)) || (rc = dalloc(a, &ad.sLhm, 12 * (size_t)E)) ||
+      (rc = dalloc(a, &ad.part_dt, std::max(ge, gn))) ||
       (rc = dalloc(a, &ad.part_dtn, gn)) || (rc = dalloc(a, &ad.part_hg, ge)) || (rc = dalloc(a, &a->scal, 4)) ||
       (rc = dalloc(a, &a->dsc, 1)) || (rc = dalloc(a, &a->we, E)) || (rc = dalloc(a, &a->wn, N)) ||
       (rc = dalloc(a, &a->fx_s, N)) || (rc = dalloc(a, &a->fy_s, N)) || (rc = dalloc(a, &a->fz_s, N)))
