@@ -764,7 +764,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     ACK(cudaEventRecord(a->ev_start, s));
     ACK(cudaStreamWaitEvent(rs, a->ev_start, 0));
     ACK(cudaStreamWaitEvent(tst, a->ev_start, 0));
-    if (recomputed(nseg - 1) && (rc = enqueue_R(nseg - 1))) return rc;
+    if (nseg > 0 && recomputed(nseg - 1) && (rc = enqueue_R(nseg - 1))) return rc;
   }
   for (int k = nseg - 1; k >= 0; --k) {
     const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
@@ -784,10 +784,13 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     ACK(cudaStreamWaitEvent(s, a->ev_done, 0));
   }
   // the first cycle's force transpose: its positions (segment 0's first
-  // tape, set 0), then both force corner buffers onto the node adjoints
-  set_cycle_pointers(a, a->sets[0].slots[0], a->sets[0].slots[1], a->sets[0].tape[0]);
-  first_cycle_force_geo(a, s);
-  ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
+  // tape, set 0), then both force corner buffers onto the node adjoints; a
+  // run that took no cycle has no tape and nothing to add
+  if (nseg > 0) {
+    set_cycle_pointers(a, a->sets[0].slots[0], a->sets[0].slots[1], a->sets[0].tape[0]);
+    first_cycle_force_geo(a, s);
+    ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
+  }
   copy_state_to_domain(a, a->final_state, s);
   AdjScal hsc;
   ACK(cudaMemcpyAsync(&hsc, a->dsc, sizeof(AdjScal), cudaMemcpyDeviceToHost, s));

@@ -295,3 +295,34 @@ def test_c5_gradient_matches_dual_oracle_full_size(gpu_lib, oracle_mod):
     assert loss == pytest.approx(ref_loss, rel=1e-9)
     vjp = float(np.dot(ge, de)) + ghg * dhg
     assert close(jvp, vjp, jscale, 1e-8), (jvp, vjp, jscale)
+
+
+def test_gradient_of_a_run_already_at_stoptime(gpu_lib):
+    """A run already at stoptime takes no cycle: its gradient is the
+    objective's own (finite, zero for positions and hgcoef, the energy
+    weights for e), the same for a plan of two overlapped segments and of
+    one segment."""
+    L = gpu_lib
+    nx = 8
+    g = developed(L, nx, 0, 5, 0xD1)
+    g.stoptime = g.time
+    snap = snapshot(g)
+    out = []
+    for every in (20, 40):
+        restore(g, snap)
+        adj = L.Adjoint(g, radius=0.3, checkpoint_every=every)
+        loss = adj.gradient(40)
+        assert adj.result.cycles == 0
+        assert loss == adj.loss()
+        grads = {f: adj.grad(f) for f in STATE}
+        for f in STATE:
+            assert np.all(np.isfinite(grads[f])), f
+        for f in ("x", "y", "z", "p", "q", "v", "ss"):
+            assert not np.any(grads[f]), f
+        assert adj.result.grad_hgcoef == 0.0
+        assert np.all(grads["e"] >= 0) and np.any(grads["e"])
+        out.append((loss, grads))
+        adj.close()
+    assert out[0][0] == out[1][0]
+    for f in STATE:
+        assert np.array_equal(out[0][1][f], out[1][1][f]), f
