@@ -124,6 +124,25 @@ def test_run_parity(gpu_lib, oracle_mod, name):
     assert abs(total - ototal) <= 1e-8 * scale * c["nx"] ** 2
 
 
+def test_reference_default_run_matches_oracle(gpu_lib, oracle_mod):
+    """examples/benchmark.jl with its defaults (src/utils.jl:13-20: N = 45,
+    num_iters = 10; examples/benchmark.jl:23-26: one region, balance and
+    cost 1), through the per-step calls in the loop of
+    examples/benchmark.jl:82-98."""
+    L = gpu_lib
+    g, o = pair(L, oracle_mod, 45, nr=1)
+    while g.time < g.stoptime:
+        L.timeIncrement(g)
+        L.lagrangeLeapFrog(g)
+        if g.cycle >= 10:
+            break
+    assert o.run(10) == 0
+    assert g.cycle == o.get("cycle") == 10
+    assert_scalars(g, o)
+    assert g.field("e")[0] == pytest.approx(o.field("e")[0], rel=1e-9)
+    assert_fields(g, o, STATE_F64 + ["arealg", "vdov", "delv"])
+
+
 def test_run_equals_stepwise_and_is_deterministic(gpu_lib, oracle_mod):
     a = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10))
     b = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10))
