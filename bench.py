@@ -304,23 +304,32 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
         times.append(time.perf_counter() - t0)
     adj_s = min(times)
     res = adj.result
+    sweep = int(res.sweep)
     ge, ghg = adj.grad("e"), res.grad_hgcoef
     hg0 = snap[1]["hgcoef"]
-    # the same gradient with each segment's recompute and transpose in turn
-    # (one tape) instead of overlapped (two tapes)
-    adj.set_overlap(False)
-    restore()
-    adj.gradient(cycles)  # warm-up (graphs)
-    seq = []
-    for _ in range(2):
+
+    # the same gradient with the other reverse-sweep plans: each segment's
+    # recompute and transpose in turn (mode 0), and overlapped on one tape
+    # (mode 2, what runs where a second tape does not fit)
+    def other_plan(mode):
+        adj.set_overlap(mode)
         restore()
-        torch.cuda.synchronize(dev)
-        t0 = time.perf_counter()
-        adj.gradient(cycles)
-        torch.cuda.synchronize(dev)
-        seq.append(time.perf_counter() - t0)
-    seq_same = bool(np.array_equal(adj.grad("e"), ge)) and adj.result.grad_hgcoef == ghg
-    adj.set_overlap(True)
+        adj.gradient(cycles)  # warm-up (graphs)
+        ts = []
+        for _ in range(2):
+            restore()
+            torch.cuda.synchronize(dev)
+            t0 = time.perf_counter()
+            adj.gradient(cycles)
+            torch.cuda.synchronize(dev)
+            ts.append(time.perf_counter() - t0)
+        same = bool(np.array_equal(adj.grad("e"), ge)) and adj.result.grad_hgcoef == ghg
+        return {"adjoint_s": min(ts), "adjoint_over_forward": min(ts) / fwd_s, "sweep": int(adj.result.sweep),
+                "gradient_bitwise_equal": same}
+
+    seq = other_plan(0)
+    one_tape = other_plan(2)
+    adj.set_overlap(1)
 
     def loss_at(e, hg):
         restore(e, hg)
@@ -366,9 +375,10 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
             "nx": nx, "cycles": int(res.cycles), "checkpoints": int(res.checkpoints),
             "forward_s": fwd_s, "adjoint_s": adj_s, "adjoint_over_forward": adj_s / fwd_s,
             "adjoint_sweep_ms": {"checkpointed_forward": res.forward_ms, "reverse": res.reverse_ms},
-            "reverse_sweep": "recompute of each segment overlapped with the transpose of the next (two tapes)",
-            "sequential": {"adjoint_s": min(seq), "adjoint_over_forward": min(seq) / fwd_s,
-                           "gradient_bitwise_equal": seq_same},
+            "reverse_sweep": {0: "each segment recomputed, then transposed",
+                              1: "recompute of each segment overlapped with the transpose of the next (two tapes)",
+                              2: "recompute of each segment overlapped with the transpose of the next (one tape)"}[sweep],
+            "sequential": seq, "one_tape": one_tape,
             "loss": loss, "grad_hgcoef": ghg, "grad_e_origin": float(ge[0]),
             "fd": {"directions": dirs, "step": h, "max_rel_err": max(errs),
                    "median_rel_err": float(np.median(errs))},

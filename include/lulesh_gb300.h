@@ -317,7 +317,7 @@ int lulesh_calc_force_for_nodes_static(const lulesh_force_args* args, void* stre
  * (about 8*(241*E + 9*N) bytes per taped cycle); a second tape of the same
  * size, allocated at the first gradient that has two or more segments if it
  * fits, lets the recompute of one segment overlap the transpose of the next
- * (lulesh_adj_set_overlap). The derivative is that of the branches the
+ * freely; without it they overlap on one tape (lulesh_adj_set_overlap). The derivative is that of the branches the
  * forward run took (dt minima, clamps, limiter cases). */
 typedef struct lulesh_adjoint lulesh_adjoint;
 
@@ -329,6 +329,8 @@ typedef struct {
   int64_t cycles;
   int32_t checkpoints;
   int32_t status;
+  int32_t sweep;        /* reverse sweep taken: 0 sequential, 1 overlapped on two tapes, 2 on one */
+  int32_t reserved;
 } lulesh_adj_result;
 
 int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_every, lulesh_adjoint** out);
@@ -345,11 +347,15 @@ int lulesh_adj_loss(lulesh_adjoint* adj, double* loss);
  * w.r.t. the initial state and hgcoef. result->cycles is the number run. */
 int lulesh_adj_gradient(lulesh_adjoint* adj, int64_t num_cycles, lulesh_adj_result* result);
 int lulesh_adj_get_gradient(lulesh_adjoint* adj, int32_t field, double* host, int64_t count);
-/* enable = 0: one tape, each segment recomputed and then transposed on the
- * domain's stream (frees the second tape). enable = 1 (the default): the
- * second tape is allocated now; LULESH_ERR_MEMORY (and the sequential sweep)
- * if it does not fit. Gradients are bitwise the same either way. */
-int lulesh_adj_set_overlap(lulesh_adjoint* adj, int32_t enable);
+/* mode = 0: one tape, each segment recomputed and then transposed on the
+ * domain's stream. mode = 1 (the default): each segment's recompute overlaps
+ * the transpose of the next, on two tapes where the second fits (allocated
+ * by the first gradient with two or more segments), else on one tape (the
+ * recompute fills each tape slot once the transpose has released it).
+ * mode = 2: overlapped on one tape. Modes 0 and 2 free the second tape. The
+ * plan a gradient took is in lulesh_adj_result.sweep; gradients are bitwise
+ * the same for every mode. */
+int lulesh_adj_set_overlap(lulesh_adjoint* adj, int32_t mode);
 
 /* Human-readable text of a status code. */
 const char* lulesh_status_string(int32_t status);

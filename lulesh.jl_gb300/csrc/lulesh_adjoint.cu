@@ -93,13 +93,16 @@ struct lulesh_adjoint {
   int K = 20;
   int E = 0, N = 0;
   std::vector<void*> allocs;
-  TapeSet sets[2];               // set 1 only for the overlapped reverse sweep
+  TapeSet sets[2];               // set 1 only for the overlapped sweep with two tapes
   std::vector<void*> set1_allocs;
-  bool overlap = true;           // overlap recompute and transpose when set 1 fits
+  // reverse sweep: 0 sequential, 1 overlapped (two tapes where they fit, else
+  // one), 2 overlapped on one tape
+  int overlap = 1;
   cudaStream_t rstream = nullptr;  // recompute stream of the overlapped sweep
   cudaStream_t tstream = nullptr;  // transpose stream of the overlapped sweep (high priority)
   cudaEvent_t ev_start = nullptr, ev_done = nullptr;
   cudaEvent_t ev_ready[2] = {nullptr, nullptr}, ev_free[2] = {nullptr, nullptr};
+  std::vector<cudaEvent_t> ev_slot;  // one tape: tape slot j released by the transpose
   std::vector<StateBuf> ckpts;   // segment start states
   std::vector<int> seg_len;      // cycles of each segment
   DevState* ckpt_st = nullptr;   // device: step state at each checkpoint
@@ -180,14 +183,12 @@ static void free_set1(lulesh_adjoint* a) {
   a->sets[1] = TapeSet{};
 }
 
-// Set 1, the streams and the events of the overlapped reverse sweep; false
-// (sequential sweep) when they do not fit. The transposes are the sweep's
-// critical path, so their stream takes the device's highest priority: the
-// block scheduler gives them the SMs first and the recompute fills what they
-// leave idle (partial waves, latency-bound phases).
-static bool ensure_overlap(lulesh_adjoint* a) {
-  if (!a->overlap) return false;
-  if (a->sets[1].ready) return true;
+// The streams and events of an overlapped reverse sweep; false (sequential
+// sweep) when they cannot be made. The transposes are the sweep's critical
+// path, so their stream takes the device's highest priority: the block
+// scheduler gives them the SMs first and the recompute fills what they leave
+// idle (partial waves, latency-bound phases).
+static bool ensure_streams(lulesh_adjoint* a) {
   if (!a->rstream && cudaStreamCreateWithFlags(&a->rstream, cudaStreamNonBlocking) != cudaSuccess) {
     cudaGetLastError();
     a->rstream = nullptr;
@@ -209,9 +210,28 @@ static bool ensure_overlap(lulesh_adjoint* a) {
       *e = nullptr;
       return false;
     }
+  return true;
+}
+
+// The second tape set; false when it does not fit.
+static bool ensure_set1(lulesh_adjoint* a) {
+  if (a->sets[1].ready) return true;
   if (alloc_set(a, a->set1_allocs, a->sets[1]) != LULESH_OK) {
     free_set1(a);
     return false;
+  }
+  return true;
+}
+
+// One event per tape slot, for the overlapped sweep on one tape.
+static bool ensure_slot_events(lulesh_adjoint* a) {
+  while ((int)a->ev_slot.size() < a->K) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      return false;
+    }
+    a->ev_slot.push_back(e);
   }
   return true;
 }
@@ -544,6 +564,7 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   free_set1(a);
   for (cudaEvent_t e : {a->ev_start, a->ev_done, a->ev_ready[0], a->ev_ready[1], a->ev_free[0], a->ev_free[1]})
     if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : a->ev_slot) cudaEventDestroy(e);
   if (a->rstream) cudaStreamDestroy(a->rstream);
   if (a->tstream) cudaStreamDestroy(a->tstream);
   for (void* p : a->allocs) cudaFree(p);
@@ -551,21 +572,15 @@ int lulesh_adj_destroy(lulesh_adjoint* a) {
   return LULESH_OK;
 }
 
-int lulesh_adj_set_overlap(lulesh_adjoint* a, int32_t enable) {
-  if (!a) return LULESH_ERR_ARGUMENT;
+int lulesh_adj_set_overlap(lulesh_adjoint* a, int32_t mode) {
+  if (!a || mode < 0 || mode > 2) return LULESH_ERR_ARGUMENT;
   ACK(cudaSetDevice(a->dom->params.device));
   ACK(cudaStreamSynchronize(a->dom->stream));
   if (a->rstream) ACK(cudaStreamSynchronize(a->rstream));
   if (a->tstream) ACK(cudaStreamSynchronize(a->tstream));
-  a->overlap = enable != 0;
-  if (!a->overlap) {
-    free_set1(a);
-    return LULESH_OK;
-  }
-  if (!ensure_overlap(a)) {
-    a->overlap = false;
-    return LULESH_ERR_MEMORY;
-  }
+  a->overlap = mode;
+  // the second tape is allocated by the next gradient that can use it
+  if (mode != 1) free_set1(a);
   return LULESH_OK;
 }
 
@@ -625,11 +640,26 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   }
   const Params prm = make_params(d);
   const bool aux = d->params.keep_aux != 0;
-  // segment k's tape set: k & 1 when recompute and transpose overlap
-  const bool pipe = nplan > 1 && ensure_overlap(a);
-  auto set_of = [&](int k) -> TapeSet& { return a->sets[pipe ? (k & 1) : 0]; };
+  // The reverse sweep's plan: sequential (one tape, one stream), overlapped
+  // with two tapes (segment k uses set k & 1), or overlapped on one tape
+  // (consecutive segments store their cycles in opposite slot orders, so the
+  // recompute of segment k-1 fills each slot as soon as the transpose of
+  // segment k, which empties them in the same order, has released it).
+  enum Plan { kSeq = 0, kTwo = 1, kOne = 2 };
+  Plan plan = kSeq;
+  if (nplan > 1 && a->overlap != 0 && ensure_streams(a)) {
+    if (a->overlap == 1 && ensure_set1(a)) plan = kTwo;
+    else if (ensure_slot_events(a)) plan = kOne;
+  }
+  const bool pipe = plan != kSeq, one = plan == kOne;
+  auto set_of = [&](int k) -> TapeSet& { return a->sets[plan == kTwo ? (k & 1) : 0]; };
+  // on one tape, segment k's cycle j goes to tape slot K-1-j and its start
+  // state to state slot K-j when an odd number of segments follow it
+  auto rev_of = [&](int k) { return one && ((nplan - 1 - k) & 1) != 0; };
+  auto tslot = [&](bool rev, int j) { return rev ? K - 1 - j : j; };
+  auto sslot = [&](bool rev, int j) { return rev ? K - j : j; };
   // segments k >= first_taped are taped by the forward sweep itself
-  const int first_taped = nplan - (pipe ? std::min(2, nplan) : 1);
+  const int first_taped = nplan - (plan == kTwo ? std::min(2, nplan) : 1);
   if (nplan > 1 && (!a->fwd_graph || std::memcmp(&a->fwd_prm, &prm, sizeof(Params)) != 0 ||
                     std::memcmp(&a->fwd_tuning, &d->tuning, sizeof(Tuning)) != 0 || a->fwd_aux != aux)) {
     if (a->fwd_graph) cudaGraphExecDestroy(a->fwd_graph);
@@ -666,10 +696,13 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
       ACK(cudaGraphLaunch(a->fwd_graph, s));
     } else {
       TapeSet& ts = set_of(k);
+      const bool rev = rev_of(k);
       const int n = k < nplan - 1 ? K : last_len;
-      tape_segment_begin(a, ts.tape[0], s);
-      for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < n ? &ts.tape[j + 1] : nullptr, ts.rec + j, s);
-      copy_state_from_domain(a, ts.slots[n], s);
+      tape_segment_begin(a, ts.tape[tslot(rev, 0)], s);
+      for (int j = 0; j < n; ++j)
+        tape_cycle(a, ts.slots[sslot(rev, j)], ts.tape[tslot(rev, j)], j + 1 < n ? &ts.tape[tslot(rev, j + 1)] : nullptr,
+                   ts.rec + tslot(rev, j), s);
+      copy_state_from_domain(a, ts.slots[sslot(rev, n)], s);
     }
   }
   ACK(cudaGetLastError());
@@ -704,26 +737,41 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   // Recompute R(k) (checkpoint k restored into the domain, its cycles taped
   // into set_of(k)) and transpose T(k) (the adjoint state through those
   // cycles, in reverse), in order k = nseg-1..0; segments the forward sweep
-  // taped skip R. Overlapped, T runs on the high-priority transpose stream
-  // and R on its own stream one segment ahead: R(k-1) is queued before T(k),
-  // waits until T(k+1) has released its set, and T(k) waits for R(k); the
-  // domain's stream joins both at the end. Sequential, R(k) runs right before
-  // T(k) on the domain's stream. Full segments run as captured graphs (one
-  // per set and phase, rebuilt when the parameters they bake in change).
+  // taped skip R. Sequential, R(k) runs right before T(k) on the domain's
+  // stream. Overlapped, T runs on the high-priority transpose stream and R on
+  // its own stream one segment ahead, and T(k) waits for R(k):
+  //  * two tapes: R(k-1) is queued before T(k) and waits until T(k+1) has
+  //    released its set;
+  //  * one tape: R(k-1) is queued after T(k), whose cycles each release their
+  //    tape slot (an event per slot); R(k-1) writes a slot (its tape, its
+  //    start state, and the next cycle's face normals) only after that
+  //    slot's event, and its end state after all of T(k).
+  // The domain's stream joins both at the end. Full segments of the first
+  // two plans run as captured graphs (one per set and phase, rebuilt when the
+  // parameters they bake in change).
   cudaStream_t rs = pipe ? a->rstream : s;
   cudaStream_t tst = pipe ? a->tstream : s;
-  auto queue_recompute = [&](TapeSet& ts, int n, cudaStream_t st) {
-    tape_segment_begin(a, ts.tape[0], st);
-    for (int j = 0; j < n; ++j) tape_cycle(a, ts.slots[j], ts.tape[j], j + 1 < n ? &ts.tape[j + 1] : nullptr, ts.rec + j, st);
-    copy_state_from_domain(a, ts.slots[n], st);
-  };
-  auto queue_transpose = [&](TapeSet& ts, int n, cudaStream_t st) {
-    for (int j = n - 1; j >= 0; --j) {
-      set_cycle_pointers(a, ts.slots[j], ts.slots[j + 1], ts.tape[j]);
-      reverse_cycle(a, ts.rec + j, st);
+  auto queue_recompute = [&](TapeSet& ts, int n, bool rev, cudaStream_t st) -> int {
+    if (one) ACK(cudaStreamWaitEvent(st, a->ev_slot[tslot(rev, 0)], 0));
+    tape_segment_begin(a, ts.tape[tslot(rev, 0)], st);
+    for (int j = 0; j < n; ++j) {
+      if (one && j + 1 < n) ACK(cudaStreamWaitEvent(st, a->ev_slot[tslot(rev, j + 1)], 0));
+      tape_cycle(a, ts.slots[sslot(rev, j)], ts.tape[tslot(rev, j)], j + 1 < n ? &ts.tape[tslot(rev, j + 1)] : nullptr,
+                 ts.rec + tslot(rev, j), st);
     }
+    if (one) ACK(cudaStreamWaitEvent(st, a->ev_free[0], 0));
+    copy_state_from_domain(a, ts.slots[sslot(rev, n)], st);
+    return LULESH_OK;
   };
-  const int nsets = pipe ? 2 : 1;
+  auto queue_transpose = [&](TapeSet& ts, int n, bool rev, cudaStream_t st) -> int {
+    for (int j = n - 1; j >= 0; --j) {
+      set_cycle_pointers(a, ts.slots[sslot(rev, j)], ts.slots[sslot(rev, j + 1)], ts.tape[tslot(rev, j)]);
+      reverse_cycle(a, ts.rec + tslot(rev, j), st);
+      if (one) ACK(cudaEventRecord(a->ev_slot[tslot(rev, j)], st));
+    }
+    return LULESH_OK;
+  };
+  const int nsets = plan == kTwo ? 2 : 1;
   if (std::memcmp(&a->rev_prm, &prm, sizeof(Params)) != 0 || std::memcmp(&a->rev_tuning, &d->tuning, sizeof(Tuning)) != 0) {
     for (int x = 0; x < 2; ++x) {
       if (a->rec_graph[x]) { cudaGraphExecDestroy(a->rec_graph[x]); a->rec_graph[x] = nullptr; }
@@ -735,28 +783,40 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   auto capture = [&](cudaGraphExec_t* out, cudaStream_t st, auto&& body) -> int {
     cudaGraph_t g;
     ACK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    body();
-    ACK(cudaStreamEndCapture(st, &g));
+    const int brc = body();
+    const cudaError_t ce = cudaStreamEndCapture(st, &g);
+    if (brc) { if (ce == cudaSuccess) cudaGraphDestroy(g); return brc; }
+    ACK(ce);
     const cudaError_t ge = cudaGraphInstantiate(out, g, 0);
     cudaGraphDestroy(g);
     ACK(ge);
     return LULESH_OK;
   };
-  const bool any_full = std::count(a->seg_len.begin(), a->seg_len.end(), K) > 0;
+  const bool any_full = !one && std::count(a->seg_len.begin(), a->seg_len.end(), K) > 0;
   for (int x = 0; x < nsets && any_full; ++x) {
     TapeSet& ts = a->sets[x];
-    if (!a->rec_graph[x] && (rc = capture(&a->rec_graph[x], rs, [&] { queue_recompute(ts, K, rs); }))) return rc;
-    if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], tst, [&] { queue_transpose(ts, K, tst); }))) return rc;
+    if (!a->rec_graph[x] && (rc = capture(&a->rec_graph[x], rs, [&] { return queue_recompute(ts, K, false, rs); })))
+      return rc;
+    if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], tst, [&] { return queue_transpose(ts, K, false, tst); })))
+      return rc;
   }
   auto recomputed = [&](int k) { return k < first_taped; };
   auto enqueue_R = [&](int k) -> int {
-    const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
-    if (pipe && k + 2 <= nseg - 1) ACK(cudaStreamWaitEvent(rs, a->ev_free[x], 0));
+    const int x = plan == kTwo ? (k & 1) : 0, n = a->seg_len[k];
+    if (plan == kTwo && k + 2 <= nseg - 1) ACK(cudaStreamWaitEvent(rs, a->ev_free[x], 0));
     copy_state_to_domain(a, a->ckpts[k], rs);
     ACK(cudaMemcpyAsync(d->dd.st, a->ckpt_st + k, sizeof(DevState), cudaMemcpyDeviceToDevice, rs));
-    if (n == K) ACK(cudaGraphLaunch(a->rec_graph[x], rs));
-    else queue_recompute(a->sets[x], n, rs);
+    if (!one && n == K) ACK(cudaGraphLaunch(a->rec_graph[x], rs));
+    else if (const int r = queue_recompute(a->sets[x], n, rev_of(k), rs)) return r;
     if (pipe) ACK(cudaEventRecord(a->ev_ready[x], rs));
+    return LULESH_OK;
+  };
+  auto enqueue_T = [&](int k) -> int {
+    const int x = plan == kTwo ? (k & 1) : 0, n = a->seg_len[k];
+    if (pipe && recomputed(k)) ACK(cudaStreamWaitEvent(tst, a->ev_ready[x], 0));
+    if (!one && n == K) ACK(cudaGraphLaunch(a->tr_graph[x], tst));
+    else if (const int r = queue_transpose(a->sets[x], n, rev_of(k), tst)) return r;
+    if (pipe) ACK(cudaEventRecord(a->ev_free[x], tst));
     return LULESH_OK;
   };
   if (pipe) {
@@ -767,16 +827,16 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     if (nseg > 0 && recomputed(nseg - 1) && (rc = enqueue_R(nseg - 1))) return rc;
   }
   for (int k = nseg - 1; k >= 0; --k) {
-    const int x = pipe ? (k & 1) : 0, n = a->seg_len[k];
-    if (pipe) {
+    if (plan == kSeq) {
+      if (recomputed(k) && (rc = enqueue_R(k))) return rc;
+      if ((rc = enqueue_T(k))) return rc;
+    } else if (plan == kTwo) {
       if (k >= 1 && recomputed(k - 1) && (rc = enqueue_R(k - 1))) return rc;
-      if (recomputed(k)) ACK(cudaStreamWaitEvent(tst, a->ev_ready[x], 0));
-    } else if (recomputed(k) && (rc = enqueue_R(k))) {
-      return rc;
+      if ((rc = enqueue_T(k))) return rc;
+    } else {
+      if ((rc = enqueue_T(k))) return rc;
+      if (k >= 1 && recomputed(k - 1) && (rc = enqueue_R(k - 1))) return rc;
     }
-    if (n == K) ACK(cudaGraphLaunch(a->tr_graph[x], tst));
-    else queue_transpose(a->sets[x], n, tst);
-    if (pipe) ACK(cudaEventRecord(a->ev_free[x], tst));
     ACK(cudaGetLastError());
   }
   if (pipe) {
@@ -784,10 +844,12 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     ACK(cudaStreamWaitEvent(s, a->ev_done, 0));
   }
   // the first cycle's force transpose: its positions (segment 0's first
-  // tape, set 0), then both force corner buffers onto the node adjoints; a
-  // run that took no cycle has no tape and nothing to add
+  // tape), then both force corner buffers onto the node adjoints; a run that
+  // took no cycle has no tape and nothing to add
   if (nseg > 0) {
-    set_cycle_pointers(a, a->sets[0].slots[0], a->sets[0].slots[1], a->sets[0].tape[0]);
+    TapeSet& t0 = set_of(0);
+    const bool r0 = rev_of(0);
+    set_cycle_pointers(a, t0.slots[sslot(r0, 0)], t0.slots[sslot(r0, 1)], t0.tape[tslot(r0, 0)]);
     first_cycle_force_geo(a, s);
     ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
   }
@@ -800,6 +862,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   ACK(cudaMemcpy(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice));
   auto t2 = std::chrono::steady_clock::now();
   out.grad_hgcoef = hsc.Lhg;
+  out.sweep = plan;
   out.forward_ms = std::chrono::duration<double, std::milli>(t1 - t0).count();
   out.reverse_ms = std::chrono::duration<double, std::milli>(t2 - t1).count();
   out.status = LULESH_OK;

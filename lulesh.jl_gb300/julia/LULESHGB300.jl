@@ -200,6 +200,8 @@ struct AdjResult
     cycles::Int64
     checkpoints::Int32
     status::Int32
+    sweep::Int32      # 0 sequential, 1 overlapped on two tapes, 2 on one
+    reserved::Int32
 end
 
 mutable struct GPUAdjoint
@@ -227,13 +229,18 @@ end
 clear_seeds!(a::GPUAdjoint) = (ccall((:lulesh_adj_clear_seeds, libpath), Cint, (Ptr{Cvoid},), a.handle); a)
 
 """
-    set_overlap!(a, enable::Bool)
+    set_overlap!(a, mode)
 
-Overlap each checkpoint segment's recompute with the transpose of the
-segment after it (two tapes, the default), or run them in turn on one tape.
+How the reverse sweep runs: `false`/0 each checkpoint segment's recompute
+and then its transpose; `true`/1 (the default) the recompute of one segment
+overlapped with the transpose of the segment after it, on two tapes where
+the second fits, else on one; 2 overlapped on one tape. The `sweep` field of
+the result tells which plan a gradient took.
 """
-function set_overlap!(a::GPUAdjoint, enable::Bool)
-    rc = ccall((:lulesh_adj_set_overlap, libpath), Cint, (Ptr{Cvoid}, Int32), a.handle, Int32(enable))
+function set_overlap!(a::GPUAdjoint, mode::Union{Bool,Integer})
+    m = Int32(mode)
+    0 <= m <= 2 || throw(ArgumentError("overlap mode is 0, 1 or 2"))
+    rc = ccall((:lulesh_adj_set_overlap, libpath), Cint, (Ptr{Cvoid}, Int32), a.handle, m)
     rc == 0 || throw(LuleshGPUError("overlap: status $rc", rc))
     return a
 end

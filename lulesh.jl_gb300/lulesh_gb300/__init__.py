@@ -112,7 +112,8 @@ class AdjResult(ctypes.Structure):
     """lulesh_adj_result."""
     _fields_ = [("loss", ctypes.c_double), ("grad_hgcoef", ctypes.c_double),
                 ("forward_ms", ctypes.c_double), ("reverse_ms", ctypes.c_double),
-                ("cycles", ctypes.c_int64), ("checkpoints", ctypes.c_int32), ("status", ctypes.c_int32)]
+                ("cycles", ctypes.c_int64), ("checkpoints", ctypes.c_int32), ("status", ctypes.c_int32),
+                ("sweep", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
 _LIB = None
@@ -578,11 +579,16 @@ class Adjoint:
     def clear_seeds(self):
         _check(self._L.lulesh_adj_clear_seeds(self._h), "clear seeds")
 
-    def set_overlap(self, enable):
-        """Overlap each segment's recompute with the next segment's transpose
-        (two tapes; the default) or run them in turn on one tape. Raises if
-        the second tape does not fit."""
-        _check(self._L.lulesh_adj_set_overlap(self._h, 1 if enable else 0), "overlap")
+    def set_overlap(self, mode):
+        """How the reverse sweep runs: False/0 each segment's recompute and
+        then its transpose; True/1 (the default) the recompute of one segment
+        overlapped with the transpose of the next, on two tapes where the
+        second fits, else on one; 2 overlapped on one tape. result.sweep
+        tells which a gradient took (0, 1 two tapes, 2 one tape)."""
+        m = int(mode)
+        if m not in (0, 1, 2):
+            raise ValueError("overlap mode is 0, 1 or 2")
+        _check(self._L.lulesh_adj_set_overlap(self._h, m), "overlap")
 
     def loss(self):
         x = ctypes.c_double()

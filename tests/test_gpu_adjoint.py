@@ -184,15 +184,17 @@ def test_checkpoint_interval_and_final_state(gpu_lib):
             assert np.array_equal(other[2][f], grads[0][2][f]), f
 
 
-@pytest.mark.parametrize("every,stop_early", [(7, False), (7, True), (14, False)])
-def test_overlapped_and_sequential_sweeps_agree(gpu_lib, every, stop_early):
-    """The reverse sweep that recomputes one segment while it transposes the
-    next (two tapes, the forward sweep taping the last two segments) gives
-    bitwise the gradients of the sequential sweep (one tape, the last segment
-    taped): 27 cycles in segments of 7 (a partial last one); a run that
-    reaches stoptime after about 17 cycles, inside the third segment (taped
-    by the overlapped forward sweep, recomputed by the sequential one); and
-    segments of 14, both taped by the overlapped forward sweep."""
+@pytest.mark.parametrize("every,stop_early", [(7, False), (7, True), (14, False), (5, False)])
+def test_reverse_sweep_plans_agree(gpu_lib, every, stop_early):
+    """The three reverse-sweep plans give bitwise the same gradients and
+    final state: sequential (mode 0: one tape, the last segment taped by the
+    forward sweep), overlapped on two tapes (mode 1 here: the forward sweep
+    tapes the last two segments) and overlapped on one tape (mode 2:
+    consecutive segments fill the tape in opposite slot orders, the
+    recompute writing each slot once the transpose has released it). Cases:
+    27 cycles in segments of 7 (a partial last one) and of 5 (six segments,
+    partial last), a run that reaches stoptime after about 17 cycles, inside
+    the third segment, and segments of 14."""
     L = gpu_lib
     nx, cycles = 8, 27
     g = developed(L, nx, 0, 0, 0xC7)
@@ -206,16 +208,17 @@ def test_overlapped_and_sequential_sweeps_agree(gpu_lib, every, stop_early):
             L.lagrangeLeapFrog(ref)
         stoptime = ref.time
     out = []
-    for overlap in (True, False, True):
+    for mode in (1, 0, 2, 1, 2):
         restore(g, snap)
         g.stoptime = stoptime
         adj = L.Adjoint(g, checkpoint_every=every)
-        adj.set_overlap(overlap)
+        adj.set_overlap(mode)
         loss = adj.gradient(cycles)
         if stop_early:
             assert 17 <= adj.result.cycles < cycles
         else:
             assert adj.result.cycles == cycles and adj.result.checkpoints == -(-cycles // every)
+        assert adj.result.sweep == mode, (mode, adj.result.sweep)
         out.append((loss, adj.result.grad_hgcoef, {f: adj.grad(f) for f in STATE},
                     {f: g.field(f) for f in STATE}))
         adj.close()
