@@ -184,7 +184,7 @@ def test_checkpoint_interval_and_final_state(gpu_lib):
             assert np.array_equal(other[2][f], grads[0][2][f]), f
 
 
-@pytest.mark.parametrize("every,stop_early", [(7, False), (7, True), (14, False), (5, False)])
+@pytest.mark.parametrize("every,stop_early", [(7, False), (7, True), (14, False), (5, False), (5, True)])
 def test_reverse_sweep_plans_agree(gpu_lib, every, stop_early):
     """The three reverse-sweep plans give bitwise the same gradients and
     final state: sequential (mode 0: one tape, the last segment taped by the
@@ -193,8 +193,8 @@ def test_reverse_sweep_plans_agree(gpu_lib, every, stop_early):
     consecutive segments fill the tape in opposite slot orders, the
     recompute writing each slot once the transpose has released it). Cases:
     27 cycles in segments of 7 (a partial last one) and of 5 (six segments,
-    partial last), a run that reaches stoptime after about 17 cycles, inside
-    the third segment, and segments of 14."""
+    partial last), runs that reach stoptime after about 17 cycles (inside the
+    third of four segments, or the fourth of six), and segments of 14."""
     L = gpu_lib
     nx, cycles = 8, 27
     g = developed(L, nx, 0, 0, 0xC7)
