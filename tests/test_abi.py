@@ -76,3 +76,32 @@ def test_no_fallback_without_library(tmp_path, monkeypatch):
     monkeypatch.setattr(lulesh_gb300, "_LIB", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         lulesh_gb300.load_library()
+
+
+def test_struct_layouts_match_header(gpu_lib, tmp_path):
+    """Every struct the Python mirror passes across the ABI has the header's
+    size and field offsets (a C program built against include/ prints them)."""
+    structs = {"lulesh_params": gpu_lib._Params, "lulesh_scalars": gpu_lib._Scalars,
+               "lulesh_instance": gpu_lib.Instance, "lulesh_tuning": gpu_lib.Tuning,
+               "lulesh_adj_result": gpu_lib.AdjResult}
+    lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "lulesh_gb300.h"', "int main(void) {"]
+    for cname, py in structs.items():
+        lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
+        for fname, _ in py._fields_:
+            lines.append(f'  printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for ln in out:
+        if ln:
+            parts = ln.split()
+            got[(parts[0], parts[1])] = int(parts[2])
+    for cname, py in structs.items():
+        assert got[(cname, "size")] == ctypes.sizeof(py), cname
+        for fname, _ in py._fields_:
+            assert got[(cname, fname)] == getattr(py, fname).offset, (cname, fname)
