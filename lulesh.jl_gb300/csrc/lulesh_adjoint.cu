@@ -443,7 +443,7 @@ int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_ever
   a->K = checkpoint_every;
   a->E = (int)dom->E;
   a->N = (int)dom->N;
-  const int E = a->E, N = a->N, K = a->K;
+  const int E = a->E, N = a->N;
   auto fail = [&](int rc) { lulesh_adj_destroy(a); return rc; };
   int rc;
   if ((rc = alloc_set(a, a->allocs, a->sets[0]))) return fail(rc);
