@@ -61,7 +61,7 @@ struct CycleTape {
   double *vnew, *delv, *arealg, *vdov, *dv[3], *dx[3];
   unsigned long long* flags;
   double *dtc, *dth;
-  double* geo;  // [102][E] force-kernel tape
+  double* geo;  // [66][E] force-kernel tape
   double* kin;  // [90][E] kinematics-kernel tape
   double* mat;  // [31][E] material-kernel tape
 };
@@ -84,6 +84,7 @@ struct TapeSet {
   std::vector<StateBuf> slots;
   std::vector<CycleTape> tape;
   CycleRec* rec = nullptr;
+  double* diag0 = nullptr;  // [36][E]: the face diagonals at the segment's start
   bool ready = false;
 };
 
@@ -164,13 +165,13 @@ static int alloc_set(lulesh_adjoint* a, std::vector<void*>& list, TapeSet& t) {
         (rc = dalloc_to(list, &c.vnew, E)) || (rc = dalloc_to(list, &c.delv, E)) ||
         (rc = dalloc_to(list, &c.arealg, E)) || (rc = dalloc_to(list, &c.vdov, E)) ||
         (rc = dalloc_to(list, &c.flags, E)) || (rc = dalloc_to(list, &c.dtc, E)) || (rc = dalloc_to(list, &c.dth, E)) ||
-        (rc = dalloc_to(list, &c.geo, 102 * (size_t)E)) || (rc = dalloc_to(list, &c.kin, 90 * (size_t)E)) ||
+        (rc = dalloc_to(list, &c.geo, 66 * (size_t)E)) || (rc = dalloc_to(list, &c.kin, 90 * (size_t)E)) ||
         (rc = dalloc_to(list, &c.mat, 31 * (size_t)E)))
       return rc;
     for (int k = 0; k < 3; ++k)
       if ((rc = dalloc_to(list, &c.dv[k], E)) || (rc = dalloc_to(list, &c.dx[k], E))) return rc;
   }
-  if ((rc = dalloc_to(list, &t.rec, K))) return rc;
+  if ((rc = dalloc_to(list, &t.rec, K)) || (rc = dalloc_to(list, &t.diag0, 36 * (size_t)E))) return rc;
   t.ready = true;
   return LULESH_OK;
 }
@@ -270,18 +271,20 @@ static void set_scalars(lulesh_domain* d, const Scalars5& s) {
 }
 
 // The start of a taped segment: the force kernel's geometry of the current
-// positions, with the first cycle's face diagonals and normals on its tape.
-static void tape_segment_begin(lulesh_adjoint* a, const CycleTape& first, cudaStream_t s) {
+// positions, with the first cycle's face normals on its tape and its face
+// diagonals in the set's diag0.
+static void tape_segment_begin(lulesh_adjoint* a, const CycleTape& first, double* diag0, cudaStream_t s) {
   DevDomain gd = a->dom->dd;
   gd.tapeGeoNext = first.geo;
+  gd.tapeDiag = diag0;
   launch_geometry(gd, s);
 }
 
 // One taped cycle, queued on the stream: the start state to its slot and
 // timeIncrement! on the device (recorded), the step kernels with the cycle's
 // intermediate values, accelerations, branch flags and dt candidates going to
-// the tape (the kinematics kernel also writes the next cycle's face diagonals
-// and normals to `next`, if there is one), then the arg-min elements of the
+// the tape (the kinematics kernel also writes the next cycle's face normals
+// to `next`, if there is one), then the arg-min elements of the
 // Courant and hydro minima.
 static void tape_cycle(lulesh_adjoint* a, StateBuf& slot, const CycleTape& tp, const CycleTape* next, CycleRec* rec,
                        cudaStream_t s) {
@@ -698,7 +701,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
       TapeSet& ts = set_of(k);
       const bool rev = rev_of(k);
       const int n = k < nplan - 1 ? K : last_len;
-      tape_segment_begin(a, ts.tape[tslot(rev, 0)], s);
+      tape_segment_begin(a, ts.tape[tslot(rev, 0)], ts.diag0, s);
       for (int j = 0; j < n; ++j)
         tape_cycle(a, ts.slots[sslot(rev, j)], ts.tape[tslot(rev, j)], j + 1 < n ? &ts.tape[tslot(rev, j + 1)] : nullptr,
                    ts.rec + tslot(rev, j), s);
@@ -753,7 +756,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
   cudaStream_t tst = pipe ? a->tstream : s;
   auto queue_recompute = [&](TapeSet& ts, int n, bool rev, cudaStream_t st) -> int {
     if (one) ACK(cudaStreamWaitEvent(st, a->ev_slot[tslot(rev, 0)], 0));
-    tape_segment_begin(a, ts.tape[tslot(rev, 0)], st);
+    tape_segment_begin(a, ts.tape[tslot(rev, 0)], ts.diag0, st);
     for (int j = 0; j < n; ++j) {
       if (one && j + 1 < n) ACK(cudaStreamWaitEvent(st, a->ev_slot[tslot(rev, j + 1)], 0));
       tape_cycle(a, ts.slots[sslot(rev, j)], ts.tape[tslot(rev, j)], j + 1 < n ? &ts.tape[tslot(rev, j + 1)] : nullptr,
@@ -850,6 +853,7 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     TapeSet& t0 = set_of(0);
     const bool r0 = rev_of(0);
     set_cycle_pointers(a, t0.slots[sslot(r0, 0)], t0.slots[sslot(r0, 1)], t0.tape[tslot(r0, 0)]);
+    a->ad.diag0 = t0.diag0;
     first_cycle_force_geo(a, s);
     ka_gather_corners<<<(a->N + kAdjBlock - 1) / kAdjBlock, kAdjBlock, 0, s>>>(a->ad);
   }

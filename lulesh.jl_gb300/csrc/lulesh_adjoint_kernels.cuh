@@ -58,7 +58,8 @@ struct AdjDev {
   const double *vnew, *delv, *arealg, *vdov;  // kinematics outputs (E)
   const double *dvl[3], *dxl[3];              // delv_{xi,eta,zeta}, delx_{xi,eta,zeta}
   const unsigned long long* flags;
-  const double* geo;                          // [102][E] force-kernel tape (dv, hms, S, N, diagonals)
+  const double* geo;                          // [66][E] force-kernel tape (dv, hms, S, N)
+  const double* diag0;                        // [36][E] face diagonals at the run's start (first cycle)
   const double* kin;                          // [90][E] kinematics-kernel tape
   const double* mat;                          // [31][E] material-kernel tape
   // adjoints of the state (in place: S1 on entry, S0 on exit)
@@ -988,8 +989,9 @@ __device__ __forceinline__ void force_geo_t(const AdjDev& a, int e, const V3 dgs
 }
 
 // The position transpose of the first cycle's k_force (the other cycles'
-// is part of ka_kinematics of the cycle before), from the force tape's
-// diagonals, into the force corner buffer that ka_gather_corners sums.
+// is part of ka_kinematics of the cycle before), from the face diagonals
+// taped at the segment's start (diag0), into the force corner buffer that
+// ka_gather_corners sums.
 template <int MODE>
 __global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
   const int E = a.E;
@@ -997,7 +999,7 @@ __global__ void __launch_bounds__(kAdjBlock, 3) ka_force_geo(AdjDev a) {
   if (e >= E) return;
   V3 dgs[12];
 #pragma unroll
-  for (int q = 0; q < 12; ++q) dgs[q] = v3(a.geo[(66 + 3 * q) * E + e], a.geo[(67 + 3 * q) * E + e], a.geo[(68 + 3 * q) * E + e]);
+  for (int q = 0; q < 12; ++q) dgs[q] = v3(a.diag0[(3 * q) * E + e], a.diag0[(3 * q + 1) * E + e], a.diag0[(3 * q + 2) * E + e]);
   const double s8 = ((-a.p0[e]) - a.q0[e]) * 0.125;
   double LX[3][8];
   force_geo_t<MODE>(a, e, dgs, s8, LX);

@@ -59,6 +59,7 @@ inline size_t layout(DevDomain& dd, char* base, int64_t E, int64_t N, bool aux, 
   dd.fcx = c.take<double>(8 * E); dd.fcy = c.take<double>(8 * E); dd.fcz = c.take<double>(8 * E);
   dd.nextGeo = c.take<double>((size_t)kGeoSlots * E);
   dd.tapeGeoNext = nullptr;
+  dd.tapeDiag = nullptr;
   dd.st = c.take<DevState>(ninst > 0 ? ninst : 1);
   if (ninst > 0) {
     dd.elemInst = c.take<int>(E);

@@ -143,8 +143,10 @@ struct DevDomain {
   // (formed by the kinematics kernel of the cycle before, or by k_geometry)
   double* nextGeo;
   // taped runs: the next cycle's force tape, where the kinematics kernel (or
-  // k_geometry) writes the face diagonals and normals of these positions
+  // k_geometry) writes the face normals of these positions, and at the start
+  // of a taped segment the buffer k_geometry writes their face diagonals to
   double* tapeGeoNext;
+  double* tapeDiag;
   // corner forces [8][E]
   double *fcx, *fcy, *fcz;
   // step state: one entry, or one per instance of an ensemble
@@ -163,12 +165,10 @@ struct DevDomain {
   unsigned long long* tapeFlags;
   double* tapeDtc;
   double* tapeDth;
-  // [102][E]: the force kernel's volume derivatives dv_j[n] (24, node
+  // [66][E]: the force kernel's volume derivatives dv_j[n] (24, node
   // order), hourglass modes over 12*determ (12), mode sums S_k[m] of the
-  // velocities (12), face-diagonal cross products (x, y, z of the 6 faces:
-  // 18; faces 0..4 written) and the 12 face diagonals d20 d31 d50 d14 d61
-  // d25 d72 d36 d43 d07 d64 d57 (36; written at the start of a taped
-  // segment only)
+  // velocities (12) and face-diagonal cross products (x, y, z of the 6
+  // faces: 18; faces 0..4 written)
   double* tapeGeo;
   // [90][E]: the kinematics kernel's Walsh vectors of positions (9) and
   // velocities (9), cofactor columns (9), 1/det (1), monotonic-Q cross

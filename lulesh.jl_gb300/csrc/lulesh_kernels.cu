@@ -204,18 +204,15 @@ __device__ __forceinline__ void tape_force_normals(double* tape, int E, int e, c
   }
 }
 
-// The force tape's face diagonals (slots 66 + 3q + k) and face normals of
-// these positions: at the start of a taped segment, where the position
-// transpose of a segment's first cycle reads them (the other cycles' is
-// fused into the kinematics transpose of the cycle before, which reads the
-// kinematics tape).
-__device__ __forceinline__ void tape_force_geometry(double* tape, int E, int e, const double g[12][3],
-                                                    const double n[6][3]) {
+// The face diagonals of these positions (slot 3q + k of a [36][E] buffer):
+// at the start of a taped segment, for the position transpose of the run's
+// first cycle (every other cycle's is fused into the kinematics transpose of
+// the cycle before, which reads the kinematics tape).
+__device__ __forceinline__ void tape_diagonals(double* diag, int E, int e, const double g[12][3]) {
 #pragma unroll
   for (int q = 0; q < 12; ++q)
 #pragma unroll
-    for (int k = 0; k < 3; ++k) tape[(66 + 3 * q + k) * E + e] = g[q][k];
-  tape_force_normals(tape, E, e, n);
+    for (int k = 0; k < 3; ++k) diag[(3 * q + k) * E + e] = g[q][k];
 }
 
 // The stored geometry of the current positions (see above): at the start of
@@ -241,7 +238,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_geometry(DevDomain d) {
   volume_terms(g, U, gU, gV, gW);
   volume_derivatives(gU, gV, gW, gr);
   store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w));
-  if (d.tapeGeoNext) tape_force_geometry(d.tapeGeoNext, E, e, g, n);
+  if (d.tapeGeoNext) tape_force_normals(d.tapeGeoNext, E, e, n);
+  if (d.tapeDiag) tape_diagonals(d.tapeDiag, E, e, g);
 }
 
 // ---------------------------------------------------------------------------
