@@ -347,8 +347,8 @@ def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
         errs.append(abs(an - fd) / max(abs(fd), 1e-12 * abs(loss)))
     adj.close()
     # the same gradient with the whole run taped in HBM (no recompute): one
-    # segment of `cycles` cycles, about 8 * (205 E + 9 N) bytes per cycle
-    tape_gb = 8.0 * (205 * g.numElem + 9 * g.numNode) * cycles / 1e9
+    # segment of `cycles` cycles, about 8 * (204 E + 6 N) bytes per cycle
+    tape_gb = 8.0 * (204 * g.numElem + 6 * g.numNode) * cycles / 1e9
     full = None
     try:
         adj2 = L.Adjoint(g, radius=0.3, checkpoint_every=cycles)

@@ -314,7 +314,7 @@ int lulesh_calc_force_for_nodes_static(const lulesh_force_args* args, void* stre
  * v ss (element); the gradient w.r.t. the run's initial value of each is
  * returned (lulesh_adj_get_gradient), with dL/dhgcoef in the result.
  * Memory: one state per checkpoint plus checkpoint_every cycles of tape
- * (about 8*(205*E + 9*N) bytes per taped cycle); a second tape of the same
+ * (about 8*(204*E + 6*N) bytes per taped cycle); a second tape of the same
  * size, allocated at the first gradient that has two or more segments if it
  * fits, lets the recompute of one segment overlap the transpose of the next
  * freely; without it they overlap on one tape (lulesh_adj_set_overlap). The derivative is that of the branches the

@@ -152,13 +152,26 @@ static int alloc_state_to(lulesh_adjoint* a, std::vector<void*>& list, StateBuf&
 }
 static int alloc_state(lulesh_adjoint* a, StateBuf& s) { return alloc_state_to(a, a->allocs, s); }
 
+// A tape set's per-cycle state: only the fields the transposes read (the
+// velocities, p, q, v, ss); positions and energy stay null, and the state
+// copies skip them.
+static int alloc_slot_state(lulesh_adjoint* a, std::vector<void*>& list, StateBuf& s) {
+  for (int k = 0; k < kStateFields; ++k) {
+    s.f[k] = nullptr;
+    if (k <= 2 || k == 6) continue;  // x y z e
+    int rc = dalloc_to(list, &s.f[k], k < 6 ? a->N : a->E);
+    if (rc) return rc;
+  }
+  return LULESH_OK;
+}
+
 // The K+1 states, K cycles of tape and K records of one tape set.
 static int alloc_set(lulesh_adjoint* a, std::vector<void*>& list, TapeSet& t) {
   const int E = a->E, N = a->N, K = a->K;
   int rc;
   t.slots.assign(K + 1, StateBuf{});
   for (auto& st : t.slots)
-    if ((rc = alloc_state_to(a, list, st))) return rc;
+    if ((rc = alloc_slot_state(a, list, st))) return rc;
   t.tape.assign(K, CycleTape{});
   for (auto& c : t.tape) {
     if ((rc = dalloc_to(list, &c.ax, N)) || (rc = dalloc_to(list, &c.ay, N)) || (rc = dalloc_to(list, &c.az, N)) ||

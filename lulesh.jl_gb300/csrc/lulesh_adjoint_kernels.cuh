@@ -1116,14 +1116,18 @@ __global__ void __launch_bounds__(kCloseBlock) ka_cycle_close(AdjDev a, int ge, 
 }
 
 // Copies the 11 state fields (node fields n < N, element fields n < E).
+// A field whose destination is null is not copied (a tape set's per-cycle
+// states keep only the fields the transposes read).
 __device__ __forceinline__ void copy_state_at(int i, const StateSet& src, const StateSet& dst, int E, int N) {
   if (i < N) {
 #pragma unroll
-    for (int k = 0; k < 6; ++k) dst.f[k][i] = src.f[k][i];
+    for (int k = 0; k < 6; ++k)
+      if (dst.f[k]) dst.f[k][i] = src.f[k][i];
   }
   if (i < E) {
 #pragma unroll
-    for (int k = 6; k < 11; ++k) dst.f[k][i] = src.f[k][i];
+    for (int k = 6; k < 11; ++k)
+      if (dst.f[k]) dst.f[k][i] = src.f[k][i];
   }
 }
 
