@@ -520,6 +520,15 @@ def run_ours(args):
         rate = inst / (dom_ms * 1e-3)
         fp64.update({"kernel": dominant, "achieved_inst_per_s": rate, "frac": rate / fma_s.value,
                      "fp64_inst_per_launch": inst, "fp64_inst_per_element": prof["fp64_inst_per_element"]})
+    # the whole step: every step kernel's FP64 instructions per cycle over the
+    # device-timed cycle
+    allprof = _profile_numbers()
+    if all(k in allprof for k in ("k_force", "k_node", "k_kinematics", "k_material")):
+        step_inst = (sum(allprof[k]["fp64_inst_per_element"] for k in ("k_force", "k_kinematics", "k_material")) * E
+                     + allprof["k_node"]["fp64_inst_per_node"] * N)
+        step_rate = step_inst * cycles / (ms * 1e-3)
+        fp64["step"] = {"fp64_inst_per_zone_cycle": step_inst / E, "achieved_inst_per_s": step_rate,
+                        "frac": step_rate / fma_s.value}
 
     g.close()  # the remaining legs build their own problems
     c3 = None
