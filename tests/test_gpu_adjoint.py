@@ -10,6 +10,9 @@ Checks:
     oracle, same bar;
   * gradients independent of the checkpoint interval, the domain left at the
     final state of a plain run, loss equal to the objective of that state;
+  * the three reverse-sweep plans (in turn, overlapped on two tapes,
+    overlapped on one) bitwise equal, also for runs stopped at stoptime;
+  * a run that takes no cycle;
   * central finite differences (step 1e-6 relative) of the GPU run on a few
     directions.
 The derivative is that of the branches the run takes; the inputs are chosen so
