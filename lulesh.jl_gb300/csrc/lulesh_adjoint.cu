@@ -697,59 +697,6 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     a->fwd_tuning = d->tuning;
     a->fwd_aux = aux;
   }
-  const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
-  state_to_device_mirror(d);  // no cycle limit: the segments count the cycles
-  ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
-  // the plain segments read the force geometry the kinematics kernel stores;
-  // the taping kernels form their own, so after the gradient (the domain left
-  // at the final state) it has to be formed again
-  ensure_geometry(d);
-  d->geo_valid = false;
-  for (int k = 0; k < nplan; ++k) {
-    copy_state_from_domain(a, a->ckpts[k], s);
-    ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
-    if (k < first_taped) {
-      ACK(cudaGraphLaunch(a->fwd_graph, s));
-    } else {
-      TapeSet& ts = set_of(k);
-      const bool rev = rev_of(k);
-      const int n = k < nplan - 1 ? K : last_len;
-      tape_segment_begin(a, ts.tape[tslot(rev, 0)], ts.diag0, s);
-      for (int j = 0; j < n; ++j)
-        tape_cycle(a, ts.slots[sslot(rev, j)], ts.tape[tslot(rev, j)], j + 1 < n ? &ts.tape[tslot(rev, j + 1)] : nullptr,
-                   ts.rec + tslot(rev, j), s);
-      copy_state_from_domain(a, ts.slots[sslot(rev, n)], s);
-    }
-  }
-  ACK(cudaGetLastError());
-  ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
-  ACK(cudaStreamSynchronize(s));
-  state_from_device_mirror(d);
-  const int64_t done = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
-  // segments that ran (a run that reached stoptime leaves later ones empty)
-  a->seg_len.clear();
-  for (int k = 0; k < nplan; ++k) {
-    const int64_t cap = k < nplan - 1 ? K : last_len;
-    const int64_t len = std::max<int64_t>(0, std::min<int64_t>(cap, done - (int64_t)k * K));
-    if (len == 0) break;
-    a->seg_len.push_back((int)len);
-  }
-  const int nseg = (int)a->seg_len.size();
-  if (d->status) { out.status = d->status; out.cycles = done; if (res) *res = out; return d->status; }
-  auto t1 = std::chrono::steady_clock::now();
-  out.cycles = done;
-  out.checkpoints = nseg;
-  if ((rc = objective(a, true, &out.loss))) return rc;
-  copy_state_from_domain(a, a->final_state, s);
-  const Scalars5 final_sc = get_scalars(d);
-  // ---- reverse sweep ----
-  ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
-  // the force-transpose inputs the first transposed cycle's ka_kinematics
-  // reads (no cycle after it): zero
-  ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
-  ACK(cudaMemsetAsync(a->ad.sLdv, 0, 24 * sizeof(double) * (size_t)a->E, s));
-  ACK(cudaMemsetAsync(a->ad.sLhm, 0, 12 * sizeof(double) * (size_t)a->E, s));
-  ACK(cudaMemsetAsync(a->ad.sLU, 0, 15 * sizeof(double) * (size_t)a->E, s));
   // Recompute R(k) (checkpoint k restored into the domain, its cycles taped
   // into set_of(k)) and transpose T(k) (the adjoint state through those
   // cycles, in reverse), in order k = nseg-1..0; segments the forward sweep
@@ -808,7 +755,9 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     ACK(ge);
     return LULESH_OK;
   };
-  const bool any_full = !one && std::count(a->seg_len.begin(), a->seg_len.end(), K) > 0;
+  // graphs of full segments, built before the forward sweep, whose taped
+  // full segments run them too
+  const bool any_full = !one && (nplan > 1 || last_len == K);
   for (int x = 0; x < nsets && any_full; ++x) {
     TapeSet& ts = a->sets[x];
     if (!a->rec_graph[x] && (rc = capture(&a->rec_graph[x], rs, [&] { return queue_recompute(ts, K, false, rs); })))
@@ -816,6 +765,58 @@ int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result
     if (!a->tr_graph[x] && (rc = capture(&a->tr_graph[x], tst, [&] { return queue_transpose(ts, K, false, tst); })))
       return rc;
   }
+  const int64_t c0 = (int64_t)d->sc[LULESH_S_CYCLE];
+  state_to_device_mirror(d);  // no cycle limit: the segments count the cycles
+  ACK(cudaMemcpyAsync(d->dd.st, d->hst, sizeof(DevState), cudaMemcpyHostToDevice, s));
+  // the plain segments read the force geometry the kinematics kernel stores;
+  // the taping kernels form their own, so after the gradient (the domain left
+  // at the final state) it has to be formed again
+  ensure_geometry(d);
+  d->geo_valid = false;
+  for (int k = 0; k < nplan; ++k) {
+    copy_state_from_domain(a, a->ckpts[k], s);
+    ACK(cudaMemcpyAsync(a->ckpt_st + k, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToDevice, s));
+    if (k < first_taped) {
+      ACK(cudaGraphLaunch(a->fwd_graph, s));
+    } else {
+      const int n = k < nplan - 1 ? K : last_len;
+      const int x = plan == kTwo ? (k & 1) : 0;
+      if (!one && n == K) {
+        ACK(cudaGraphLaunch(a->rec_graph[x], s));
+      } else if ((rc = queue_recompute(set_of(k), n, rev_of(k), s))) {
+        return rc;
+      }
+    }
+  }
+  ACK(cudaGetLastError());
+  ACK(cudaMemcpyAsync(d->hst, d->dd.st, sizeof(DevState), cudaMemcpyDeviceToHost, s));
+  ACK(cudaStreamSynchronize(s));
+  state_from_device_mirror(d);
+  const int64_t done = (int64_t)d->sc[LULESH_S_CYCLE] - c0;
+  // segments that ran (a run that reached stoptime leaves later ones empty)
+  a->seg_len.clear();
+  for (int k = 0; k < nplan; ++k) {
+    const int64_t cap = k < nplan - 1 ? K : last_len;
+    const int64_t len = std::max<int64_t>(0, std::min<int64_t>(cap, done - (int64_t)k * K));
+    if (len == 0) break;
+    a->seg_len.push_back((int)len);
+  }
+  const int nseg = (int)a->seg_len.size();
+  if (d->status) { out.status = d->status; out.cycles = done; if (res) *res = out; return d->status; }
+  auto t1 = std::chrono::steady_clock::now();
+  out.cycles = done;
+  out.checkpoints = nseg;
+  if ((rc = objective(a, true, &out.loss))) return rc;
+  copy_state_from_domain(a, a->final_state, s);
+  const Scalars5 final_sc = get_scalars(d);
+  // ---- reverse sweep ----
+  ACK(cudaMemsetAsync(a->dsc, 0, sizeof(AdjScal), s));
+  // the force-transpose inputs the first transposed cycle's ka_kinematics
+  // reads (no cycle after it): zero
+  ACK(cudaMemsetAsync(a->ad.fV, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLdv, 0, 24 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLhm, 0, 12 * sizeof(double) * (size_t)a->E, s));
+  ACK(cudaMemsetAsync(a->ad.sLU, 0, 15 * sizeof(double) * (size_t)a->E, s));
   auto recomputed = [&](int k) { return k < first_taped; };
   auto enqueue_R = [&](int k) -> int {
     const int x = plan == kTwo ? (k & 1) : 0, n = a->seg_len[k];
