@@ -704,9 +704,11 @@ __device__ __forceinline__ void volu_der(const double ex[12], const double ey[12
 //   dL/dhms_j = -coef sum_k (S_k (lf_k . dv_j) + T_k (V_k . dv_j)),
 //   dL/dcoef  = sum_k S_k . T_k,
 // where hg^T u = Gamma(u) - sum_j hms_j (dv_j . u): 3x3 dot-product tables
-// replace the 8x4 matrices hg and dL/dhg.
+// replace the 8x4 matrices hg and dL/dhg. Three blocks per SM (168
+// registers, a few spilled) run faster than two without spills: the
+// transpose is partly latency-bound at 48^3.
 template <int MODE>
-__global__ void __launch_bounds__(kAdjBlock) ka_hourglass(AdjDev a, double hgcoef) {
+__global__ void __launch_bounds__(kAdjBlock, 3) ka_hourglass(AdjDev a, double hgcoef) {
   const int E = a.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   double Lhg_coef = 0.0;
