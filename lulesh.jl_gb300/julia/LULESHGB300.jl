@@ -1,8 +1,12 @@
 # Julia binding of liblulesh_gb300 for LULESH.jl (single rank, one GPU).
 #
-# `GPUDomain(prob)` replaces `Domain(prob)`; `timeIncrement!` and
-# `lagrangeLeapFrog` get methods for it, so the loop of
-# examples/benchmark.jl:82-98 runs unchanged:
+# `GPUDomain(prob)` replaces `Domain(prob)`; `timeIncrement!`,
+# `lagrangeLeapFrog`, `commRecv`, `commSend`, `commSBN` and
+# `verifyAndWriteFinalOutput` get methods for it and it answers the
+# properties the script reads (`sizeX/Y/Z`, `nodalMass`, `time`, `stoptime`,
+# `cycle`, `deltatime`, `e`, ...), so examples/benchmark.jl:22-110 runs with
+# only `Domain(prob)` replaced by `GPUDomain(prob)` (and `enzyme` false).
+# Its loop, for example:
 #
 #     using LULESH, LULESHGB300
 #     prob = LuleshProblem(num_iters, true, nx, nr, balance, cost, Vector, Float64, nothing)
@@ -148,9 +152,23 @@ function Base.getproperty(d::GPUDomain, s::Symbol)
         return getfield(d, :nx)^3
     elseif s === :numNode
         return (getfield(d, :nx) + 1)^3
+    elseif s in (:sizeX, :sizeY, :sizeZ)
+        # a cube of edge nx on one rank (src/domain.jl:536-543)
+        return getfield(d, :nx)
+    elseif s === :comm
+        return nothing
     end
     error("GPUDomain has no field $s")
 end
+
+# ---- the one-rank communication calls of examples/benchmark.jl:57-64 ----
+# At one rank (comm === nothing) the reference's commRecv, commSend and
+# commSBN return at once (src/comm.jl:18-23, 296-302, 776-780); these methods
+# do the same for a GPUDomain, so the script's initial boundary exchange runs
+# unchanged. A GPUDomain is always one rank: its nodal masses are complete.
+LULESH.commRecv(::GPUDomain, msgType, xferFields, dx, dy, dz, doRecv, planeOnly) = nothing
+LULESH.commSend(::GPUDomain, msgType, fields, dx, dy, dz, doSend, planeOnly) = nothing
+LULESH.commSBN(::GPUDomain, fields) = nothing
 
 function Base.setproperty!(d::GPUDomain, s::Symbol, v)
     h = getfield(d, :handle)
