@@ -1147,8 +1147,8 @@ __global__ void __launch_bounds__(kAdjBlock) ka_tape_begin(StateSet src, StateSe
   copy_state_at(blockIdx.x * blockDim.x + threadIdx.x, src, dst, E, N);
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   if (st->status != 0u || st->done) return;
-  if (st->acc_courant != kInfBits) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
-  if (st->acc_hydro != kInfBits) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
+  if (dt_registers(st->acc_courant)) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
+  if (dt_registers(st->acc_hydro)) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
   st->acc_courant = kInfBits;
   st->acc_hydro = kInfBits;
   if (!(st->time < prm.stoptime)) { st->done = 1; return; }
@@ -1178,12 +1178,12 @@ __global__ void __launch_bounds__(kAdjBlock) ka_tape_close(const double* dtc, co
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned long long bc = st->acc_courant, bh = st->acc_hydro;
   if (i == 0) {
-    rec->active_c = bc != kInfBits;
-    rec->active_h = bh != kInfBits;
+    rec->active_c = dt_registers(bc);
+    rec->active_h = dt_registers(bh);
   }
   if (i >= E) return;
-  if (bc != kInfBits && (unsigned long long)__double_as_longlong(dtc[i]) == bc) atomicMin(&rec->argmin_c, i);
-  if (bh != kInfBits && (unsigned long long)__double_as_longlong(dth[i]) == bh) atomicMin(&rec->argmin_h, i);
+  if (dt_registers(bc) && (unsigned long long)__double_as_longlong(dtc[i]) == bc) atomicMin(&rec->argmin_c, i);
+  if (dt_registers(bh) && (unsigned long long)__double_as_longlong(dth[i]) == bh) atomicMin(&rec->argmin_h, i);
 }
 
 // Loss seed and value: L = sum_e w_e e + sum_n 0.5 w_n |u|^2 with

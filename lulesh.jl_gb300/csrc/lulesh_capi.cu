@@ -107,8 +107,8 @@ void lulesh::state_from_device_mirror(lulesh_domain* d) {
   d->sc[LULESH_S_TIME] = s->time;
   d->sc[LULESH_S_DELTATIME] = s->deltatime;
   double dtc = s->dtcourant, dth = s->dthydro;
-  if (s->acc_courant != kInfBits) { unsigned long long b = s->acc_courant; std::memcpy(&dtc, &b, 8); }
-  if (s->acc_hydro != kInfBits) { unsigned long long b = s->acc_hydro; std::memcpy(&dth, &b, 8); }
+  if (dt_registers(s->acc_courant)) { unsigned long long b = s->acc_courant; std::memcpy(&dtc, &b, 8); }
+  if (dt_registers(s->acc_hydro)) { unsigned long long b = s->acc_hydro; std::memcpy(&dth, &b, 8); }
   d->sc[LULESH_S_DTCOURANT] = dtc;
   d->sc[LULESH_S_DTHYDRO] = dth;
   d->sc[LULESH_S_CYCLE] = (double)s->cycle;

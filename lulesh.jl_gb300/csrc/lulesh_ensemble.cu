@@ -326,8 +326,10 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
   int64_t budget = 1;
   for (int i = 0; i < s->n; ++i) {
     DevState& d = s->hst[i];
-    if (d.acc_courant != kInfBits) { std::memcpy(&d.dtcourant, &d.acc_courant, 8); d.acc_courant = kInfBits; }
-    if (d.acc_hydro != kInfBits) { std::memcpy(&d.dthydro, &d.acc_hydro, 8); d.acc_hydro = kInfBits; }
+    if (dt_registers(d.acc_courant)) std::memcpy(&d.dtcourant, &d.acc_courant, 8);
+    if (dt_registers(d.acc_hydro)) std::memcpy(&d.dthydro, &d.acc_hydro, 8);
+    d.acc_courant = kInfBits;
+    d.acc_hydro = kInfBits;
     if (d.status == 0u) d.done = 0;
     d.first = 1;
     d.num_iters = num_iters;
@@ -386,8 +388,8 @@ int lulesh_ens_get_scalars(const lulesh_ensemble* s, int32_t i, lulesh_scalars* 
   DevState d;
   if (cudaMemcpy(&d, s->dd.st + i, sizeof(DevState), cudaMemcpyDeviceToHost) != cudaSuccess) return LULESH_ERR_CUDA;
   double dtc = d.dtcourant, dth = d.dthydro;
-  if (d.acc_courant != kInfBits) std::memcpy(&dtc, &d.acc_courant, 8);
-  if (d.acc_hydro != kInfBits) std::memcpy(&dth, &d.acc_hydro, 8);
+  if (dt_registers(d.acc_courant)) std::memcpy(&dtc, &d.acc_courant, 8);
+  if (dt_registers(d.acc_hydro)) std::memcpy(&dth, &d.acc_hydro, 8);
   out->time = d.time;
   out->deltatime = d.deltatime;
   out->dtcourant = dtc;

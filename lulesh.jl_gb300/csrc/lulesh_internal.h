@@ -113,6 +113,14 @@ struct DevState {
 
 constexpr unsigned long long kInfBits = 0x7FF0000000000000ull;
 
+// The Courant and hydro scans start at 1.0e+20 and keep a candidate only if it
+// is strictly below (src/domain.jl:2966, 3003-3014, 3022, 3041-3052): a cycle
+// registers a new dtcourant/dthydro only when its minimum lies below 1e20.
+// kDtRegisterBits is the bit pattern of 1.0e+20; for non-negative doubles
+// (and NaNs, whose patterns lie above +inf) the unsigned order is the FP order.
+constexpr unsigned long long kDtRegisterBits = 0x4415AF1D78B58C40ull;
+__host__ __device__ inline bool dt_registers(unsigned long long acc) { return acc < kDtRegisterBits; }
+
 // doubles per element of DevDomain::nextGeo
 constexpr int kGeoSlots = 51;
 

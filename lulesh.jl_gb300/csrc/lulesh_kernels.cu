@@ -992,8 +992,8 @@ __device__ void advance_time(DevState* st, const Params& prm) {
   if (st->done) return;
   if (st->status) { st->done = 1; return; }
   // fold the previous step's minima (src/domain.jl:3012-3014, 3050-3052)
-  if (st->acc_courant != kInfBits) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
-  if (st->acc_hydro != kInfBits) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
+  if (dt_registers(st->acc_courant)) st->dtcourant = __longlong_as_double((long long)st->acc_courant);
+  if (dt_registers(st->acc_hydro)) st->dthydro = __longlong_as_double((long long)st->acc_hydro);
   st->acc_courant = kInfBits;
   st->acc_hydro = kInfBits;
   // examples/benchmark.jl:82-98: while time < stoptime ... break if cycle >= num_iters

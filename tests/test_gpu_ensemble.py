@@ -112,3 +112,52 @@ def test_ensemble_stops_each_instance_at_stoptime(gpu_lib):
     for i in range(2):
         s = ens.scalars(i)
         assert s["time"] == 1e-2 and s["status"] == 0, (i, s)
+
+
+def c4_sample(instances, k=16, seed=0xC4):
+    """A seeded sample of k instance indices of the C4 draw that always holds
+    the smallest and the largest mesh and both region counts."""
+    nxs = [s["nx"] for s in instances]
+    must = {int(np.argmin(nxs)), int(np.argmax(nxs))}
+    must.add(next(i for i, s in enumerate(instances) if s["nr"] == 1))
+    must.add(next(i for i, s in enumerate(instances) if s["nr"] == 11))
+    rest = [i for i in range(len(instances)) if i not in must]
+    rng = np.random.default_rng(seed)
+    pick = rng.choice(rest, size=k - len(must), replace=False)
+    return sorted(must | {int(i) for i in pick})
+
+
+@pytest.mark.gpu
+def test_c4_draw_matches_oracle(gpu_lib, oracle_mod):
+    """The batched-ensemble configuration itself: the 256-instance draw of
+    seed 0xC4 (nx uniform in [16, 64], energy factor in [0.5, 2], hgcoef in
+    [2, 4], 1 or 11 regions) advanced 300 cycles as one ensemble; a seeded
+    sample of 16 instances, holding the smallest and largest meshes and both
+    region counts, is compared with the oracle run of the same instance."""
+    draw = gpu_lib.sedov_instances(0xC4, 256, 16, 64)
+    ens = gpu_lib.Ensemble(draw, mode=0)
+    iters = 300
+    ens.run(iters)
+    sample = c4_sample(draw)
+    assert len(sample) == 16
+    assert {draw[i]["nr"] for i in sample} == {1, 11}
+    assert min(draw[i]["nx"] for i in sample) == min(s["nx"] for s in draw)
+    assert max(draw[i]["nx"] for i in sample) == max(s["nx"] for s in draw)
+    for i in sample:
+        spec = draw[i]
+        o = oracle_mod.OracleDomain(spec["nx"], nr=spec["nr"], mode=0, seed=spec["region_seed"])
+        o.set("hgcoef", spec["hgcoef"])
+        o.set_einit(spec["einit"])
+        assert o.run(iters) == 0
+        s = ens.scalars(i)
+        assert s["status"] == 0, i
+        assert s["cycle"] == o.get("cycle"), i
+        assert s["cycle"] == iters or o.get("time") >= o.get("stoptime"), i
+        assert s["time"] == pytest.approx(o.get("time"), rel=1e-12), i
+        assert s["dtcourant"] == pytest.approx(o.get("dtcourant"), rel=1e-12), i
+        assert ens.field(i, "e")[0] == pytest.approx(o.field("e")[0], rel=1e-9), i
+        for f in STATE + ["vdov", "arealg"]:
+            a, b = ens.field(i, f), o.field(f)
+            assert rel_err(a, b, field_floor(f, b)) <= 1e-8, (i, f)
+        o.close()
+    ens.close()

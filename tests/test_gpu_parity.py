@@ -228,6 +228,53 @@ def test_bad_bc_mask_error(gpu_lib, oracle_mod):
     assert o.lagrange_leapfrog() == 3
 
 
+@pytest.mark.parametrize("path", ["stepwise", "device_run"])
+def test_courant_constraint_not_registered_at_or_above_1e20(gpu_lib, oracle_mod, path):
+    """calcCourantConstraintForElems starts its minimum at 1.0e+20 and keeps a
+    candidate only if it is strictly below (src/domain.jl:2966, 3003-3014):
+    when every active element's arealg/sqrt(dtf) is >= 1e20, dtcourant keeps
+    its old value. Provoked on the host: a 2^3 mesh scaled by 200 (elements
+    of edge 112.5, relative volume 8e6 after the step), a cold state (e = p =
+    q = 0, so ss takes its 3.3e-19 floor) and a uniform expansion (every
+    element active, vdov > 0)."""
+    L = gpu_lib
+    g, o = pair(L, oracle_mod, 2, mode=0)
+    for n in ["x", "y", "z"]:
+        pos = o.field(n) * 200.0
+        g.set_field(n, pos)
+        o.set_field(n, pos)
+        vel = 1e-3 * pos
+        g.set_field(n + "d", vel)
+        o.set_field(n + "d", vel)
+    zero = np.zeros(8)
+    for n in ["e", "p", "q"]:
+        g.set_field(n, zero)
+        o.set_field(n, zero)
+    g.dtcourant = 0.5
+    o.set("dtcourant", 0.5)
+    if path == "stepwise":
+        L.timeIncrement(g)
+        L.lagrangeLeapFrog(g)
+    else:
+        L.run(g, 1)
+    o.time_increment()
+    assert o.lagrange_leapfrog() == 0
+    # the precondition: every element active, every Courant candidate >= 1e20
+    vdov, arealg, ss = o.field("vdov"), o.field("arealg"), o.field("ss")
+    assert np.all(vdov > 0.0)
+    assert np.all(arealg / ss >= 1e20)
+    assert o.get("dtcourant") == 0.5
+    assert g.dtcourant == 0.5
+    assert g.dthydro == pytest.approx(o.get("dthydro"), rel=1e-12)
+    assert g.dthydro < 1e20
+    assert_scalars(g, o)
+    assert_fields(g, o, STATE_F64 + ["vdov", "arealg"])
+    # the next cycle's timeIncrement! sees the kept value in both
+    L.timeIncrement(g)
+    o.time_increment()
+    assert g.deltatime == pytest.approx(o.get("deltatime"), rel=1e-12)
+
+
 def test_error_stops_device_run(gpu_lib):
     g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=6))
     gpu_lib.run(g, 10)
@@ -262,12 +309,24 @@ def test_tiny_meshes_match_oracle(gpu_lib, oracle_mod, nx, mode):
 # ---- full-size checks -----------------------------------------------------------
 
 def test_full_size_s150_matches_oracle(gpu_lib, oracle_mod):
-    """The benchmark mesh (150^3) for a few cycles against the oracle."""
+    """The benchmark problem at its stated length: 150^3 (3,375,000
+    elements), 11 regions, faithful mode, 200 cycles, against the oracle
+    (OpenMP, ~25 s on 16 host cores). Same cycle count and time, origin
+    energy to 1e-9, every state field plus vdov and arealg to 1e-8, and
+    LULESH's symmetry numbers."""
     g, o = pair(gpu_lib, oracle_mod, 150, mode=0)
-    gpu_lib.run(g, 3)
-    assert o.run(3) == 0
+    s = gpu_lib.run(g, 200)
+    assert o.run(200) == 0
+    assert s["cycle"] == o.get("cycle") == 200
     assert_scalars(g, o)
-    assert_fields(g, o, STATE_F64 + ["vdov", "arealg"])
+    assert g.field("e")[0] == pytest.approx(o.field("e")[0], rel=1e-9)
+    assert_fields(g, o, STATE_F64 + ["vdov", "arealg", "delv"])
+    e0, maxabs, total, maxrel = gpu_lib.verify(g)
+    omaxabs, ototal, omaxrel = o.symmetry()
+    scale = np.abs(o.field("e")[: 150 ** 2]).max()
+    assert abs(maxabs - omaxabs) <= 1e-8 * scale
+    g.close()
+    o.close()
 
 
 def test_full_size_s150_is_deterministic(gpu_lib):
@@ -281,17 +340,24 @@ def test_full_size_s150_is_deterministic(gpu_lib):
     b.close()
 
 
+C3_CYCLES = int(os.environ.get("LULESH_C3_CYCLES", "500"))
+
+
 def test_largest_configuration_matches_oracle(gpu_lib, oracle_mod):
-    """The unbalanced-regions problem at its full size (256^3 = 16.8 M
-    elements, 11 regions, balance 4, cost 2) for 2 cycles, with the region
-    cost model on in the GPU run (results unchanged by it)."""
+    """The unbalanced-regions problem at its full size and length (256^3 =
+    16.8 M elements, 11 regions, balance 4, cost 2, 500 cycles), with the
+    region cost model on in the GPU run (results unchanged by it), against
+    the oracle (OpenMP, about five minutes on 16 host cores)."""
     L = gpu_lib
     g = L.Domain(L.LuleshProblem(nx=256, nr=11, balance=4, cost=2, region_reps=True))
     o = oracle_mod.OracleDomain(256, nr=11, balance=4, cost=2)
     for n in ["regNumList", "regElemSize", "regReps"]:
         assert np.array_equal(g.field(n), o.field(n)), n
-    L.run(g, 2)
-    assert o.run(2) == 0
+    s = L.run(g, C3_CYCLES)
+    assert o.run(C3_CYCLES) == 0
+    assert s["cycle"] == o.get("cycle") == C3_CYCLES
     assert_scalars(g, o)
-    assert_fields(g, o, STATE_F64 + ["vdov", "arealg"])
+    assert g.field("e")[0] == pytest.approx(o.field("e")[0], rel=1e-9)
+    assert_fields(g, o, STATE_F64 + ["vdov", "arealg", "delv"])
     g.close()
+    o.close()
