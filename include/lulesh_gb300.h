@@ -273,17 +273,24 @@ int lulesh_measure_fp64_peak(int32_t device, double* fma_per_s, double* add_per_
  * computation needs is a fixed array inside the library, so the call makes no
  * cudaMalloc, cudaFree or other allocating call.
  *   - at most LULESH_STATIC_MAX_ELEMS elements; larger problems are rejected
- *     with LULESH_ERR_ARGUMENT. The fixed array (6 MiB) stays resident on
- *     every GPU that loads the library until the process exits.
+ *     with LULESH_ERR_ARGUMENT.
+ *   - the fixed array (6 MiB) is committed on a device by the first call
+ *     there (CUDA loads the library's device code lazily), not when the
+ *     library is loaded; it then stays until the process exits. On a device
+ *     with no free memory that first call returns LULESH_ERR_CUDA.
  *   - every call shares that array: calls that overlap on the GPU (two
  *     streams or two host threads at once) race and give wrong forces.
  *   - the first call on a device looks up the array's address on that
  *     device; make it before any stream capture.
- * Computes fx, fy, fz exactly as calcForceForNodes (src/domain.jl:1764-1779)
- * does from the given state, on `stream` (a cudaStream_t, 0 for the legacy
- * default stream), and synchronizes that stream before returning.
- * Returns LULESH_ERR_VOLUME (with *site EARLY or HOURGLASS) on the
- * reference's volume checks. */
+ * Computes the nodal forces fx, fy, fz (stress plus hourglass forces) of the
+ * given state on `stream` (a cudaStream_t, 0 for the legacy default stream),
+ * then copies a status word to the host and synchronizes that stream before
+ * returning. The forces agree with those of the step's own force kernel to
+ * 1e-8 relative, not bitwise: here each corner's stress and hourglass terms
+ * are added before the node sum.
+ * Returns LULESH_ERR_VOLUME with *site LULESH_SITE_EARLY (an element's
+ * Jacobian determinant <= 0) or LULESH_SITE_HOURGLASS (a relative volume
+ * <= 0). */
 #define LULESH_STATIC_MAX_ELEMS 32768
 
 typedef struct {

@@ -11,7 +11,8 @@
 //
 // Costs and limits:
 //  * the array holds kStaticMaxElems elements' corner forces (6 MiB plus a
-//    status word) and every GPU that loads the library keeps it until the
+//    status word); CUDA loads the library's device code lazily, so a device
+//    commits the array at the first call made there and keeps it until the
 //    process exits;
 //  * all calls share it: two calls that overlap on the GPU (different
 //    streams, or different host threads) race on it and give wrong forces;
@@ -53,10 +54,12 @@ int scratch_address(double** out) {
   return LULESH_OK;
 }
 
-// Corner forces of one element, the same arithmetic as the step's force
-// kernel: stress integration (src/domain.jl:1087-1110) plus the FB hourglass
-// force (src/domain.jl:1462-1694), written to the scratch in the reference's
-// fx_elem layout (8*e + c).
+// Corner forces of one element: stress integration (src/domain.jl:1087-1110)
+// plus the FB hourglass force (src/domain.jl:1462-1694), written to the
+// scratch in the reference's fx_elem layout (8*e + c). The formulation is its
+// own (Walsh coefficients, each voluDer call as one FMA chain) rather than the
+// step kernels' shared face-diagonal functions; the tests hold it to the
+// step's forces and to the CPU oracle's calcForceForNodes at 1e-8.
 template <int MODE>
 __global__ void __launch_bounds__(128) k_static_corner_forces(lulesh_force_args a, double* scratch,
                                                                int64_t max_elems) {

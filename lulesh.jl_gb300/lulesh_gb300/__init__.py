@@ -116,6 +116,19 @@ class AdjResult(ctypes.Structure):
                 ("sweep", ctypes.c_int32), ("reserved", ctypes.c_int32)]
 
 
+class ForceArgs(ctypes.Structure):
+    """lulesh_force_args: device pointers for lulesh_calc_force_for_nodes_static."""
+    _fields_ = [("num_elem", ctypes.c_int64), ("num_node", ctypes.c_int64),
+                ("nodelist", ctypes.c_void_p), ("nodeElemStart", ctypes.c_void_p),
+                ("nodeElemCount", ctypes.c_void_p), ("nodeElemCornerList", ctypes.c_void_p),
+                ("x", ctypes.c_void_p), ("y", ctypes.c_void_p), ("z", ctypes.c_void_p),
+                ("xd", ctypes.c_void_p), ("yd", ctypes.c_void_p), ("zd", ctypes.c_void_p),
+                ("p", ctypes.c_void_p), ("q", ctypes.c_void_p), ("ss", ctypes.c_void_p),
+                ("v", ctypes.c_void_p), ("volo", ctypes.c_void_p), ("elemMass", ctypes.c_void_p),
+                ("hgcoef", ctypes.c_double), ("mode", ctypes.c_int32),
+                ("fx", ctypes.c_void_p), ("fy", ctypes.c_void_p), ("fz", ctypes.c_void_p)]
+
+
 _LIB = None
 
 

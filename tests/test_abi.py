@@ -83,7 +83,7 @@ def test_struct_layouts_match_header(gpu_lib, tmp_path):
     size and field offsets (a C program built against include/ prints them)."""
     structs = {"lulesh_params": gpu_lib._Params, "lulesh_scalars": gpu_lib._Scalars,
                "lulesh_instance": gpu_lib.Instance, "lulesh_tuning": gpu_lib.Tuning,
-               "lulesh_adj_result": gpu_lib.AdjResult}
+               "lulesh_adj_result": gpu_lib.AdjResult, "lulesh_force_args": gpu_lib.ForceArgs}
     lines = ["#include <stddef.h>", "#include <stdio.h>", '#include "lulesh_gb300.h"', "int main(void) {"]
     for cname, py in structs.items():
         lines.append(f'  printf("{cname} size %zu\\n", sizeof({cname}));')
