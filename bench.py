@@ -118,6 +118,14 @@ class ClockSampler:
                 "samples": len(sms)}
 
 
+def workload_config(nx, mode, world):
+    """The `config` both arms print for the same problem (identical dicts)."""
+    return {"workload": f"Sedov blast {nx}^3, 11 regions, balance 1, cost 1, FP64",
+            "nx": nx, "elements": nx ** 3, "nodes": (nx + 1) ** 3, "mode": mode,
+            "parallelism": "replicas" if world > 1 else "one problem",
+            "l2": "state larger than L2 (no flush)"}
+
+
 def _dist():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -173,7 +181,7 @@ def run_reference(args):
     oracle.build()
     L = oracle.load(openmp=True)
     threads = L.ora_max_threads()
-    d = oracle.OracleDomain(args.nx, nr=11)
+    d = oracle.OracleDomain(args.nx, nr=11, mode=args.mode)
     for _ in range(args.warmup):
         d.time_increment()
         d.lagrange_leapfrog()
@@ -190,8 +198,8 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": n, "warmup": args.warmup, "ms_per_step": 1e3 * dt / n, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Sedov blast {args.nx}^3, 11 regions, balance 1, cost 1, FP64",
-                       "nx": args.nx, "parallelism": "none (CPU)", "l2": "state larger than L2"},
+            "config": workload_config(args.nx, args.mode, world),
+            "device": f"host CPU, {threads} threads",
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -446,18 +454,31 @@ def run_ours(args):
     torch.cuda.synchronize(dev)
     barrier(world)
     start, end = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    # The timed region (exactly K cycles) runs `repeats` times back to back,
+    # through the problem's configured 200 cycles, so that the clock sampler
+    # (one reading per 200 ms) sees several readings; the reported time is the
+    # median region.
+    repeats = max(1, args.config_cycles // args.steps)
     c0 = g.cycle
+    region_ms = []
     with ClockSampler(dev) as clocks:
-        torch.cuda.synchronize(dev)
-        start.record(stream)
-        s = L.run(g, c0 + args.steps)
-        end.record(stream)
-        torch.cuda.synchronize(dev)
-    cycles = s["cycle"] - c0
-    ms = start.elapsed_time(end)
+        for _ in range(repeats):
+            torch.cuda.synchronize(dev)
+            barrier(world)
+            cr = g.cycle
+            start.record(stream)
+            s = L.run(g, cr + args.steps)
+            end.record(stream)
+            torch.cuda.synchronize(dev)
+            if s["cycle"] - cr != args.steps:
+                raise RuntimeError(f"a timed region ran {s['cycle'] - cr} of {args.steps} cycles")
+            region_ms.append(start.elapsed_time(end))
+    cycles = args.steps
+    total_cycles = g.cycle - c0
+    ms = sorted(region_ms)[len(region_ms) // 2]
     ms_max = max_over_ranks(ms, world)
     barrier(world)
-    ktimes = g.kernel_times()
+    ktimes = {k: v * cycles / total_cycles for k, v in g.kernel_times().items()}
     value = world * E * cycles / (ms_max * 1e-3)
 
     # end to end through the reference-facing calls: the Domain state comes
@@ -509,6 +530,7 @@ def run_ours(args):
     traffic = prof["dram_bytes_per_launch"] * prof_scale if prof.get("dram_bytes_per_launch") else None
     roofline = {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": hbm, "unit": "GB/s",
                 "frac": achieved / hbm, "traffic": traffic,
+                "traffic_source": _profile_numbers().get("source") if traffic else None,
                 "peak_source": f"MEASURED_PEAKS.json hbm_gbs ({peak_kind})",
                 "algorithmic_bytes_per_launch": dom_bytes}
     step_bytes = STEP_BYTES_PER_ELEM * E + STEP_BYTES_PER_NODE * N
@@ -548,13 +570,14 @@ def run_ours(args):
                "single_thread": {"value": rate1, "cores": 1,
                                  "sample": f"{n1} cycles in {dt1:.1f} s (oracle, serial build)"}}
 
+    clock_record = clocks.summary()
+    if clock_record.get("sm_mhz"):
+        clock_record["ms_per_step_x_sm_mhz"] = ms_max / cycles * clock_record["sm_mhz"]
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": cycles,
             "warmup": args.warmup, "ms_per_step": ms_max / cycles, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Sedov blast {args.nx}^3, 11 regions, balance 1, cost 1, FP64",
-                       "nx": args.nx, "elements": E, "nodes": N, "mode": args.mode,
-                       "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "state larger than L2 (no flush)"},
+            "config": workload_config(args.nx, args.mode, world),
+            "device": "GB300",
             "roofline": roofline,
             "step_roofline": {"achieved": step_gbs, "peak": hbm, "unit": "GB/s", "frac": step_gbs / hbm,
                               "algorithmic_bytes_per_cycle": step_bytes},
@@ -562,7 +585,9 @@ def run_ours(args):
             "kernel_ms_per_cycle": {k: v / cycles for k, v in ktimes.items()},
             "dominant_kernel": dominant,
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
-            "clocks": clocks.summary(), "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint,
+            "clocks": clock_record, "timed_regions": {"repeats": repeats, "cycles_each": cycles,
+                                                      "ms_each": region_ms, "reported": "median"},
+            "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint,
             "c3_unbalanced_regions": c3}
     print(json.dumps(line), flush=True)
     g.close()
@@ -577,6 +602,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--nx", type=int, default=NX)
     ap.add_argument("--mode", type=int, default=0)
+    ap.add_argument("--config-cycles", type=int, default=200,
+                    help="cycles of the configured problem the repeated timed regions span")
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-tune", action="store_true", help="keep the default block sizes")
@@ -586,7 +613,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-c3", action="store_true", help="skip the unbalanced-regions leg")
     ap.add_argument("--c3-nx", type=int, default=256)
-    ap.add_argument("--c3-cycles", type=int, default=50)
+    ap.add_argument("--c3-cycles", type=int, default=500)
     ap.add_argument("--adj-nx", type=int, default=48)
     ap.add_argument("--adj-cycles", type=int, default=200)
     ap.add_argument("--adj-every", type=int, default=20)
