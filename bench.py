@@ -40,6 +40,8 @@ NX = 150
 STEP_BYTES_PER_ELEM, STEP_BYTES_PER_NODE = 364, 152
 KERNEL_BYTES = {"k_force": (80, 48), "k_kinematics": (120, 48), "k_material": (164, 0), "k_node": (0, 104)}
 STATE_FIELDS = ["x", "y", "z", "xd", "yd", "zd", "e", "p", "q", "v", "ss"]
+GEOMETRY_SPLIT = {0: "force geometry formed by k_kinematics and stored for k_force",
+                  1: "force geometry formed inside k_force"}
 
 
 def _measured_peaks():
@@ -235,6 +237,7 @@ def ensemble_leg(L, torch, dev, n, cycles, world=1, rank=0):
     ens.close()
     # the same instances, one single-problem handle after another (setup untimed)
     loop_s = 0.0
+    per_instance = []
     for i, spec in enumerate(inst):
         g = L.Domain(L.LuleshProblem(nx=spec["nx"], nr=spec["nr"], device=dev))
         g.hgcoef = spec["hgcoef"]
@@ -248,9 +251,25 @@ def ensemble_leg(L, torch, dev, n, cycles, world=1, rank=0):
         L.run(g, cycles)
         b.record(s)
         torch.cuda.synchronize(dev)
-        loop_s += a.elapsed_time(b) * 1e-3
+        t_i = a.elapsed_time(b) * 1e-3
+        loop_s += t_i
+        per_instance.append((spec["nx"], t_i))
         g.close()
     loop_s = max_over_ranks(loop_s, world)
+    # where looping loses: per mesh-size bucket, the looped time against the
+    # time the same zone-cycles take at the ensemble's rate
+    ens_rate = total_elems * cycles / ens_s
+    breakdown = []
+    for lo, hi in ((16, 24), (25, 32), (33, 40), (41, 48), (49, 56), (57, 64)):
+        sel = [(nx, t) for nx, t in per_instance if lo <= nx <= hi]
+        if not sel:
+            continue
+        zc = sum(nx ** 3 for nx, _ in sel) * cycles
+        t_loop = sum(t for _, t in sel)
+        breakdown.append({"nx": f"{lo}-{hi}", "instances": len(sel), "looped_s": t_loop,
+                          "looped_zones_cycles_per_s": zc / t_loop,
+                          "us_per_cycle_per_instance": 1e6 * t_loop / (len(sel) * cycles),
+                          "s_at_ensemble_rate": zc / ens_rate, "lost_s": t_loop - zc / ens_rate})
     return {"config": f"{n} Sedov instances, nx uniform in [16, 64] (seed 0xC4), {cycles} cycles each, FP64",
             "instances": n, "cycles": cycles, "total_elements_rank0": total_elems,
             "instances_rank0": mine, "instances_completed_rank0": int(done),
@@ -259,7 +278,8 @@ def ensemble_leg(L, torch, dev, n, cycles, world=1, rank=0):
             "looped_plain_problems_per_s": n / loop_s, "looped_plain_seconds": loop_s,
             "speedup_vs_looped_plain": loop_s / ens_s,
             "zones_cycles_per_s_rank0": total_elems * cycles / ens_s,
-            "tuning": tuning}
+            "looped_breakdown_rank0": breakdown,
+            "tuning": tuning, "geometry_split": GEOMETRY_SPLIT[tuning["geometry"]]}
 
 
 def adjoint_leg(L, torch, dev, nx, cycles, every, dirs):
@@ -426,6 +446,36 @@ def c3_leg(L, torch, dev, nx, cycles, warmup=2):
     return out
 
 
+def blocks_leg(L, torch, dev, nx, tp, cycles, plain_ms, warmup=3):
+    """The multi-rank decomposition on one GPU: the (tp*nx)^3 problem as tp^3
+    blocks of nx^3 elements with halo copies across block faces (bitwise the
+    single-block run, tested), timed over `cycles` cycles against the
+    single-block step time of the same problem."""
+    g = L.Domain(L.LuleshProblem(nx=nx, nr=11, blocks_per_edge=tp, device=dev))
+    stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+    L.run(g, warmup)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    c0 = g.cycle
+    torch.cuda.synchronize(dev)
+    a.record(stream)
+    L.run(g, c0 + cycles)
+    b.record(stream)
+    torch.cuda.synchronize(dev)
+    ms = a.elapsed_time(b) / (g.cycle - c0)
+    g.enable_timing(True)
+    L.run(g, g.cycle + 5)
+    kt = {k: v / 5 for k, v in g.kernel_times().items()}
+    out = {"config": f"Sedov {nx * tp}^3 as {tp}^3 blocks of {nx}^3 (the reference's {tp ** 3}-rank "
+                     "decomposition) with halo copies, FP64, one GPU",
+           "blocks": tp ** 3, "block_nx": nx, "cycles": int(g.cycle - c0), "ms_per_cycle": ms,
+           "zones_cycles_per_s": (nx * tp) ** 3 / (ms * 1e-3),
+           "single_block_ms_per_cycle": plain_ms, "overhead_vs_single_block": ms / plain_ms - 1.0,
+           "kernel_ms_per_cycle_with_halo": kt,
+           "nodes_packed": g.numNode, "nodes_whole_mesh": (nx * tp + 1) ** 3}
+    g.close()
+    return out
+
+
 def run_ours(args):
     world, rank, local = _dist()
     import torch
@@ -553,6 +603,9 @@ def run_ours(args):
                         "frac": step_rate / fma_s.value}
 
     g.close()  # the remaining legs build their own problems
+    blocks = None
+    if not args.no_blocks and args.nx % 2 == 0:
+        blocks = blocks_leg(L, torch, dev, args.nx // 2, 2, args.steps, ms / cycles)
     c3 = None
     if not args.no_c3:
         c3 = c3_leg(L, torch, dev, args.c3_nx, args.c3_cycles)
@@ -587,8 +640,8 @@ def run_ours(args):
             "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": 5 * cycles,
             "clocks": clock_record, "timed_regions": {"repeats": repeats, "cycles_each": cycles,
                                                       "ms_each": region_ms, "reported": "median"},
-            "tuning": tuning, "ensemble": ensemble, "adjoint": adjoint,
-            "c3_unbalanced_regions": c3}
+            "tuning": tuning, "geometry_split": GEOMETRY_SPLIT[tuning["geometry"]], "ensemble": ensemble, "adjoint": adjoint,
+            "c3_unbalanced_regions": c3, "blocks": blocks}
     print(json.dumps(line), flush=True)
     g.close()
     return 0
@@ -612,6 +665,7 @@ def main():
     ap.add_argument("--ens-cycles", type=int, default=300)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-c3", action="store_true", help="skip the unbalanced-regions leg")
+    ap.add_argument("--no-blocks", action="store_true", help="skip the multi-block (halo) leg")
     ap.add_argument("--c3-nx", type=int, default=256)
     ap.add_argument("--c3-cycles", type=int, default=500)
     ap.add_argument("--adj-nx", type=int, default=48)

@@ -189,15 +189,50 @@ int lulesh_enable_timing(lulesh_domain* dom, int32_t enable);
 int lulesh_kernel_times(lulesh_domain* dom, double* ms, int32_t max_kernels, int32_t* n_kernels);
 const char* lulesh_kernel_name(int32_t index);
 
+/* ---- Blocks of one mesh (the multi-rank decomposition) --------------------
+ * The reference's multi-rank run splits the (tp*nx)^3 Sedov mesh into a cube
+ * of tp^3 ranks of nx^3 elements each (initMeshDecomp, src/LULESH.jl:62-97)
+ * and exchanges block-face data every cycle: the summed nodal forces
+ * (commSBN, src/comm.jl:776), positions and velocities (commSyncPosVel,
+ * src/comm.jl:1251), the monotonic-Q gradients beside a face (commMonoQ,
+ * src/comm.jl:1127) and the time-step minimum (comm_min, src/mpi.jl:81).
+ * lulesh_create_blocks builds that decomposition in one GPU's memory: the
+ * handle's arrays hold the blocks one after another (rank order, each in its
+ * per-rank element and node order, nodes on block faces once per block that
+ * touches them; params->nx is the block edge), and every value that crosses
+ * a block face is a ghost slot filled by a halo copy from the block that
+ * owns it. The result is bitwise the single-block run of the whole mesh.
+ * Every other call (step, run, fields, state files, tuning) works on the
+ * packed arrays; lulesh_block_map gives each packed element's and node's id
+ * in the whole mesh. The region cost model and the adjoint need one block.
+ * lulesh_block_plan_sizes / lulesh_block_plan return the decomposition and
+ * its halo plan without a GPU: per ghost slot the packed element (delv) or
+ * corner-force slot c*E + e (corners) it copies and the block it belongs to;
+ * sizes = {E, N, ghost delv slots, ghost corner slots, corner-list entries}. */
+int lulesh_create_blocks(const lulesh_params* params, int32_t blocks_per_edge, lulesh_domain** out);
+int lulesh_block_map(const lulesh_domain* dom, int32_t* blocks_per_edge, int32_t* elem_global,
+                     int32_t* node_global);
+int lulesh_block_plan_sizes(int32_t nx, int32_t blocks_per_edge, int32_t mode, int64_t sizes[5]);
+int lulesh_block_plan(int32_t nx, int32_t blocks_per_edge, int32_t mode, int32_t* elem_global, int32_t* node_global,
+                      int32_t* halo_delv_src, int32_t* halo_delv_dst, int32_t* halo_corner_src,
+                      int32_t* halo_corner_dst);
+
 /* ---- Launch tuning --------------------------------------------------------
- * Threads per block of the four step kernels. lulesh_autotune tries each
- * candidate for one kernel at a time on the live problem (cycles timed with
- * CUDA events), keeps the fastest, and restores the problem's state. */
+ * Threads per block of the four step kernels and the fusion split of the
+ * force geometry. lulesh_autotune tries each block-size candidate for one
+ * kernel at a time on the live problem (cycles timed with CUDA events),
+ * keeps the fastest, then times the other geometry split with its own best
+ * force and kinematics blocks and keeps the faster split; it restores the
+ * problem's state. No choice changes any result (bitwise). */
 typedef struct {
   int32_t force_block;   /* k_force: 64, 128 or 256 */
   int32_t node_block;    /* k_node: 128, 256 or 512 */
   int32_t kin_block;     /* k_kinematics: 64, 128 or 256 */
   int32_t mat_block;     /* k_material: 64, 128 or 256 */
+  int32_t geometry;      /* where the force kernel's geometry of the positions
+                            (volume derivatives, hourglass modes, node normals)
+                            is formed: 0 by k_kinematics of the cycle before,
+                            stored (408 B per element); 1 inside k_force */
 } lulesh_tuning;
 
 int lulesh_get_tuning(const lulesh_domain* dom, lulesh_tuning* out);

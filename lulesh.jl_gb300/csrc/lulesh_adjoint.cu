@@ -450,6 +450,8 @@ extern "C" {
 
 int lulesh_adj_create(lulesh_domain* dom, double radius, int32_t checkpoint_every, lulesh_adjoint** out) {
   if (!dom || !out || checkpoint_every < 1 || !(radius >= 0.0)) return LULESH_ERR_ARGUMENT;
+  // the adjoint kernels have no halo transposes: one block only
+  if (dom->dd.haloDelvSrc || dom->dd.haloCornerSrc) return LULESH_ERR_ARGUMENT;
   *out = nullptr;
   ACK(cudaSetDevice(dom->params.device));
   lulesh_adjoint* a = new (std::nothrow) lulesh_adjoint();

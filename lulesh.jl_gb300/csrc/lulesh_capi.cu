@@ -66,8 +66,10 @@ Params lulesh::make_params(const lulesh_domain* d) {
   return p;
 }
 
+// The stored force geometry is needed before a step of the stored split; the
+// other split forms it in k_force and leaves d.nextGeo untouched (stale).
 void lulesh::ensure_geometry(lulesh_domain* d) {
-  if (d->geo_valid) return;
+  if (d->geo_valid || d->tuning.geo != 0) return;
   launch_geometry(d->dd, d->stream);
   d->geo_valid = true;
 }
@@ -271,20 +273,15 @@ const char* lulesh_kernel_name(int32_t index) {
   return (index >= 0 && index < kNumKernels) ? kKernelNames[index] : "";
 }
 
-int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
-  if (!params || !out) return LULESH_ERR_ARGUMENT;
-  *out = nullptr;
+}  // extern "C"
+
+// A handle for the mesh `m` (one block, or packed blocks with their halo plan).
+static int create_domain(const lulesh_params* params, HostMesh& m, lulesh_domain** out) {
   const int nx = params->nx;
-  // 8*numElem must fit a 32-bit index
-  if (nx < 1 || nx > 640 || params->nr < 1 || params->balance < 0 || params->cost < 0 ||
-      params->mode < 0 || params->mode > 7)
-    return LULESH_ERR_ARGUMENT;
   CK(cudaSetDevice(params->device));
   lulesh_domain* d = new (std::nothrow) lulesh_domain();
   if (!d) return LULESH_ERR_MEMORY;
   d->params = *params;
-  HostMesh m;
-  build_mesh(m, nx, params->nr, params->balance, params->cost, params->region_seed);
   d->E = m.E;
   d->N = m.N;
   set_default_scalars(d->sc);
@@ -292,10 +289,10 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
 
   const bool aux = params->keep_aux != 0;
   DevDomain& dd = d->dd;
-  const size_t bytes = layout(dd, nullptr, m.E, m.N, aux, 0);
+  const size_t bytes = layout(dd, nullptr, m.E, m.N, aux, 0, m.Eg, m.nCornerSlot, m.nCornerList);
   cudaError_t err = cudaMalloc(&d->arena, bytes);
   if (err != cudaSuccess) { delete d; cudaGetLastError(); return LULESH_ERR_MEMORY; }
-  layout(dd, (char*)d->arena, m.E, m.N, aux, 0);
+  layout(dd, (char*)d->arena, m.E, m.N, aux, 0, m.Eg, m.nCornerSlot, m.nCornerList);
   dd.E = (int)m.E;
   dd.N = (int)m.N;
   dd.nx = nx;
@@ -320,7 +317,7 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
       (rc = h2d(dd.z, m.z.data(), N, s)) || (rc = h2d(dd.nodalMass, m.nodalMass.data(), N, s)) ||
       (rc = h2d(dd.inv_nodalMass, inv_mass.data(), N, s)) ||
       (rc = h2d(dd.nodeElemStart, start.data(), N + 1, s)) ||
-      (rc = h2d(dd.cornerList, m.cornerList.data(), 8 * E, s)) ||
+      (rc = h2d(dd.cornerList, m.cornerList.data(), m.cornerList.size(), s)) ||
       (rc = h2d(dd.nodelist, nodelist_cm.data(), 8 * E, s)) ||
       (rc = h2d(dd.volo, m.volo.data(), E, s)) || (rc = h2d(dd.inv_volo, inv_volo.data(), E, s)) ||
       (rc = h2d(dd.elemMass, m.elemMass.data(), E, s)) || (rc = h2d(dd.v, ones.data(), E, s)) ||
@@ -329,6 +326,15 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
       (rc = h2d(dd.letam, m.letam.data(), E, s)) || (rc = h2d(dd.letap, m.letap.data(), E, s)) ||
       (rc = h2d(dd.lzetam, m.lzetam.data(), E, s)) || (rc = h2d(dd.lzetap, m.lzetap.data(), E, s)))
     return fail(rc);
+  if (!m.haloDelvSrc.empty() && (rc = h2d(const_cast<int*>(dd.haloDelvSrc), m.haloDelvSrc.data(), m.haloDelvSrc.size(), s)))
+    return fail(rc);
+  if (!m.haloCornerSrc.empty() &&
+      (rc = h2d(const_cast<int*>(dd.haloCornerSrc), m.haloCornerSrc.data(), m.haloCornerSrc.size(), s)))
+    return fail(rc);
+  d->blocks_per_edge = m.blocks_per_edge;
+  d->elemGlobal = m.elemGlobal;
+  d->nodeGlobal = m.nodeGlobal;
+  d->haloCornerSrc = m.haloCornerSrc;
   d->symmX = m.symmX; d->symmY = m.symmY; d->symmZ = m.symmZ;
   d->regNumList = m.regNumList; d->regElemlist = m.regElemlist; d->regCSR = m.regCSR;
   d->regReps = m.regReps; d->regSorted = m.regSorted; d->regElemSize = m.regElemSize;
@@ -359,6 +365,87 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
   if ((rc = h2d(dd.st, d->hst, 1, s))) return fail(rc);
   if ((err = cudaStreamSynchronize(s)) != cudaSuccess) return fail(cuda_fail(err));
   *out = d;
+  return LULESH_OK;
+}
+
+static bool valid_params(const lulesh_params* p) {
+  return p && p->nx >= 1 && p->nx <= 640 && p->nr >= 1 && p->balance >= 0 && p->cost >= 0 && p->mode >= 0 &&
+         p->mode <= 7;
+}
+
+extern "C" {
+
+int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
+  if (!params || !out) return LULESH_ERR_ARGUMENT;
+  *out = nullptr;
+  // 8*numElem must fit a 32-bit index
+  if (!valid_params(params)) return LULESH_ERR_ARGUMENT;
+  HostMesh m;
+  build_mesh(m, params->nx, params->nr, params->balance, params->cost, params->region_seed);
+  return create_domain(params, m, out);
+}
+
+// The packed block mesh of (nx*tp)^3 elements in tp^3 blocks; 0 or the error.
+static int block_mesh(HostMesh& m, int nx, int tp, int nr, int balance, int cost, int mode, uint64_t seed) {
+  const int64_t nxg = (int64_t)nx * tp;
+  // every packed index (corner slots and corner-list entries included) must fit 31 bits
+  if (tp < 1 || nx < 1 || nxg > 600) return LULESH_ERR_ARGUMENT;
+  HostMesh g;
+  build_mesh(g, (int)nxg, 1, 1, 1, 0);
+  build_block_mesh(m, g, nx, tp, mode);
+  if (m.nCornerSlot >= INT32_MAX || m.nCornerList >= INT32_MAX || m.Eg >= INT32_MAX) return LULESH_ERR_ARGUMENT;
+  build_regions(m, nr, balance, cost, seed);
+  return LULESH_OK;
+}
+
+int lulesh_create_blocks(const lulesh_params* params, int32_t blocks_per_edge, lulesh_domain** out) {
+  if (!params || !out) return LULESH_ERR_ARGUMENT;
+  *out = nullptr;
+  if (!valid_params(params) || params->region_reps) return LULESH_ERR_ARGUMENT;
+  HostMesh m;
+  int rc = block_mesh(m, params->nx, blocks_per_edge, params->nr, params->balance, params->cost, params->mode,
+                      params->region_seed);
+  if (rc) return rc;
+  return create_domain(params, m, out);
+}
+
+int lulesh_block_map(const lulesh_domain* d, int32_t* blocks_per_edge, int32_t* elem_global, int32_t* node_global) {
+  if (!d) return LULESH_ERR_ARGUMENT;
+  if (blocks_per_edge) *blocks_per_edge = d->blocks_per_edge;
+  for (int64_t i = 0; elem_global && i < d->E; ++i) elem_global[i] = d->elemGlobal.empty() ? (int32_t)i : d->elemGlobal[i];
+  for (int64_t i = 0; node_global && i < d->N; ++i) node_global[i] = d->nodeGlobal.empty() ? (int32_t)i : d->nodeGlobal[i];
+  return LULESH_OK;
+}
+
+int lulesh_block_plan_sizes(int32_t nx, int32_t blocks_per_edge, int32_t mode, int64_t sizes[5]) {
+  if (!sizes || mode < 0 || mode > 7) return LULESH_ERR_ARGUMENT;
+  HostMesh m;
+  int rc = block_mesh(m, nx, blocks_per_edge, 1, 1, 1, mode, 0);
+  if (rc) return rc;
+  sizes[0] = m.E;
+  sizes[1] = m.N;
+  sizes[2] = (int64_t)m.haloDelvSrc.size();
+  sizes[3] = (int64_t)m.haloCornerSrc.size();
+  sizes[4] = m.nCornerList;
+  return LULESH_OK;
+}
+
+int lulesh_block_plan(int32_t nx, int32_t blocks_per_edge, int32_t mode, int32_t* elem_global, int32_t* node_global,
+                      int32_t* halo_delv_src, int32_t* halo_delv_dst, int32_t* halo_corner_src,
+                      int32_t* halo_corner_dst) {
+  if (mode < 0 || mode > 7) return LULESH_ERR_ARGUMENT;
+  HostMesh m;
+  int rc = block_mesh(m, nx, blocks_per_edge, 1, 1, 1, mode, 0);
+  if (rc) return rc;
+  auto put = [](int32_t* dst, const std::vector<int>& v) {
+    if (dst) std::copy(v.begin(), v.end(), dst);
+  };
+  put(elem_global, m.elemGlobal);
+  put(node_global, m.nodeGlobal);
+  put(halo_delv_src, m.haloDelvSrc);
+  put(halo_delv_dst, m.haloDelvDst);
+  put(halo_corner_src, m.haloCornerSrc);
+  put(halo_corner_dst, m.haloCornerDst);
   return LULESH_OK;
 }
 
@@ -414,8 +501,9 @@ int lulesh_lagrange_leapfrog(lulesh_domain* d) {
   CK(cudaStreamSynchronize(d->stream));
   if (d->timing && (rc = collect_times(d))) return rc;
   state_from_device_mirror(d);
-  // a step that stopped early may leave the stored geometry behind the positions
-  if (d->status) d->geo_valid = false;
+  // a step that stopped early may leave the stored geometry behind the
+  // positions; the inline split stores none
+  if (d->status || d->tuning.geo != 0) d->geo_valid = false;
   return d->status;
 }
 
@@ -472,7 +560,7 @@ int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
   if ((rc = d2h(d->hst, d->dd.st, 1, s))) return rc;
   CK(cudaStreamSynchronize(s));
   state_from_device_mirror(d);
-  if (d->status) d->geo_valid = false;
+  if (d->status || d->tuning.geo != 0) d->geo_valid = false;
   if (out) lulesh_get_scalars(d, out);
   return d->status;
 }
@@ -583,7 +671,7 @@ static int64_t field_len(const lulesh_domain* d, int32_t f) {
     case LULESH_F_SYMMY: return (int64_t)d->symmY.size();
     case LULESH_F_SYMMZ: return (int64_t)d->symmZ.size();
     case LULESH_F_NODEELEMCOUNT: case LULESH_F_NODEELEMSTART: return N;
-    case LULESH_F_NODEELEMCORNERLIST: return 8 * E;
+    case LULESH_F_NODEELEMCORNERLIST: return d->dd.nCornerList;
     case LULESH_F_MATELEMLIST: case LULESH_F_REGNUMLIST: case LULESH_F_REGELEMLIST: return E;
     case LULESH_F_REGCSR: case LULESH_F_REGREPS: case LULESH_F_REGSORTED: case LULESH_F_REGELEMSIZE:
       return d->params.nr;
@@ -660,12 +748,15 @@ int lulesh_download_field(lulesh_domain* d, int32_t f, void* host, int64_t count
       return LULESH_OK;
     }
     case LULESH_F_NODEELEMCORNERLIST: {
-      std::vector<int> t(8 * E);
-      if ((rc = d2h(t.data(), d->dd.cornerList, 8 * E, s))) return rc;
+      std::vector<int> t(n);
+      if ((rc = d2h(t.data(), d->dd.cornerList, n, s))) return rc;
       CK(cudaStreamSynchronize(s));
-      // Julia value: 1-based element-major corner k = 8*e + c + 1
-      for (int64_t i = 0; i < 8 * E; ++i) {
-        const int64_t v = t[i], c = v / E, e = v % E;
+      // Julia value: 1-based element-major corner k = 8*e + c + 1 (a ghost
+      // slot of a block mesh gives the corner it copies)
+      for (int64_t i = 0; i < n; ++i) {
+        int64_t v = t[i];
+        if (v >= 8 * E) v = d->haloCornerSrc[v - 8 * E];
+        const int64_t c = v / E, e = v % E;
         out[i] = 8 * e + c + 1;
       }
       return LULESH_OK;
@@ -777,18 +868,22 @@ int lulesh_get_tuning(const lulesh_domain* d, lulesh_tuning* out) {
   out->node_block = d->tuning.node;
   out->kin_block = d->tuning.kin;
   out->mat_block = d->tuning.mat;
+  out->geometry = d->tuning.geo;
   return LULESH_OK;
 }
 
 int lulesh_set_tuning(lulesh_domain* d, const lulesh_tuning* t) {
   auto elem_ok = [](int b) { return b == 64 || b == 128 || b == 256; };
   if (!d || !t || !elem_ok(t->force_block) || !elem_ok(t->kin_block) || !elem_ok(t->mat_block) ||
-      !(t->node_block == 128 || t->node_block == 256 || t->node_block == 512))
+      !(t->node_block == 128 || t->node_block == 256 || t->node_block == 512) ||
+      !(t->geometry == 0 || t->geometry == 1))
     return LULESH_ERR_ARGUMENT;
   d->tuning.force = t->force_block;
   d->tuning.node = t->node_block;
   d->tuning.kin = t->kin_block;
   d->tuning.mat = t->mat_block;
+  if (d->tuning.geo != t->geometry) d->geo_valid = false;
+  d->tuning.geo = t->geometry;
   drop_graph(d);
   return LULESH_OK;
 }

@@ -338,7 +338,7 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
   ECK(cudaMemcpyAsync(s->dd.st, s->hst, sizeof(DevState) * s->n, cudaMemcpyHostToDevice, st));
   // the force kernel's stored geometry (an instance that stopped on an error
   // keeps its positions until a reset, which clears this)
-  if (!s->geo_valid) {
+  if (!s->geo_valid && s->tuning.geo == 0) {
     launch_geometry(s->dd, st);
     s->geo_valid = true;
   }
@@ -366,6 +366,7 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
     for (int i = 0; i < s->n && all_done; ++i) all_done = s->hst[i].done != 0;
     if (all_done || launched >= budget) break;
   }
+  if (s->tuning.geo != 0) s->geo_valid = false;  // the inline split stores no geometry
   for (int i = 0; i < s->n; ++i) {
     int32_t status, site;
     decode(s->hst[i].status, &status, &site);
@@ -465,13 +466,15 @@ int lulesh_ens_get_tuning(const lulesh_ensemble* s, lulesh_tuning* out) {
   out->node_block = s->tuning.node;
   out->kin_block = s->tuning.kin;
   out->mat_block = s->tuning.mat;
+  out->geometry = s->tuning.geo;
   return LULESH_OK;
 }
 
 static bool valid_tuning(const lulesh_tuning* t) {
   auto elem_ok = [](int b) { return b == 64 || b == 128 || b == 256; };
   return t && elem_ok(t->force_block) && elem_ok(t->kin_block) && elem_ok(t->mat_block) &&
-         (t->node_block == 128 || t->node_block == 256 || t->node_block == 512);
+         (t->node_block == 128 || t->node_block == 256 || t->node_block == 512) &&
+         (t->geometry == 0 || t->geometry == 1);
 }
 
 int lulesh_ens_set_tuning(lulesh_ensemble* s, const lulesh_tuning* t) {
@@ -480,6 +483,8 @@ int lulesh_ens_set_tuning(lulesh_ensemble* s, const lulesh_tuning* t) {
   s->tuning.node = t->node_block;
   s->tuning.kin = t->kin_block;
   s->tuning.mat = t->mat_block;
+  if (s->tuning.geo != t->geometry) s->geo_valid = false;
+  s->tuning.geo = t->geometry;
   drop_graph(s);
   return LULESH_OK;
 }

@@ -32,6 +32,10 @@ struct lulesh_domain {
   bool geo_valid = false;
   // host copies of what only the host uses
   std::vector<int> symmX, symmY, symmZ;
+  // a block mesh (lulesh_create_blocks): blocks per edge, packed -> whole-mesh
+  // element and node ids, and the corner slot each ghost corner copies
+  int blocks_per_edge = 1;
+  std::vector<int> elemGlobal, nodeGlobal, haloCornerSrc;
   std::vector<int64_t> regNumList, regElemlist, regCSR, regReps, regSorted, regElemSize;
   // timing: a ring of cycles x (kNumKernels+1) events, read back when full
   // or when the caller asks, so timed runs never stall per cycle

@@ -126,9 +126,16 @@ constexpr int kGeoSlots = 51;
 
 // Pointers of one problem's device fields. Element arrays have E entries,
 // node arrays N; corner arrays 8E in corner-major order (c*E + e).
+// A block-partitioned mesh adds ghost slots: the delv arrays hold Eg >= E
+// entries, the corner-force arrays nCornerSlot >= 8E and the corner list
+// nCornerList >= 8E; haloDelvSrc / haloCornerSrc give the element or
+// corner-force slot each ghost slot copies before the kernel that reads it.
 struct DevDomain {
   int E, N, nx;
   int mode;
+  int Eg, nCornerSlot, nCornerList;
+  const int* haloDelvSrc;    // Eg - E entries (null without ghosts)
+  const int* haloCornerSrc;  // nCornerSlot - 8E entries (null without ghosts)
   // nodes
   double *x, *y, *z, *xd, *yd, *zd;
   double *nodalMass, *inv_nodalMass;

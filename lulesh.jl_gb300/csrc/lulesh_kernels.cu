@@ -215,6 +215,23 @@ __device__ __forceinline__ void tape_diagonals(double* diag, int E, int e, const
     for (int k = 0; k < 3; ++k) diag[(3 * q + k) * E + e] = g[q][k];
 }
 
+// The force kernel's geometry of one element's positions, formed by the same
+// calls in the same order as k_geometry and k_kinematics, so the values are
+// bitwise those they store.
+__device__ __forceinline__ void force_geometry(const double x[8], const double y[8], const double z[8],
+                                               double gr[3][8], double hm[3][4], double B[3][4], double& pz01,
+                                               double& ny4, double& det) {
+  double g[12][3], w[3][3], n[6][3], U[3][3], gU[3][3], gV[3][3], gW[3][3];
+  face_diagonals(x, y, z, g);
+  position_walsh(x, y, z, g, w, hm);
+#pragma unroll
+  for (int f = 0; f < 5; ++f) face_normal(g, f, n[f]);
+  node_normals(n, B, pz01, ny4);
+  volume_terms(g, U, gU, gV, gW);
+  volume_derivatives(gU, gV, gW, gr);
+  det = jacobian_det(w);
+}
+
 // The stored geometry of the current positions (see above): at the start of
 // a run, after the host changed the positions, and for the ensemble's reset;
 // in a taped run also the first cycle's face diagonals and normals.
@@ -245,10 +262,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_geometry(DevDomain d) {
 // ---------------------------------------------------------------------------
 // k_force
 // ---------------------------------------------------------------------------
-// Every variant loads the geometry of the cycle's positions from d.nextGeo;
-// the taping variant adds the volume derivatives, scaled modes and mode
-// sums to the force tape (the diagonals and normals are there already).
-template <int MODE, bool ENS, bool TAPE>
+// The geometry of the cycle's positions is loaded from d.nextGeo, or, with
+// GEO_INLINE (the other fusion split, chosen by the autotuner), formed here
+// from the positions (k_kinematics then stores none); the taping variant
+// loads it and adds the volume derivatives, scaled modes and mode sums to
+// the force tape (the diagonals and normals are there already).
+template <int MODE, bool ENS, bool TAPE, bool GEO_INLINE>
 __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -263,7 +282,12 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_force(DevDomain d, Params prm
   for (int c = 0; c < 8; ++c) nd[c] = LULESH_IDX(LDG(&d.nodelist[c * E + e]), d.N, st);
 
   double gr[3][8], hm[3][4], B[3][4], pz01, ny4, det;
-  {
+  if (GEO_INLINE) {
+    double x[8], y[8], z[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) { x[c] = LDG(&d.x[nd[c]]); y[c] = LDG(&d.y[nd[c]]); z[c] = LDG(&d.z[nd[c]]); }
+    force_geometry(x, y, z, gr, hm, B, pz01, ny4, det);
+  } else {
     const double* geo = d.nextGeo;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
@@ -397,15 +421,15 @@ __global__ void __launch_bounds__(kMaxNodeBlock) k_node(DevDomain d, Params prm)
   const int s = LDG(&d.nodeElemStart[i]);
   int t = LDG(&d.nodeElemStart[i + 1]);
 #ifdef LULESH_CHECK
-  // the node's corner range must lie within [0, 8E]; an empty one reads nothing
-  if (s < 0 || t < s || t > 8 * d.E) { atomicOr(&st->status, ST_INDEX); t = s; }
+  // the node's corner range must lie within the corner list; an empty one reads nothing
+  if (s < 0 || t < s || t > d.nCornerList) { atomicOr(&st->status, ST_INDEX); t = s; }
 #endif
   double fx = 0.0, fy = 0.0, fz = 0.0;
   if (s < t) {
-    const int c0 = LULESH_IDX(LDG(&d.cornerList[s]), 8 * d.E, st);
+    const int c0 = LULESH_IDX(LDG(&d.cornerList[s]), d.nCornerSlot, st);
     fx = LDG(&d.fcx[c0]); fy = LDG(&d.fcy[c0]); fz = LDG(&d.fcz[c0]);
     for (int j = s + 1; j < t; ++j) {
-      const int c = LULESH_IDX(LDG(&d.cornerList[j]), 8 * d.E, st);
+      const int c = LULESH_IDX(LDG(&d.cornerList[j]), d.nCornerSlot, st);
       fx += LDG(&d.fcx[c]); fy += LDG(&d.fcy[c]); fz += LDG(&d.fcz[c]);
     }
   }
@@ -434,7 +458,9 @@ __global__ void __launch_bounds__(kMaxNodeBlock) k_node(DevDomain d, Params prm)
 // ---------------------------------------------------------------------------
 // k_kinematics
 // ---------------------------------------------------------------------------
-template <bool AUX, bool ENS, bool TAPE>
+// GEO: also store the next force kernel's geometry of these positions
+// (d.nextGeo); without it (the GEO_INLINE split) k_force forms it itself.
+template <bool AUX, bool ENS, bool TAPE, bool GEO>
 __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Params prm) {
   const int E = d.E;
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
@@ -509,12 +535,14 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_kinematics(DevDomain d, Param
       // the next cycle's face normals, for its hourglass transpose
       if (d.tapeGeoNext) tape_force_normals(d.tapeGeoNext, E, e, n);
     }
-    {
+    if (GEO) {
       double B[3][4], pz01, ny4, gr[3][8];
       node_normals(n, B, pz01, ny4);
       volume_derivatives(gU, gV, gW, gr);
       eta_cofactors(w, cet);
       store_geometry(d.nextGeo, E, e, gr, hm, B, pz01, ny4, jacobian_det(w, cet));
+    } else {
+      eta_cofactors(w, cet);
     }
   }
   const double* wx = w[0];
@@ -763,18 +791,19 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
     int src0, src1, src2;
     // xi-plus: the reference indexes delv_xi[lxip[i]] without +1 (:2349)
     const int ixp = (MODE & 4) ? LDG(&d.lxip[i]) : LDG(&d.lxip[i]) - 1;
-    double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, E, bad);
-    double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, E, bad);
+    const int Eg = d.Eg;  // neighbour reads may reach the ghost slots of a block-partitioned mesh
+    double dm = monoq_neighbour(d.delv_xi, mask, XI_M, XI_M_SYMM, XI_M_FREE, XI_M_COMM, LDG(&d.lxim[i]), i, Eg, bad);
+    double dp = monoq_neighbour(d.delv_xi, mask, XI_P, XI_P_SYMM, XI_P_FREE, XI_P_COMM, ixp, i, Eg, bad);
     double tl[9];  // limiter terms per direction: norm, dm/norm, dp/norm (TAPE)
     // the three 1/(delv + ptiny) from one division
     double inx, iny, inz;
     recip3(dvxi + 1.e-36, dveta + 1.e-36, dvzeta + 1.e-36, inx, iny, inz);
     const double phixi = monoq_phi(inx, dm, dp, prm, src0, tl[0], tl[3], tl[6]);
-    dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, E, bad);
-    dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, E, bad);
+    dm = monoq_neighbour(d.delv_eta, mask, ETA_M, ETA_M_SYMM, ETA_M_FREE, ETA_M_COMM, LDG(&d.letam[i]), i, Eg, bad);
+    dp = monoq_neighbour(d.delv_eta, mask, ETA_P, ETA_P_SYMM, ETA_P_FREE, ETA_P_COMM, LDG(&d.letap[i]), i, Eg, bad);
     const double phieta = monoq_phi(iny, dm, dp, prm, src1, tl[1], tl[4], tl[7]);
-    dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, E, bad);
-    dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, E, bad);
+    dm = monoq_neighbour(d.delv_zeta, mask, ZETA_M, ZETA_M_SYMM, ZETA_M_FREE, ZETA_M_COMM, LDG(&d.lzetam[i]), i, Eg, bad);
+    dp = monoq_neighbour(d.delv_zeta, mask, ZETA_P, ZETA_P_SYMM, ZETA_P_FREE, ZETA_P_COMM, LDG(&d.lzetap[i]), i, Eg, bad);
     const double phizeta = monoq_phi(inz, dm, dp, prm, src2, tl[2], tl[5], tl[8]);
     if (bad) err |= ST_BAD_BC;
     // d.tapeMat slot q of this element (TAPE only)
@@ -986,6 +1015,32 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
 }
 
 // ---------------------------------------------------------------------------
+// Halo copies of a block-partitioned mesh (the single-GPU form of commSBN and
+// commMonoQ, src/comm.jl:776, 1127): each ghost slot takes the value of the
+// corner force or element its owning block computed.
+// ---------------------------------------------------------------------------
+__global__ void k_halo_corners(DevDomain d) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  const int base = 8 * d.E;
+  if (g >= d.nCornerSlot - base) return;
+  if (step_off(d.st)) return;
+  const int s = LULESH_IDX(LDG(&d.haloCornerSrc[g]), base, d.st);
+  d.fcx[base + g] = d.fcx[s];
+  d.fcy[base + g] = d.fcy[s];
+  d.fcz[base + g] = d.fcz[s];
+}
+
+__global__ void k_halo_delv(DevDomain d) {
+  const int g = blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= d.Eg - d.E) return;
+  if (step_off(d.st)) return;
+  const int s = LULESH_IDX(LDG(&d.haloDelvSrc[g]), d.E, d.st);
+  d.delv_xi[d.E + g] = d.delv_xi[s];
+  d.delv_eta[d.E + g] = d.delv_eta[s];
+  d.delv_zeta[d.E + g] = d.delv_zeta[s];
+}
+
+// ---------------------------------------------------------------------------
 // k_time_increment (device run loop): one thread per problem
 // ---------------------------------------------------------------------------
 __device__ void advance_time(DevState* st, const Params& prm) {
@@ -1026,10 +1081,13 @@ void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaSt
   const int bs = t.force;
   const int grid = (d.E + bs - 1) / bs;
   const bool ens = d.elemInst != nullptr;
-#define LULESH_FORCE(M)                                                      \
-  (ens ? k_force<M, true, false><<<grid, bs, 0, s>>>(d, prm)                  \
-       : d.tapeGeo ? k_force<M, false, true><<<grid, bs, 0, s>>>(d, prm)      \
-                   : k_force<M, false, false><<<grid, bs, 0, s>>>(d, prm))
+  const bool inl = t.geo != 0 && !d.tapeGeo;  // the taping kernels always use the stored geometry
+#define LULESH_FORCE(M)                                                                            \
+  (ens ? (inl ? k_force<M, true, false, true><<<grid, bs, 0, s>>>(d, prm)                          \
+              : k_force<M, true, false, false><<<grid, bs, 0, s>>>(d, prm))                        \
+       : d.tapeGeo ? k_force<M, false, true, false><<<grid, bs, 0, s>>>(d, prm)                    \
+                   : (inl ? k_force<M, false, false, true><<<grid, bs, 0, s>>>(d, prm)              \
+                          : k_force<M, false, false, false><<<grid, bs, 0, s>>>(d, prm)))
   switch (d.mode & 3) {
     case 0: LULESH_FORCE(0); break;
     case 1: LULESH_FORCE(1); break;
@@ -1040,6 +1098,10 @@ void launch_force(const DevDomain& d, const Params& prm, const Tuning& t, cudaSt
 }
 
 void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
+  if (d.haloCornerSrc) {
+    const int n = d.nCornerSlot - 8 * d.E;
+    k_halo_corners<<<(n + 255) / 256, 256, 0, s>>>(d);
+  }
   const int bs = t.node;
   const int grid = (d.N + bs - 1) / bs;
   if (d.nodeInst) k_node<false, true><<<grid, bs, 0, s>>>(d, prm);
@@ -1050,13 +1112,26 @@ void launch_node(const DevDomain& d, const Params& prm, bool aux, const Tuning& 
 void launch_kinematics(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
   const int bs = t.kin;
   const int grid = (d.E + bs - 1) / bs;
-  if (d.elemInst) k_kinematics<false, true, false><<<grid, bs, 0, s>>>(d, prm);
-  else if (d.tapeFlags) k_kinematics<false, false, true><<<grid, bs, 0, s>>>(d, prm);
-  else if (aux) k_kinematics<true, false, false><<<grid, bs, 0, s>>>(d, prm);
-  else k_kinematics<false, false, false><<<grid, bs, 0, s>>>(d, prm);
+  const bool geo = t.geo == 0;
+  if (d.elemInst) {
+    if (geo) k_kinematics<false, true, false, true><<<grid, bs, 0, s>>>(d, prm);
+    else k_kinematics<false, true, false, false><<<grid, bs, 0, s>>>(d, prm);
+  } else if (d.tapeFlags) {
+    k_kinematics<false, false, true, true><<<grid, bs, 0, s>>>(d, prm);
+  } else if (aux) {
+    if (geo) k_kinematics<true, false, false, true><<<grid, bs, 0, s>>>(d, prm);
+    else k_kinematics<true, false, false, false><<<grid, bs, 0, s>>>(d, prm);
+  } else {
+    if (geo) k_kinematics<false, false, false, true><<<grid, bs, 0, s>>>(d, prm);
+    else k_kinematics<false, false, false, false><<<grid, bs, 0, s>>>(d, prm);
+  }
 }
 
 void launch_material(const DevDomain& d, const Params& prm, bool aux, const Tuning& t, cudaStream_t s) {
+  if (d.haloDelvSrc) {
+    const int n = d.Eg - d.E;
+    k_halo_delv<<<(n + 255) / 256, 256, 0, s>>>(d);
+  }
   const int bs = t.mat;
   const int grid = (d.E + bs - 1) / bs;
   const bool fix = (d.mode & 4) != 0;

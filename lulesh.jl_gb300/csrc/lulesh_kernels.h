@@ -14,12 +14,17 @@ constexpr int kMaxElemBlock = 256;
 constexpr int kMaxNodeBlock = 512;
 
 // Launch configuration chosen by the autotuner (defaults are the block sizes
-// that measured best for the 150^3 problem).
+// that measured best for the 150^3 problem). `geo` is the fusion split of the
+// force geometry: 0 formed by k_kinematics of the cycle before and stored in
+// DevDomain::nextGeo (fewer FP64 instructions, 816 more bytes per element
+// and cycle), 1 formed inside k_force from the positions. Both give bitwise
+// the same results. The taping kernels of the adjoint always use 0.
 struct Tuning {
   int force = 128;
   int node = 256;
   int kin = 128;
   int mat = 128;
+  int geo = 0;
 };
 
 // k_geometry: the force kernel's geometry of the current positions (needed

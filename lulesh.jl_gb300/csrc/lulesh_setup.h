@@ -19,6 +19,15 @@ struct HostMesh {
   std::vector<int> cornerList;               // 8E, values c*E + e
   std::vector<int64_t> regNumList, regElemlist, regCSR, regReps, regSorted, regElemSize;
   double einit = 0.0, deltatime = 0.0;
+  // A block-partitioned mesh (build_block_mesh) packs tp^3 blocks; its
+  // limiter reads and node gathers that cross a block face go through ghost
+  // slots filled by halo copies. Zero sizes mean a single block (Eg = E,
+  // corner slots = corner list entries = 8E).
+  int blocks_per_edge = 1;
+  int64_t Eg = 0, nCornerSlot = 0, nCornerList = 0;
+  std::vector<int> haloDelvSrc, haloDelvDst;      // per ghost delv slot: source element, receiving block
+  std::vector<int> haloCornerSrc, haloCornerDst;  // per ghost corner slot: source slot c*E + e, receiving block
+  std::vector<int> elemGlobal, nodeGlobal;        // packed -> global element / node of the whole mesh
 };
 
 // Builds the nx^3 single-rank Sedov mesh exactly as Domain(prob) does. A
@@ -28,5 +37,19 @@ void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t see
 
 // createRegionIndexSets! (results-neutral region layout).
 void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed);
+
+// The reference's multi-rank decomposition (initMeshDecomp, src/LULESH.jl:62-97:
+// tp^3 ranks, rank r the block col = r % tp, row = (r / tp) % tp,
+// plane = r / tp^2 of edge nx) of the (tp*nx)^3 mesh `g` (built by
+// build_mesh), packed block after block into `m`: each block's elements and
+// (nx+1)^3 nodes in the reference's per-rank order, nodes on block faces
+// duplicated in every block that touches them, COMM masks on block faces
+// (src/domain.jl:822-916). Values come from `g`, so the blocks hold the whole
+// mesh's bits. The limiter's neighbour reads and each node's corner gather
+// keep the whole mesh's order; where they cross a block face they read ghost
+// slots that the halo copies fill from the neighbouring block (the reads of
+// commMonoQ and commSBN, src/comm.jl:1127, 776). `mode` selects the xi-plus
+// read of the limiter (the reference's defect unless bit 4 is set).
+void build_block_mesh(HostMesh& m, const HostMesh& g, int nx, int tp, int mode);
 
 }  // namespace lulesh

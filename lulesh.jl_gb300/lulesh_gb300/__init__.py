@@ -21,7 +21,7 @@ __all__ = [
     "LuleshProblem", "Domain", "timeIncrement", "lagrangeLeapFrog", "run",
     "verifyAndWriteFinalOutput", "LuleshError", "load_library", "library_path",
     "FIELDS", "SCALARS", "MODE_FAITHFUL", "MODE_LULESH2", "Ensemble", "sedov_instances",
-    "Adjoint", "STATE_FIELDS", "partition", "shard", "read_state",
+    "Adjoint", "STATE_FIELDS", "partition", "shard", "read_state", "block_plan",
 ]
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
@@ -100,9 +100,11 @@ class Instance(ctypes.Structure):
 
 
 class Tuning(ctypes.Structure):
-    """lulesh_tuning: threads per block of the four step kernels."""
+    """lulesh_tuning: threads per block of the four step kernels and the
+    geometry split (0 stored by k_kinematics, 1 formed in k_force)."""
     _fields_ = [("force_block", ctypes.c_int32), ("node_block", ctypes.c_int32),
-                ("kin_block", ctypes.c_int32), ("mat_block", ctypes.c_int32)]
+                ("kin_block", ctypes.c_int32), ("mat_block", ctypes.c_int32),
+                ("geometry", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -198,6 +200,10 @@ def load_library():
         "lulesh_adj_gradient": (ctypes.c_int, [P, i64, ctypes.POINTER(AdjResult)]),
         "lulesh_adj_get_gradient": (ctypes.c_int, [P, i32, P, i64]),
         "lulesh_adj_set_overlap": (ctypes.c_int, [P, i32]),
+        "lulesh_create_blocks": (ctypes.c_int, [ctypes.POINTER(_Params), i32, ctypes.POINTER(P)]),
+        "lulesh_block_map": (ctypes.c_int, [P, ctypes.POINTER(i32), P, P]),
+        "lulesh_block_plan_sizes": (ctypes.c_int, [i32, i32, i32, ctypes.POINTER(i64)]),
+        "lulesh_block_plan": (ctypes.c_int, [i32, i32, i32, P, P, P, P, P, P]),
     }
     for name, (res, args) in sig.items():
         fn = getattr(L, name)
@@ -221,7 +227,8 @@ class LuleshProblem:
     """
 
     def __init__(self, num_iters=10, structured=True, nx=45, nr=11, balance=1, cost=1,
-                 mode=MODE_FAITHFUL, region_reps=False, keep_aux=False, device=0, region_seed=0):
+                 mode=MODE_FAITHFUL, region_reps=False, keep_aux=False, device=0, region_seed=0,
+                 blocks_per_edge=1):
         if not structured:
             raise LuleshError("Reading unstructured mesh is currently missing in the Julia version of LULESH.")
         self.num_iters = int(num_iters)
@@ -235,9 +242,12 @@ class LuleshProblem:
         self.keep_aux = bool(keep_aux)
         self.device = int(device)
         self.region_seed = int(region_seed)
-        # single rank: col = row = plane = 0, side = 1 (initMeshDecomp at one rank)
+        # single rank: col = row = plane = 0, side = 1 (initMeshDecomp at one rank);
+        # blocks_per_edge = tp > 1 builds the tp^3-rank decomposition of the
+        # (tp*nx)^3 mesh as blocks of one handle (lulesh_create_blocks)
         self.col = self.row = self.plane = 0
         self.side = 1
+        self.blocks_per_edge = int(blocks_per_edge)
 
 
 class Domain:
@@ -256,7 +266,11 @@ class Domain:
         p.region_reps, p.keep_aux, p.device = int(prob.region_reps), int(prob.keep_aux), prob.device
         p.region_seed = prob.region_seed
         h = ctypes.c_void_p()
-        _check(L.lulesh_create(ctypes.byref(p), ctypes.byref(h)), "Domain(prob)")
+        tp = getattr(prob, "blocks_per_edge", 1)
+        if tp > 1:
+            _check(L.lulesh_create_blocks(ctypes.byref(p), tp, ctypes.byref(h)), "Domain(prob) in blocks")
+        else:
+            _check(L.lulesh_create(ctypes.byref(p), ctypes.byref(h)), "Domain(prob)")
         object.__setattr__(self, "_h", h)
         object.__setattr__(self, "_L", L)
         object.__setattr__(self, "prob", prob)
@@ -269,6 +283,26 @@ class Domain:
     @property
     def handle(self):
         return self._h
+
+    def block_map(self):
+        """(blocks per edge, whole-mesh element id of every packed element,
+        whole-mesh node id of every packed node)."""
+        tp = ctypes.c_int32()
+        eg = np.empty(self.numElem, dtype=np.int32)
+        ng = np.empty(self.numNode, dtype=np.int32)
+        _check(self._L.lulesh_block_map(self._h, ctypes.byref(tp), eg.ctypes.data_as(ctypes.c_void_p),
+                                        ng.ctypes.data_as(ctypes.c_void_p)), "block map")
+        return tp.value, eg, ng
+
+    def global_field(self, name):
+        """A state or step field of a block mesh in the whole mesh's order
+        (a node on a block face takes its first block's copy)."""
+        _, eg, ng = self.block_map()
+        v = self.field(name)
+        ids = eg if v.size == self.numElem else ng
+        out = np.empty(int(ids.max()) + 1, dtype=v.dtype)
+        out[ids[::-1]] = v[::-1]  # the first copy wins
+        return out
 
     def close(self):
         if self._h:
@@ -426,6 +460,26 @@ def verifyAndWriteFinalOutput(elapsed_time, domain, nx, numRanks=1, file=None):
     print(f"FOM                  = {1000.0 / grind2:.8f} (z/s)\n", file=f)
     return {"origin_energy": e0, "MaxAbsDiff": maxabs, "TotalAbsDiff": total, "MaxRelDiff": maxrel,
             "cycle": cyc, "grind_us": grind2, "fom_kzs": 1000.0 / grind2}
+
+
+def block_plan(nx, blocks_per_edge, mode=MODE_FAITHFUL):
+    """The tp^3 decomposition of the (tp*nx)^3 mesh and its halo plan,
+    computed on the host (no GPU): packed -> whole-mesh element and node ids,
+    and per ghost slot the packed element (delv) or corner-force slot
+    c*E + e (corners) it copies and the block that holds the slot."""
+    L = load_library()
+    sizes = (ctypes.c_int64 * 5)()
+    _check(L.lulesh_block_plan_sizes(int(nx), int(blocks_per_edge), int(mode), sizes), "block plan sizes")
+    E, N, gd, gc, ncl = (int(v) for v in sizes)
+    out = {"E": E, "N": N, "corner_list_entries": ncl,
+           "elem_global": np.empty(E, np.int32), "node_global": np.empty(N, np.int32),
+           "halo_delv_src": np.empty(gd, np.int32), "halo_delv_dst": np.empty(gd, np.int32),
+           "halo_corner_src": np.empty(gc, np.int32), "halo_corner_dst": np.empty(gc, np.int32)}
+    ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)
+    _check(L.lulesh_block_plan(int(nx), int(blocks_per_edge), int(mode), ptr(out["elem_global"]),
+                               ptr(out["node_global"]), ptr(out["halo_delv_src"]), ptr(out["halo_delv_dst"]),
+                               ptr(out["halo_corner_src"]), ptr(out["halo_corner_dst"])), "block plan")
+    return out
 
 
 def sedov_instances(seed=0xC4, n=256, nx_min=16, nx_max=64):

@@ -1,0 +1,92 @@
+"""The multi-rank decomposition as blocks of one mesh on one GPU
+(lulesh_create_blocks): tp^3 blocks of nx^3 elements with halo copies
+across the block faces give bitwise the single-block run of the whole
+(tp*nx)^3 mesh, in the reference's faithful mode and with its defects
+corrected, through the device run loop and the per-step calls."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+STATE = ["e", "p", "q", "v", "ss", "x", "y", "z", "xd", "yd", "zd"]
+STEP = ["vdov", "arealg", "delv", "vnew", "delv_xi", "delv_eta", "delv_zeta", "delx_xi", "delx_eta", "delx_zeta"]
+NODE = {"x", "y", "z", "xd", "yd", "zd", "fx", "fy", "fz", "xdd", "ydd", "zdd", "nodalMass"}
+
+
+def pair(L, nx, tp, mode, keep_aux=False):
+    whole = L.Domain(L.LuleshProblem(nx=nx * tp, mode=mode, keep_aux=keep_aux))
+    blocks = L.Domain(L.LuleshProblem(nx=nx, mode=mode, keep_aux=keep_aux, blocks_per_edge=tp))
+    return whole, blocks
+
+
+def assert_same(whole, blocks, names):
+    _, eg, ng = blocks.block_map()
+    for f in names:
+        a, v = whole.field(f), blocks.field(f)
+        ids = ng if f in NODE else eg
+        # every packed copy holds the whole mesh's bits (shared nodes included)
+        assert np.array_equal(v.view(np.uint64), a[ids].view(np.uint64)), f
+    for s in ["time", "deltatime", "dtcourant", "dthydro", "cycle"]:
+        assert getattr(whole, s) == getattr(blocks, s), s
+
+
+@pytest.mark.parametrize("nx,tp,mode", [(6, 2, 0), (6, 2, 7), (4, 3, 0), (4, 3, 1), (5, 3, 4)])
+def test_blocks_run_is_the_single_block_run(gpu_lib, nx, tp, mode):
+    L = gpu_lib
+    whole, blocks = pair(L, nx, tp, mode)
+    assert blocks.numElem == whole.numElem and blocks.numNode == tp ** 3 * (nx + 1) ** 3
+    # the setup: masses, volumes, positions of every copy
+    assert_same(whole, blocks, ["x", "y", "z", "nodalMass", "volo", "elemMass", "e"])
+    sw, sb = L.run(whole, 80), L.run(blocks, 80)
+    assert sw["cycle"] == sb["cycle"] == 80
+    assert_same(whole, blocks, STATE + STEP)
+
+
+@pytest.mark.parametrize("mode", [0, 7])
+def test_blocks_stepwise_with_aux_fields(gpu_lib, mode):
+    """The per-step calls (timeIncrement!, lagrangeLeapFrog) with the kept
+    auxiliary fields, from a developed state."""
+    L = gpu_lib
+    whole, blocks = pair(L, 4, 2, mode, keep_aux=True)
+    L.run(whole, 40)
+    L.run(blocks, 40)
+    for _ in range(5):
+        L.timeIncrement(whole)
+        L.lagrangeLeapFrog(whole)
+        L.timeIncrement(blocks)
+        L.lagrangeLeapFrog(blocks)
+    assert_same(whole, blocks, STATE + STEP + ["fx", "fy", "fz", "xdd", "ydd", "zdd", "dxx", "dyy", "dzz", "ql", "qq"])
+
+
+def test_blocks_run_to_stoptime(gpu_lib):
+    L = gpu_lib
+    whole, blocks = pair(L, 5, 2, L.MODE_LULESH2)
+    sw, sb = L.run(whole, 10 ** 9), L.run(blocks, 10 ** 9)
+    assert sw["time"] == sb["time"] == 1e-2 and sw["cycle"] == sb["cycle"]
+    assert_same(whole, blocks, STATE)
+    # the reference's rank-0 report: origin energy and plane-0 symmetry of block 0
+    e0 = L.verify(blocks)[0]
+    assert e0 == whole.field("e")[0]
+
+
+def test_blocks_with_the_inline_geometry_split(gpu_lib):
+    L = gpu_lib
+    whole, blocks = pair(L, 4, 2, 0)
+    blocks.set_tuning(geometry=1)
+    L.run(whole, 50)
+    L.run(blocks, 50)
+    assert_same(whole, blocks, STATE)
+
+
+def test_blocks_errors_and_limits(gpu_lib):
+    L = gpu_lib
+    _, blocks = pair(L, 3, 2, 0)
+    with pytest.raises(L.LuleshError):
+        L.Adjoint(blocks)  # the adjoint kernels have no halo transposes
+    with pytest.raises(L.LuleshError):
+        L.Domain(L.LuleshProblem(nx=3, blocks_per_edge=2, region_reps=True))
+    # an error in one block stops every block: a QStop provoked on the host
+    L.run(blocks, 10)
+    blocks.qstop = 1e-30
+    with pytest.raises(L.LuleshError, match="QStopError"):
+        L.run(blocks, 20)

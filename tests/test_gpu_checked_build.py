@@ -4,7 +4,8 @@ range and records LULESH_ERR_INDEX instead of reading outside its array.
 
 Small cases run under it in a separate process (the library is loaded once
 per process): single problems of nx = 1, 2, 3, 5, 8 in the faithful and the
-corrected mode, a region-cost-model run and a three-instance ensemble. None
+corrected mode, a region-cost-model run, a three-instance ensemble and a
+27-block mesh (the halo copies and ghost slots checked too). None
 may report an index error, and every state field must agree with the
 normal build's run of the same case (relative 1e-10 with the parity floors:
 the checks do not change the arithmetic).
@@ -51,6 +52,12 @@ def cases():
     for i in range(len(ENSEMBLE)):
         for f in STATE:
             out[f"e{i}_{f}"] = ens.field(i, f)
+    for mode in (0, 7):
+        g = L.Domain(L.LuleshProblem(nx=3, mode=mode, blocks_per_edge=3))
+        L.run(g, 30)
+        for f in STATE:
+            out[f"b{mode}_{f}"] = g.field(f)
+        g.close()
     return out
 '''
 
