@@ -87,13 +87,19 @@ Base.showerror(io::IO, e::LuleshGPUError) = print(io, e.msg)
 mutable struct GPUDomain
     handle::Ptr{Cvoid}
     nx::Int
-    function GPUDomain(prob::LuleshProblem; mode::Integer=0, device::Integer=0, keep_aux::Bool=false)
+    # blocks_per_edge = tp > 1: the tp^3-rank decomposition of the (tp*nx)^3
+    # mesh as blocks of one GPU handle (lulesh_create_blocks)
+    function GPUDomain(prob::LuleshProblem; mode::Integer=0, device::Integer=0, keep_aux::Bool=false,
+                       blocks_per_edge::Integer=1)
         prob.structured || error("Reading unstructured mesh is currently missing in the Julia version of LULESH.")
         p = Ref{Params}()
         ccall((:lulesh_default_params, libpath), Cvoid, (Ptr{Params}, Int32), p, prob.nx)
         p[] = Params(prob.nx, prob.nr, prob.balance, prob.cost, mode, 0, keep_aux, device, 0)
         h = Ref{Ptr{Cvoid}}(C_NULL)
-        rc = ccall((:lulesh_create, libpath), Cint, (Ptr{Params}, Ptr{Ptr{Cvoid}}), p, h)
+        rc = blocks_per_edge > 1 ?
+            ccall((:lulesh_create_blocks, libpath), Cint, (Ptr{Params}, Int32, Ptr{Ptr{Cvoid}}), p,
+                  Int32(blocks_per_edge), h) :
+            ccall((:lulesh_create, libpath), Cint, (Ptr{Params}, Ptr{Ptr{Cvoid}}), p, h)
         rc == 0 || throw(LuleshGPUError("Domain(prob) failed with status $rc", rc))
         d = new(h[], prob.nx)
         finalizer(d) do x
@@ -148,10 +154,10 @@ function Base.getproperty(d::GPUDomain, s::Symbol)
                    h, id, out, n[])
         rc == 0 || throw(LuleshGPUError("download of $s failed", rc))
         return out
-    elseif s === :numElem
-        return getfield(d, :nx)^3
-    elseif s === :numNode
-        return (getfield(d, :nx) + 1)^3
+    elseif s === :numElem || s === :numNode
+        ne, nn = Ref{Int64}(), Ref{Int64}()
+        ccall((:lulesh_sizes, libpath), Cint, (Ptr{Cvoid}, Ptr{Int64}, Ptr{Int64}), h, ne, nn)
+        return s === :numElem ? Int(ne[]) : Int(nn[])
     elseif s in (:sizeX, :sizeY, :sizeZ)
         # a cube of edge nx on one rank (src/domain.jl:536-543)
         return getfield(d, :nx)
