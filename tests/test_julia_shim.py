@@ -5,7 +5,9 @@ Julia lays out an isbits struct like the C struct with the same fields, so a
 header's field names, order and types. The shim's structs are parsed here and
 their C layout (natural alignment) is compared with the ctypes mirrors, which
 tests/test_abi.py compares with the compiled header. The field and scalar ids
-and the methods examples/benchmark.jl:22-110 needs are checked the same way.
+and the methods examples/benchmark.jl:22-110 needs are checked the same way,
+and every `ccall` of the shim and of the ChainRules rule against the C
+prototype it binds (return type, argument count and types).
 """
 import ctypes
 import os
@@ -131,3 +133,74 @@ def test_shim_serves_the_benchmark_script():
     for p in BENCHMARK_PROPERTIES:
         assert p in served, p
     assert re.search(r"s in \(:sizeX, :sizeY, :sizeZ\)", text)
+
+
+# ---- every ccall against the header's prototype ---------------------------
+CHAINRULES = os.path.join(ROOT, "lulesh.jl_gb300", "julia", "LULESHGB300ChainRules.jl")
+
+# C parameter type -> the Julia types a ccall may declare for it
+C_TO_JULIA = {
+    "int32_t": {"Int32", "Cint"}, "int": {"Cint", "Int32"}, "int64_t": {"Int64"}, "double": {"Float64"},
+    "uint64_t": {"UInt64"}, "double*": {"Ptr{Float64}"}, "const double*": {"Ptr{Float64}"},
+    "int64_t*": {"Ptr{Int64}"}, "int32_t*": {"Ptr{Int32}"}, "const char*": {"Cstring"},
+    "void*": {"Ptr{Cvoid}"}, "const void*": {"Ptr{Cvoid}"},
+    "const lulesh_params*": {"Ptr{Params}"}, "lulesh_params*": {"Ptr{Params}"},
+    "lulesh_scalars*": {"Ptr{Scalars}"}, "lulesh_adj_result*": {"Ptr{AdjResult}"},
+}
+HANDLES = ("lulesh_domain", "lulesh_adjoint", "lulesh_ensemble")
+
+
+def c_prototypes():
+    text = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    out = {}
+    for m in re.finditer(r"^\s*(int|void|const char\*)\s+(lulesh_\w+)\s*\(([^)]*)\)\s*;", text, re.M):
+        args = [a.strip() for a in m.group(3).split(",") if a.strip() and a.strip() != "void"]
+        types = []
+        for a in args:
+            a = re.sub(r"\s+\w+(\[\d*\])?$", lambda k: "*" if k.group(1) is not None else "", a)  # drop the name
+            types.append(re.sub(r"\s*\*", "*", a).strip())
+        out[m.group(2)] = (m.group(1), types)
+    return out
+
+
+def julia_ccalls(text):
+    calls = []
+    for m in re.finditer(r"ccall\(\(:(lulesh_\w+),\s*[\w.]+\),\s*(\w+),\s*\(", text):
+        depth, i = 1, m.end()
+        while depth:
+            depth += {"(": 1, ")": -1}.get(text[i], 0)
+            i += 1
+        tup = text[m.end():i - 1]
+        parts, depth, cur = [], 0, ""
+        for ch in tup:
+            if ch == "," and depth == 0:
+                parts.append(cur.strip())
+                cur = ""
+                continue
+            depth += {"{": 1, "}": -1}.get(ch, 0)
+            cur += ch
+        if cur.strip():
+            parts.append(cur.strip())
+        calls.append((m.group(1), m.group(2), parts))
+    return calls
+
+
+def compatible(ctype, jtype):
+    base = ctype.replace("const ", "")
+    if base.rstrip("*") in HANDLES:
+        return jtype == ("Ptr{Ptr{Cvoid}}" if base.endswith("**") else "Ptr{Cvoid}")
+    return jtype in C_TO_JULIA.get(ctype, set())
+
+
+@pytest.mark.parametrize("path", [SHIM, CHAINRULES])
+def test_every_ccall_matches_its_c_prototype(path):
+    protos = c_prototypes()
+    calls = julia_ccalls(open(path).read())
+    assert calls, path
+    for name, ret, args in calls:
+        assert name in protos, name
+        cret, ctypes_ = protos[name]
+        assert (ret in ("Cint", "Int32")) if cret == "int" else (ret == "Cvoid") if cret == "void" else True, name
+        assert len(args) == len(ctypes_), (name, args, ctypes_)
+        for c, j in zip(ctypes_, args):
+            assert compatible(c, j), (name, c, j)
