@@ -5,10 +5,11 @@
 // connectivity, neighbour and corner indices shifted into the packed space.
 // The step kernels are the single-problem kernels in their ensemble
 // instantiation: each thread reads its element's or node's instance for dt,
-// status and hgcoef, and the dt minima are reduced per instance. A run is a
-// captured CUDA graph of kGraphCycles cycles ([per-instance timeIncrement!,
-// force, node, kinematics, material] each), launched until every instance
-// has stopped; dt never leaves the device.
+// status and hgcoef, and the dt minima are reduced per instance. A run is
+// one launch of a captured CUDA graph of the whole run ([per-instance
+// timeIncrement!, force, node, kinematics, material] per cycle; runs longer
+// than kMaxGraphCycles launch it again until every instance has stopped);
+// dt never leaves the device.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -33,8 +34,8 @@ using namespace lulesh;
 
 namespace {
 
-constexpr int kGraphCycles = 16;
-constexpr int kPollLaunches = 4;
+// a run's graph covers up to this many cycles; a longer run relaunches it
+constexpr int kMaxGraphCycles = 512;
 
 int cuda_rc(cudaError_t e) {
   if (e == cudaSuccess) return LULESH_OK;
@@ -342,24 +343,25 @@ int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
     launch_geometry(s->dd, st);
     s->geo_valid = true;
   }
-  // the run limit lives in the device state, so one graph serves every call
-  if (!s->graph) {
+  // one graph of the whole run (up to kMaxGraphCycles cycles), kept for the
+  // next run of the same length; the run limit lives in the device state and
+  // cycles past an instance's stop are no-ops for it
+  const int64_t glen = std::min<int64_t>(budget, kMaxGraphCycles);
+  if (!s->graph || s->graph_key != glen) {
     drop_graph(s);
     cudaGraph_t g;
     ECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
-    for (int c = 0; c < kGraphCycles; ++c) launch_cycle(s);
+    for (int64_t c = 0; c < glen; ++c) launch_cycle(s);
     ECK(cudaStreamEndCapture(st, &g));
     cudaError_t e = cudaGraphInstantiate(&s->graph, g, 0);
     cudaGraphDestroy(g);
     ECK(e);
-    s->graph_key = 0;
+    s->graph_key = glen;
   }
   int64_t launched = 0;
   for (;;) {
-    for (int k = 0; k < kPollLaunches && launched < budget; ++k) {
-      ECK(cudaGraphLaunch(s->graph, st));
-      launched += kGraphCycles;
-    }
+    ECK(cudaGraphLaunch(s->graph, st));
+    launched += glen;
     ECK(cudaMemcpyAsync(s->hst, s->dd.st, sizeof(DevState) * s->n, cudaMemcpyDeviceToHost, st));
     ECK(cudaStreamSynchronize(st));
     bool all_done = true;
