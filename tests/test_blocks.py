@@ -150,3 +150,20 @@ def test_halo_exchange_over_gloo_ranks(gpu_lib, world):
         assert p.exitcode == 0
     assert all(ok_d and ok_c for _, _, ok_d, ok_c in counts)
     assert sum(d for d, _, _, _ in counts) == nd and sum(c for _, c, _, _ in counts) == nc
+
+
+def test_block_plan_edges_and_limits(gpu_lib):
+    import ctypes
+    L = gpu_lib.load_library()
+    # one block: the whole mesh, no ghost slots
+    p = gpu_lib.block_plan(4, 1, 0)
+    assert p["E"] == 64 and p["N"] == 125
+    assert p["halo_delv_src"].size == 0 and p["halo_corner_src"].size == 0
+    assert np.array_equal(p["elem_global"], np.arange(64)) and np.array_equal(p["node_global"], np.arange(125))
+    assert p["corner_list_entries"] == 8 * 64
+    # rejected before any work: empty blocks, a bad mode, a mesh past the index limit
+    sizes = (ctypes.c_int64 * 5)()
+    assert L.lulesh_block_plan_sizes(0, 2, 0, sizes) == 6
+    assert L.lulesh_block_plan_sizes(3, 0, 0, sizes) == 6
+    assert L.lulesh_block_plan_sizes(3, 2, 9, sizes) == 6
+    assert L.lulesh_block_plan_sizes(301, 2, 0, sizes) == 6

@@ -90,3 +90,32 @@ def test_blocks_errors_and_limits(gpu_lib):
     blocks.qstop = 1e-30
     with pytest.raises(L.LuleshError, match="QStopError"):
         L.run(blocks, 20)
+
+
+def test_one_block_is_the_plain_domain(gpu_lib):
+    L = gpu_lib
+    a = L.Domain(L.LuleshProblem(nx=7))
+    b = L.Domain(L.LuleshProblem(nx=7, blocks_per_edge=1))
+    L.run(a, 40)
+    L.run(b, 40)
+    for f in STATE + ["vdov", "arealg"]:
+        assert np.array_equal(a.field(f), b.field(f)), f
+
+
+def test_blocks_state_file_resumes_bitwise(gpu_lib, tmp_path):
+    L = gpu_lib
+    _, blocks = pair(L, 4, 2, 0)
+    L.run(blocks, 20)
+    path = str(tmp_path / "blocks.state")
+    blocks.save_state(path)
+    L.run(blocks, 45)
+    after = {f: blocks.field(f) for f in STATE}
+    blocks.load_state(path)
+    assert blocks.cycle == 20
+    L.run(blocks, 45)
+    for f in STATE:
+        assert np.array_equal(blocks.field(f), after[f]), f
+    # a single-block handle of the block edge does not take the packed state
+    single = L.Domain(L.LuleshProblem(nx=4))
+    with pytest.raises(L.LuleshError):
+        single.load_state(path)

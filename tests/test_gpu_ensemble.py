@@ -161,3 +161,21 @@ def test_c4_draw_matches_oracle(gpu_lib, oracle_mod):
             assert rel_err(a, b, field_floor(f, b)) <= 1e-8, (i, f)
         o.close()
     ens.close()
+
+
+@pytest.mark.gpu
+def test_single_instance_ensemble_is_the_single_problem(gpu_lib):
+    spec = {"nx": 10, "nr": 11, "hgcoef": 2.7, "einit": 1.3 * 3.948746e7 * (10 / 45) ** 3}
+    ens = gpu_lib.Ensemble([spec])
+    dt0 = ens.scalars(0)["deltatime"]
+    ens.run(50)
+    g = gpu_lib.Domain(gpu_lib.LuleshProblem(nx=10, nr=11))
+    g.hgcoef = spec["hgcoef"]
+    e = g.field("e")
+    e[0] = spec["einit"]
+    g.set_field("e", e)
+    g.deltatime = dt0
+    gpu_lib.run(g, 50)
+    for f in STATE:
+        assert np.array_equal(ens.field(0, f), g.field(f)), f
+    assert ens.scalars(0)["time"] == g.time
