@@ -119,3 +119,31 @@ def test_blocks_state_file_resumes_bitwise(gpu_lib, tmp_path):
     single = L.Domain(L.LuleshProblem(nx=4))
     with pytest.raises(L.LuleshError):
         single.load_state(path)
+
+
+@pytest.mark.parametrize("tp,mode", [(2, 0), (3, 7)])
+def test_blocks_from_a_random_state(gpu_lib, tp, mode):
+    """A seeded random state (no symmetry to hide a halo slot read from the
+    wrong neighbour) put into the whole mesh and, through the block map, into
+    every block copy; five steps later every packed value is the whole
+    mesh's bit for bit."""
+    L = gpu_lib
+    whole, blocks = pair(L, 4, tp, mode, keep_aux=True)
+    _, eg, ng = blocks.block_map()
+    rng = np.random.default_rng(0xB10C + tp)
+    E, N = whole.numElem, whole.numNode
+    state = {"e": rng.uniform(0, 2e4, E) * (rng.random(E) < 0.7),
+             "p": rng.uniform(0, 1e3, E) * (rng.random(E) < 0.5),
+             "q": rng.uniform(0, 50, E) * (rng.random(E) < 0.3),
+             "v": rng.uniform(0.97, 1.03, E), "ss": rng.uniform(0, 50, E)}
+    for f in ("xd", "yd", "zd"):
+        state[f] = rng.normal(0, 0.5, N) * (rng.random(N) < 0.6)
+    for f, v in state.items():
+        whole.set_field(f, v)
+        blocks.set_field(f, v[ng] if f in NODE else v[eg])
+    for _ in range(5):
+        L.timeIncrement(whole)
+        L.lagrangeLeapFrog(whole)
+        L.timeIncrement(blocks)
+        L.lagrangeLeapFrog(blocks)
+    assert_same(whole, blocks, STATE + STEP + ["fx", "fy", "fz", "ql", "qq"])
