@@ -244,7 +244,8 @@ int lulesh_autotune(lulesh_domain* dom, int32_t cycles, lulesh_tuning* chosen);
  * instances' elements and nodes are packed into one index space, so every
  * kernel launch covers every instance whatever their sizes; each instance
  * keeps its own dt, time, cycle and status, computed on the device. A run is
- * a sequence of CUDA-graph launches with no host work per cycle. The
+ * one launch of a CUDA graph of the whole run (runs over 512 cycles relaunch
+ * it) with no host work per cycle. The
  * reference has one problem per process; this batches Domain(prob) /
  * timeIncrement! / lagrangeLeapFrog over instances. */
 typedef struct {
