@@ -381,20 +381,29 @@ int lulesh_create(const lulesh_params* params, lulesh_domain** out) {
   // 8*numElem must fit a 32-bit index
   if (!valid_params(params)) return LULESH_ERR_ARGUMENT;
   HostMesh m;
-  build_mesh(m, params->nx, params->nr, params->balance, params->cost, params->region_seed);
+  try {
+    build_mesh(m, params->nx, params->nr, params->balance, params->cost, params->region_seed);
+  } catch (const std::bad_alloc&) {
+    return LULESH_ERR_MEMORY;  // the host mesh did not fit
+  }
   return create_domain(params, m, out);
 }
 
 // The packed block mesh of (nx*tp)^3 elements in tp^3 blocks; 0 or the error.
 static int block_mesh(HostMesh& m, int nx, int tp, int nr, int balance, int cost, int mode, uint64_t seed) {
-  const int64_t nxg = (int64_t)nx * tp;
-  // every packed index (corner slots and corner-list entries included) must fit 31 bits
-  if (tp < 1 || nx < 1 || nxg > 600) return LULESH_ERR_ARGUMENT;
-  HostMesh g;
-  build_mesh(g, (int)nxg, 1, 1, 1, 0);
-  build_block_mesh(m, g, nx, tp, mode);
-  if (m.nCornerSlot >= INT32_MAX || m.nCornerList >= INT32_MAX || m.Eg >= INT32_MAX) return LULESH_ERR_ARGUMENT;
-  build_regions(m, nr, balance, cost, seed);
+  if (tp < 1 || nx < 1 || (int64_t)nx * tp > 600) return LULESH_ERR_ARGUMENT;
+  // every packed index must fit 31 bits: the corner list (at most 8 entries
+  // per packed node) bounds the corner slots and ghost slots as well
+  const int64_t en = nx + 1, packed_nodes = (int64_t)tp * tp * tp * en * en * en;
+  if (8 * packed_nodes >= INT32_MAX) return LULESH_ERR_ARGUMENT;
+  try {
+    HostMesh g;
+    build_mesh(g, nx * tp, 1, 1, 1, 0);
+    build_block_mesh(m, g, nx, tp, mode);
+    build_regions(m, nr, balance, cost, seed);
+  } catch (const std::bad_alloc&) {
+    return LULESH_ERR_MEMORY;
+  }
   return LULESH_OK;
 }
 
