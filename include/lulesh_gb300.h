@@ -204,7 +204,10 @@ const char* lulesh_kernel_name(int32_t index);
  * owns it. The result is bitwise the single-block run of the whole mesh.
  * Every other call (step, run, fields, state files, tuning) works on the
  * packed arrays; lulesh_block_map gives each packed element's and node's id
- * in the whole mesh. The region cost model and the adjoint need one block.
+ * in the whole mesh. Each block holds its rank's region sets (draws seeded
+ * with region_seed + rank, numbers rotated by the rank; the nr-sized region
+ * arrays a field download returns are rank 0's), so the region cost model
+ * works on a block mesh; the adjoint needs one block.
  * lulesh_block_plan_sizes / lulesh_block_plan return the decomposition and
  * its halo plan without a GPU: per ghost slot the packed element (delv) or
  * corner-force slot c*E + e (corners) it copies and the block it belongs to;

@@ -188,4 +188,34 @@ void build_block_mesh(HostMesh& m, const HostMesh& g, int nx, int tp, int mode) 
   m.nCornerSlot = 8 * E + (int64_t)m.haloCornerSrc.size();
 }
 
+void build_block_regions(HostMesh& m, int nx, int tp, int nr, int balance, int cost, uint64_t seed) {
+  const int64_t Eb = (int64_t)nx * nx * nx, nb = (int64_t)tp * tp * tp, E = nb * Eb;
+  m.regNumList.assign(E, 0);
+  m.regElemlist.assign(E, 0);
+  m.regionOrder.assign(E, 0);
+  m.regionReps.assign(E, 0);
+  for (int64_t b = 0; b < nb; ++b) {
+    HostMesh r;
+    r.E = Eb;
+    build_regions(r, nr, balance, cost, seed + (uint64_t)b, (int)b);
+    const int64_t off = b * Eb;
+    int64_t pos = 0;
+    for (size_t q = 0; q < r.regElemSize.size(); ++q)
+      for (int64_t k = 0; k < r.regElemSize[q]; ++k, ++pos) {
+        m.regionOrder[off + pos] = (int)(off + r.regElemlist[pos] - 1);
+        m.regionReps[off + pos] = (int)r.regReps[q];
+      }
+    for (int64_t k = 0; k < Eb; ++k) {
+      m.regNumList[off + k] = r.regNumList[k];
+      m.regElemlist[off + k] = off + r.regElemlist[k];
+    }
+    if (b == 0) {
+      m.regCSR = r.regCSR;
+      m.regReps = r.regReps;
+      m.regSorted = r.regSorted;
+      m.regElemSize = r.regElemSize;
+    }
+  }
+}
+
 }  // namespace lulesh

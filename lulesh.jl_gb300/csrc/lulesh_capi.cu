@@ -342,13 +342,19 @@ static int create_domain(const lulesh_params* params, HostMesh& m, lulesh_domain
   if (d->params.region_reps) {
     // the region cost model: elements in region order (regElemlist, grouped by
     // sorted region) and each position's region rep count
+    // (a block mesh brings both, block after block)
     std::vector<int> order(E), reps(E);
-    int64_t pos = 0;
-    for (size_t r = 0; r < m.regElemSize.size(); ++r)
-      for (int64_t k = 0; k < m.regElemSize[r]; ++k, ++pos) {
-        order[pos] = (int)(m.regElemlist[pos] - 1);
-        reps[pos] = (int)m.regReps[r];
-      }
+    if (!m.regionOrder.empty()) {
+      order = m.regionOrder;
+      reps = m.regionReps;
+    } else {
+      int64_t pos = 0;
+      for (size_t r = 0; r < m.regElemSize.size(); ++r)
+        for (int64_t k = 0; k < m.regElemSize[r]; ++k, ++pos) {
+          order[pos] = (int)(m.regElemlist[pos] - 1);
+          reps[pos] = (int)m.regReps[r];
+        }
+    }
     if ((err = cudaMalloc(&d->region_buf, 2 * (size_t)E * sizeof(int))) != cudaSuccess) {
       cudaGetLastError();
       d->region_buf = nullptr;
@@ -400,7 +406,7 @@ static int block_mesh(HostMesh& m, int nx, int tp, int nr, int balance, int cost
     HostMesh g;
     build_mesh(g, nx * tp, 1, 1, 1, 0);
     build_block_mesh(m, g, nx, tp, mode);
-    build_regions(m, nr, balance, cost, seed);
+    build_block_regions(m, nx, tp, nr, balance, cost, seed);
   } catch (const std::bad_alloc&) {
     return LULESH_ERR_MEMORY;
   }
@@ -410,7 +416,7 @@ static int block_mesh(HostMesh& m, int nx, int tp, int nr, int balance, int cost
 int lulesh_create_blocks(const lulesh_params* params, int32_t blocks_per_edge, lulesh_domain** out) {
   if (!params || !out) return LULESH_ERR_ARGUMENT;
   *out = nullptr;
-  if (!valid_params(params) || params->region_reps) return LULESH_ERR_ARGUMENT;
+  if (!valid_params(params)) return LULESH_ERR_ARGUMENT;
   HostMesh m;
   int rc = block_mesh(m, params->nx, blocks_per_edge, params->nr, params->balance, params->cost, params->mode,
                       params->region_seed);

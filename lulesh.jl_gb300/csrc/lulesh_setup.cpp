@@ -33,7 +33,7 @@ static double elem_volume(const double x[8], const double y[8], const double z[8
   return v * (1.0 / 12.0);
 }
 
-void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed) {
+void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed, int rank) {
   const int64_t E = m.E;
   std::mt19937_64 rng(seed);
   // Julia's rand(Int) is a signed 64-bit draw; its % keeps the dividend's sign.
@@ -56,7 +56,7 @@ void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed) {
       const int64_t r = draw() % denom;
       int64_t i = 0;
       while (r >= binEnd[i]) ++i;
-      return (i % nr) + 1;  // rotation by rank 0
+      return ((i + rank) % nr) + 1;  // region numbers rotate by the rank
     };
     while (next < E) {
       int64_t region = pick();

@@ -28,6 +28,7 @@ struct HostMesh {
   std::vector<int> haloDelvSrc, haloDelvDst;      // per ghost delv slot: source element, receiving block
   std::vector<int> haloCornerSrc, haloCornerDst;  // per ghost corner slot: source slot c*E + e, receiving block
   std::vector<int> elemGlobal, nodeGlobal;        // packed -> global element / node of the whole mesh
+  std::vector<int> regionOrder, regionReps;       // region cost model of a block mesh (build_block_regions)
 };
 
 // Builds the nx^3 single-rank Sedov mesh exactly as Domain(prob) does. A
@@ -35,8 +36,18 @@ struct HostMesh {
 // the initial dt computed from it); 0 keeps 3.948746e7*(nx/45)^3.
 void build_mesh(HostMesh& m, int nx, int nr, int balance, int cost, uint64_t seed, double einit = 0.0);
 
-// createRegionIndexSets! (results-neutral region layout).
-void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed);
+// createRegionIndexSets! (results-neutral region layout) of rank `rank`: the
+// reference seeds each rank's draws with its rank and rotates the region
+// numbers by it (src/domain.jl:338-465); a single rank is rank 0.
+void build_regions(HostMesh& m, int nr, int balance, int cost, uint64_t seed, int rank = 0);
+
+// The region sets of a block mesh: block b gets rank b's (draws seeded with
+// seed + b, numbers rotated by b) over its own elements. regNumList and
+// regElemlist hold every block's entries in packed order (regElemlist's
+// 1-based ids are packed ids); regCSR, regReps, regSorted and regElemSize are
+// block 0's; regionOrder / regionReps give the cost model's packed element
+// of every position and its rep count, block after block.
+void build_block_regions(HostMesh& m, int nx, int tp, int nr, int balance, int cost, uint64_t seed);
 
 // The reference's multi-rank decomposition (initMeshDecomp, src/LULESH.jl:62-97:
 // tp^3 ranks, rank r the block col = r % tp, row = (r / tp) % tp,

@@ -83,8 +83,6 @@ def test_blocks_errors_and_limits(gpu_lib):
     _, blocks = pair(L, 3, 2, 0)
     with pytest.raises(L.LuleshError):
         L.Adjoint(blocks)  # the adjoint kernels have no halo transposes
-    with pytest.raises(L.LuleshError):
-        L.Domain(L.LuleshProblem(nx=3, blocks_per_edge=2, region_reps=True))
     # an error in one block stops every block: a QStop provoked on the host
     L.run(blocks, 10)
     blocks.qstop = 1e-30
@@ -147,3 +145,28 @@ def test_blocks_from_a_random_state(gpu_lib, tp, mode):
         L.timeIncrement(blocks)
         L.lagrangeLeapFrog(blocks)
     assert_same(whole, blocks, STATE + STEP + ["fx", "fy", "fz", "ql", "qq"])
+
+
+def test_blocks_regions_per_rank_and_cost_model(gpu_lib):
+    """Each block holds the region sets of its rank (draws seeded with the
+    rank, region numbers rotated by it, src/domain.jl:338-465): block 0's are
+    the single-rank sets of an nx^3 mesh. The region cost model (balance 4,
+    cost 2, per-region EOS repetitions in region order) runs on the block
+    mesh and leaves the results bitwise those of the whole mesh without it."""
+    L = gpu_lib
+    nx, tp = 5, 2
+    blocks = L.Domain(L.LuleshProblem(nx=nx, nr=11, balance=4, cost=2, region_reps=True, blocks_per_edge=tp))
+    single = L.Domain(L.LuleshProblem(nx=nx, nr=11, balance=4, cost=2))
+    Eb = nx ** 3
+    reg = blocks.field("regNumList")
+    assert np.array_equal(reg[:Eb], single.field("regNumList"))
+    assert not np.array_equal(reg[:Eb], reg[Eb:2 * Eb])
+    for n in ("regReps", "regElemSize", "regSorted"):
+        assert np.array_equal(blocks.field(n), single.field(n)), n
+    el = blocks.field("regElemlist")
+    for b in range(tp ** 3):  # each block's index set covers its own elements
+        assert np.array_equal(np.sort(el[b * Eb:(b + 1) * Eb]), np.arange(b * Eb, (b + 1) * Eb) + 1)
+    whole = L.Domain(L.LuleshProblem(nx=nx * tp, nr=11, balance=4, cost=2))
+    L.run(whole, 40)
+    L.run(blocks, 40)
+    assert_same(whole, blocks, STATE)
