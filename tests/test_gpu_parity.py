@@ -84,16 +84,16 @@ def test_first_steps_match(gpu_lib, oracle_mod, mode):
         assert_fields(g, o, STEP_F64 + AUX_F64, where=f"step {step}")
 
 
-@pytest.mark.parametrize("seed", range(6))
-@pytest.mark.parametrize("mode", [0, 7])
-def test_random_states_match_oracle(gpu_lib, oracle_mod, mode, seed):
-    """Seeded random states on the 6^3 mesh (energies, pressures, viscosities,
+@pytest.mark.parametrize("nx,seed", [(6, s) for s in range(6)] + [(12, 100), (12, 101)])
+@pytest.mark.parametrize("mode", [0, 1, 2, 4, 7])
+def test_random_states_match_oracle(gpu_lib, oracle_mod, mode, nx, seed):
+    """Seeded random states on 6^3 and 12^3 meshes (energies, pressures, viscosities,
     sound speeds, relative volumes within 3 % of 1, velocities with exact
     zeros, a random hourglass coefficient) stepped three cycles with every
     step and auxiliary field compared: the limiter's cases, the clamps, the
     cut-offs and the EOS branches that the Sedov blast reaches rarely or late."""
     rng = np.random.default_rng(seed)
-    g, o = pair(gpu_lib, oracle_mod, 6, mode=mode, keep_aux=True)
+    g, o = pair(gpu_lib, oracle_mod, nx, mode=mode, keep_aux=True)
     E, N = g.numElem, g.numNode
     state = {"e": rng.uniform(0, 2e4, E) * (rng.random(E) < 0.7),
              "p": rng.uniform(0, 1e3, E) * (rng.random(E) < 0.5),
