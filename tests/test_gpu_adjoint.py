@@ -121,6 +121,57 @@ def test_one_cycle_block_dot_products(gpu_lib, oracle_mod, mode):
     assert not bad, bad
 
 
+@pytest.mark.parametrize("mode,seed", [(0, 0xD0), (0, 0xD1), (7, 0xD2)])
+def test_one_cycle_dot_products_from_random_states(gpu_lib, oracle_mod, mode, seed):
+    """The block dot products of one cycle from a seeded random state
+    (positive energies, random pressures, viscosities, sound speeds, relative
+    volumes within 3 % of 1, velocities with exact zeros, random hourglass
+    coefficient), which takes the transposes through limiter cases, clamps
+    and the compression / expansion branches of the EOS that a developed
+    Sedov state at one cycle does not reach."""
+    L = gpu_lib
+    nx = 6
+    g = L.Domain(L.LuleshProblem(nx=nx, mode=mode))
+    rng = np.random.default_rng(seed)
+    E, N = g.numElem, g.numNode
+    g.set_field("e", rng.uniform(1e2, 2e4, E))
+    g.set_field("p", rng.uniform(0, 1e3, E) * (rng.random(E) < 0.5))
+    g.set_field("q", rng.uniform(0, 50, E) * (rng.random(E) < 0.3))
+    g.set_field("v", rng.uniform(0.97, 1.03, E))
+    g.set_field("ss", rng.uniform(1, 50, E))
+    for f in ("xd", "yd", "zd"):
+        g.set_field(f, rng.normal(0, 0.5, N) * (rng.random(N) < 0.6))
+    g.hgcoef = float(rng.uniform(1, 4))
+    snap = snapshot(g)
+    fields = snap[0]
+    w = {f: rng.standard_normal(fields[f].size) for f in STATE}
+    scale = {f: np.mean(np.abs(fields[f])) + 1e-3 for f in STATE}
+    v = {f: rng.standard_normal(fields[f].size) * scale[f] for f in STATE}
+    jv = {}
+    for fi in STATE:
+        d = dual_from(oracle_mod, snap, nx, mode)
+        d.set_field(fi, fields[fi], v[fi])
+        assert d.cycles(1) == 0
+        jv[fi] = {fo: d.field(fo)[1] for fo in STATE}
+    adj = L.Adjoint(g, checkpoint_every=1)
+    bad = []
+    for fo in STATE:
+        restore(g, snap)
+        adj.clear_seeds()
+        adj.set_seed(fo, w[fo])
+        adj.gradient(1)
+        for fi in STATE:
+            a = float(np.dot(w[fo], jv[fi][fo]))
+            a_scale = float(np.dot(np.abs(w[fo]), np.abs(jv[fi][fo])))
+            gi = adj.grad(fi)
+            b = float(np.dot(gi, v[fi]))
+            b_scale = float(np.dot(np.abs(gi), np.abs(v[fi])))
+            if not close(a, b, max(a_scale, b_scale), 1e-10):
+                bad.append((fo, fi, a, b, max(a_scale, b_scale)))
+    adj.close()
+    assert not bad, bad
+
+
 @pytest.mark.parametrize("mode,hgcoef", [(0, None), (1, None), (2, None), (7, None), (0, 0.0)])
 def test_run_gradient_matches_dual_oracle(gpu_lib, oracle_mod, mode, hgcoef):
     """Modes 1 and 2 take the face-5 and volume-derivative corrections one
