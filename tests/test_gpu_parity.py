@@ -116,6 +116,51 @@ def test_random_states_match_oracle(gpu_lib, oracle_mod, mode, nx, seed):
         assert_fields(g, o, STEP_F64 + AUX_F64, where=f"step {step}")
 
 
+# The limiter's face masks (interior 0, then symmetry, free and comm bits of
+# each face's three), src/types.jl's XI_M .. ZETA_P_COMM
+FACE_BITS = [(0x1, 0x2, 0x4), (0x8, 0x10, 0x20), (0x40, 0x80, 0x100),
+             (0x200, 0x400, 0x800), (0x1000, 0x2000, 0x4000), (0x8000, 0x10000, 0x20000)]
+NEIGHBOURS = ["lxim", "lxip", "letam", "letap", "lzetam", "lzetap"]
+
+
+@pytest.mark.parametrize("mode,seed", [(0, 0xBC0), (1, 0xBC1), (4, 0xBC2), (7, 0xBC3)])
+def test_random_boundary_masks_and_neighbours_match_oracle(gpu_lib, oracle_mod, mode, seed):
+    """Every face of every element takes a random limiter case (interior,
+    symmetry, free or comm; src/domain.jl:2330-2420) and a random neighbour
+    element, on a random state: the GPU's neighbour reads, the faithful
+    xi-plus offset included, are the oracle's in every case. A single-rank
+    Sedov mesh has no comm faces and symmetry or free faces only on its six
+    boundary planes."""
+    rng = np.random.default_rng(seed)
+    g, o = pair(gpu_lib, oracle_mod, 6, mode=mode, keep_aux=True)
+    E, N = g.numElem, g.numNode
+    state = {"e": rng.uniform(0, 2e4, E), "p": rng.uniform(0, 1e3, E) * (rng.random(E) < 0.5),
+             "q": rng.uniform(0, 50, E) * (rng.random(E) < 0.3), "v": rng.uniform(0.97, 1.03, E),
+             "ss": rng.uniform(0, 50, E)}
+    for f in ("xd", "yd", "zd"):
+        state[f] = rng.normal(0, 0.5, N)
+    bc = np.zeros(E, np.uint32)
+    for bits in FACE_BITS:
+        bc |= np.array((0,) + bits, np.uint32)[rng.integers(0, 4, E)]
+    state["elemBC"] = bc
+    for name in NEIGHBOURS:
+        # the faithful xi-plus read is element lxip - 1, so lxip >= 1 there
+        lo = 1 if (name == "lxip" and not mode & 4) else 0
+        state[name] = rng.integers(lo, E, E).astype(np.int64)
+    for f, v in state.items():
+        g.set_field(f, v)
+        o.set_field(f, v)
+    for n in ["elemBC"] + NEIGHBOURS:
+        assert np.array_equal(g.field(n), o.field(n)), n
+    for step in range(3):
+        gpu_lib.timeIncrement(g)
+        o.time_increment()
+        gpu_lib.lagrangeLeapFrog(g)
+        assert o.lagrange_leapfrog() == 0
+        assert_scalars(g, o)
+        assert_fields(g, o, STEP_F64 + AUX_F64, where=f"step {step}")
+
+
 @pytest.mark.parametrize("mode", [0, 7])
 def test_one_step_from_developed_state(gpu_lib, oracle_mod, mode):
     """Load the oracle's state after 120 cycles into the GPU and take one step."""
