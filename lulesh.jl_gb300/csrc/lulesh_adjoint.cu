@@ -35,6 +35,7 @@
 #include "lulesh_adjoint_kernels.cuh"
 #include "lulesh_device.cuh"
 #include "lulesh_handle.h"
+#include "lulesh_trace.h"
 
 using namespace lulesh;
 
@@ -629,6 +630,7 @@ int lulesh_adj_loss(lulesh_adjoint* a, double* loss) {
 
 int lulesh_adj_gradient(lulesh_adjoint* a, int64_t num_cycles, lulesh_adj_result* res) {
   if (!a || num_cycles < 1) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("lulesh_adj_gradient");
   lulesh_domain* d = a->dom;
   ACK(cudaSetDevice(d->params.device));
   cudaStream_t s = d->stream;

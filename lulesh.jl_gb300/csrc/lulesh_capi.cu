@@ -16,6 +16,7 @@
 #include "lulesh_arena.h"
 #include "lulesh_handle.h"
 #include "lulesh_device.cuh"
+#include "lulesh_trace.h"
 
 using namespace lulesh;
 
@@ -221,15 +222,30 @@ static int launch_step(lulesh_domain* d, const Params& prm, bool with_time_incre
     d->ring_used += 1;
   }
   if (ev) cudaEventRecord(ev[0], s);
-  if (with_time_increment) launch_time_increment(d->dd.st, 1, prm, s);
+  if (with_time_increment) {
+    TraceRange r("timeIncrement!");
+    launch_time_increment(d->dd.st, 1, prm, s);
+  }
   if (ev) cudaEventRecord(ev[1], s);
-  launch_force(d->dd, prm, d->tuning, s);
+  {
+    TraceRange r("calcForceForNodes");
+    launch_force(d->dd, prm, d->tuning, s);
+  }
   if (ev) cudaEventRecord(ev[2], s);
-  launch_node(d->dd, prm, aux, d->tuning, s);
+  {
+    TraceRange r("calcAccelerationForNodes .. calcPositionForNodes");
+    launch_node(d->dd, prm, aux, d->tuning, s);
+  }
   if (ev) cudaEventRecord(ev[3], s);
-  launch_kinematics(d->dd, prm, aux, d->tuning, s);
+  {
+    TraceRange r("calcLagrangeElements + calcMonotonicQGradientsForElems");
+    launch_kinematics(d->dd, prm, aux, d->tuning, s);
+  }
   if (ev) cudaEventRecord(ev[4], s);
-  launch_material(d->dd, prm, aux, d->tuning, s);
+  {
+    TraceRange r("calcQForElems .. calcTimeConstraintsForElems");
+    launch_material(d->dd, prm, aux, d->tuning, s);
+  }
   if (ev) cudaEventRecord(ev[5], s);
   CK(cudaGetLastError());
   return LULESH_OK;
@@ -493,6 +509,7 @@ int lulesh_get_stream(lulesh_domain* d, void** stream) {
 
 int lulesh_time_increment(lulesh_domain* d) {
   if (!d) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("timeIncrement!");
   const Params prm = make_params(d);
   double time = d->sc[LULESH_S_TIME], dt = d->sc[LULESH_S_DELTATIME];
   long long cycle = (long long)d->sc[LULESH_S_CYCLE];
@@ -505,6 +522,7 @@ int lulesh_time_increment(lulesh_domain* d) {
 
 int lulesh_lagrange_leapfrog(lulesh_domain* d) {
   if (!d) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("lagrangeLeapFrog");
   CK(cudaSetDevice(d->params.device));
   const Params prm = make_params(d);
   state_to_device_mirror(d);
@@ -524,6 +542,7 @@ int lulesh_lagrange_leapfrog(lulesh_domain* d) {
 
 int lulesh_run(lulesh_domain* d, int64_t num_iters, lulesh_scalars* out) {
   if (!d) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("lulesh_run");
   CK(cudaSetDevice(d->params.device));
   const Params prm = make_params(d);
   state_to_device_mirror(d);
@@ -905,6 +924,7 @@ int lulesh_set_tuning(lulesh_domain* d, const lulesh_tuning* t) {
 
 int lulesh_autotune(lulesh_domain* d, int32_t cycles, lulesh_tuning* chosen) {
   if (!d) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("lulesh_autotune");
   CK(cudaSetDevice(d->params.device));
   cudaStream_t s = d->stream;
   // save the fields the tuning cycles change, then restore them and the scalars

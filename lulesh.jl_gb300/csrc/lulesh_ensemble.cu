@@ -27,6 +27,7 @@
 #include "lulesh_device.cuh"
 #include "lulesh_handle.h"
 #include "lulesh_internal.h"
+#include "lulesh_trace.h"
 #include "lulesh_kernels.h"
 #include "lulesh_setup.h"
 
@@ -319,6 +320,7 @@ int lulesh_ens_reset(lulesh_ensemble* s) {
 
 int lulesh_ens_run(lulesh_ensemble* s, int64_t num_iters) {
   if (!s) return LULESH_ERR_ARGUMENT;
+  TraceRange trace("lulesh_ens_run");
   ECK(cudaSetDevice(s->device));
   cudaStream_t st = s->stream;
   // every instance becomes runnable again (first = 1): benchmark.jl semantics per instance
