@@ -928,7 +928,10 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       return pn;
     };
     const double pq_old = p_old + q_old;
-    double e_new = fma(-0.5 * delvc, pq_old, e_old);
+    // 0.5 delvc and pHalfStep + q_new serve both energy updates (the negated
+    // and scaled forms are exact, so the values are those of separate products)
+    const double hdv = 0.5 * delvc;
+    double e_new = fma(-hdv, pq_old, e_old);
     if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E1_MIN; }
     const double bvc_half = c1s * bvh;
     const double pHalfStep = pressure(e_new, bvc_half, TF_PH_CUT, TF_PH_MIN);
@@ -947,7 +950,8 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       tm(19, 0.0); tm(28, 0.0);
     }
     tm(20, q_new);
-    e_new = fma(0.5 * delvc, fma(3.0, pq_old, -4.0 * (pHalfStep + q_new)), e_new);
+    const double sh = pHalfStep + q_new;
+    e_new = fma(hdv, fma(3.0, pq_old, -4.0 * sh), e_new);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E2_CUT; }
     if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E2_MIN; }
     const double bvc = c1s * bv;
@@ -964,7 +968,7 @@ __global__ void __launch_bounds__(kMaxElemBlock) k_material(DevDomain d, Params 
       tm(23, 0.0); tm(29, 0.0);
     }
     tm(24, q_tilde);
-    e_new = e_new - ((fma(7.0, pq_old, -8.0 * (pHalfStep + q_new)) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
+    e_new = e_new - ((fma(7.0, pq_old, -8.0 * sh) + (p_new + q_tilde)) * delvc) * (1.0 / 6.0);
     if (abs_lt(e_new, prm.e_cut)) { e_new = 0.0; if (TAPE) fl |= TF_E3_CUT; }
     if (fkey(e_new) < prm.k_emin) { e_new = prm.emin; if (TAPE) fl |= TF_E3_MIN; }
     p_new = pressure(e_new, bvc, TF_PN2_CUT, TF_PN2_MIN);
