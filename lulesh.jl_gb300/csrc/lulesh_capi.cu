@@ -40,6 +40,7 @@ static int cuda_fail(cudaError_t e) {
 
 Params lulesh::make_params(const lulesh_domain* d) {
   Params p;
+  std::memset(&p, 0, sizeof p);  // padding too: parameter sets are compared bytewise
   p.u_cut = d->sc[LULESH_S_U_CUT];
   p.hgcoef = d->sc[LULESH_S_HGCOEF];
   p.qstop = d->sc[LULESH_S_QSTOP];

@@ -48,6 +48,7 @@ int cuda_rc(cudaError_t e) {
 // The reference's parameters (src/domain.jl:663-701), shared by all instances.
 Params reference_params() {
   Params p;
+  std::memset(&p, 0, sizeof p);  // padding too: parameter sets are compared bytewise
   p.u_cut = 1.0e-7; p.hgcoef = 3.0; p.qstop = 1.0e+12; p.monoq_max_slope = 1.0;
   p.monoq_limiter_mult = 2.0; p.e_cut = 1.0e-7; p.p_cut = 1.0e-7; p.q_cut = 1.0e-7;
   p.v_cut = 1.0e-10; p.qlc_monoq = 0.5; p.qqc_monoq = 2.0 / 3.0; p.qqc = 2.0;
