@@ -96,17 +96,6 @@ __device__ __forceinline__ void cross(double ax, double ay, double az, double bx
   cz = fma(ax, by, -ay * bx);
 }
 
-// triple_product of calcElemVolume, src/utils.jl:40-43; t receives its
-// cross-product factor (the same values the product uses).
-__device__ __forceinline__ double triple(double x1, double y1, double z1, double x2, double y2,
-                                        double z2, double x3, double y3, double z3, double* t = nullptr) {
-  const double t1 = fma(y2, z3, -z2 * y3);
-  const double t2 = fma(z1, y3, -y1 * z3);
-  const double t3 = fma(y1, z2, -z1 * y2);
-  if (t) { t[0] = t1; t[1] = t2; t[2] = t3; }
-  return fma(x1, t1, fma(x2, t2, x3 * t3));
-}
-
 // Integer-pipe helpers for exact tests on FP64 values (keeps DSETP off the
 // scarce FP64 pipe). Valid for non-NaN inputs.
 __device__ __forceinline__ bool le_zero(double a) {  // a <= 0.0

@@ -704,11 +704,6 @@ __device__ __forceinline__ double monoq_neighbour(const double* dv, unsigned mas
   return 0.0;
 }
 
-// TINY-guarded sound-speed square root, src/domain.jl:2655-2659.
-__device__ __forceinline__ double ssc_sqrt(double ssc) {
-  return (ssc <= 0.111111e-36) ? 0.333333e-18 : sqrt(ssc);
-}
-
 __device__ __forceinline__ void block_min2(unsigned long long a, unsigned long long b,
                                            unsigned long long* ga, unsigned long long* gb) {
   __shared__ unsigned long long sa[32], sb[32];
