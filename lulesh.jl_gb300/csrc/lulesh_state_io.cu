@@ -70,7 +70,7 @@ int lulesh_save_state(lulesh_domain* d, const char* path) {
   }
   FILE* f = std::fopen(path, "wb");
   if (!f) return LULESH_ERR_ARGUMENT;
-  Writer w{f};
+  Writer w{f, Hash{}, true};
   if (std::fwrite(kMagic, 1, 8, f) != 8) w.ok = false;
   const lulesh_params& p = d->params;
   const int32_t head[6] = {kVersion, p.nx, p.nr, p.balance, p.cost, p.mode};
@@ -96,7 +96,7 @@ int lulesh_load_state(lulesh_domain* d, const char* path) {
   if (!d || !path) return LULESH_ERR_ARGUMENT;
   FILE* f = std::fopen(path, "rb");
   if (!f) return LULESH_ERR_ARGUMENT;
-  Reader r{f};
+  Reader r{f, Hash{}, true};
   char magic[8];
   if (std::fread(magic, 1, 8, f) != 8 || std::memcmp(magic, kMagic, 8) != 0) { std::fclose(f); return LULESH_ERR_ARGUMENT; }
   int32_t head[6];
