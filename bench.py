@@ -449,6 +449,56 @@ def c3_leg(L, torch, dev, nx, cycles, warmup=2):
     return out
 
 
+def c1_leg(L, torch, dev, cpu=True, cpu_seconds=3.0):
+    """Config C1, the reference's CPU-runnable case: the 30^3 Sedov problem
+    (11 regions) run to stoptime 1e-2 in the corrected mode (LULESH 2.0's
+    method; 932 cycles) and, in the faithful mode, whose dt collapses before
+    stoptime, for 1000 cycles. Each whole run is timed on the GPU through
+    lulesh_run (after a run of another handle of the same problem), and the
+    oracle on the host cores: the OpenMP build over the whole corrected run,
+    the serial build over a bounded sample of it."""
+    nx = 30
+    out = {"config": f"Sedov {nx}^3, 11 regions, balance 1, cost 1, FP64, run to stoptime 1e-2", "nx": nx}
+    for mode, iters, key in ((7, 10 ** 9, "corrected_to_stoptime"), (0, 1000, "faithful_1000_cycles")):
+        w = L.Domain(L.LuleshProblem(nx=nx, mode=mode, device=dev))
+        L.run(w, 20)
+        w.close()
+        g = L.Domain(L.LuleshProblem(nx=nx, mode=mode, device=dev))
+        stream = torch.cuda.ExternalStream(g.stream(), device=dev)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        a.record(stream)
+        sc = L.run(g, iters)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        wall = time.perf_counter() - t0
+        ms = a.elapsed_time(b)
+        out[key] = {"cycles": int(sc["cycle"]), "time": sc["time"], "origin_energy": float(g.field("e")[0]),
+                    "gpu_s": ms * 1e-3, "host_wall_s": wall,
+                    "zones_cycles_per_s": nx ** 3 * sc["cycle"] / (ms * 1e-3)}
+        g.close()
+    if cpu:
+        import oracle
+        d = oracle.OracleDomain(nx, nr=11, mode=7, openmp=True)
+        used = oracle.load(True).ora_max_threads()
+        t0 = time.perf_counter()
+        while d.get("time") < d.get("stoptime"):
+            d.time_increment()
+            d.lagrange_leapfrog()
+        dt = time.perf_counter() - t0
+        n = d.get("cycle")
+        d.close()
+        rate1, _, n1, dt1 = cpu_oracle_rate(nx, cpu_seconds, serial=True)
+        out["cpu_baseline"] = {
+            "kind": "port", "openmp": {"cores": used, "cycles": n, "seconds": dt,
+                                       "zones_cycles_per_s": nx ** 3 * n / dt,
+                                       "sample": "the whole corrected run to stoptime (oracle, OpenMP)"},
+            "serial": {"cores": 1, "zones_cycles_per_s": rate1, "projected_run_s": nx ** 3 * n / rate1,
+                       "sample": f"{n1} cycles in {dt1:.1f} s (oracle, serial build, faithful mode)"}}
+    return out
+
+
 def blocks_leg(L, torch, dev, nx, tp, cycles, plain_ms, warmup=3):
     """The multi-rank decomposition on one GPU: the (tp*nx)^3 problem as tp^3
     blocks of nx^3 elements with halo copies across block faces (bitwise the
@@ -613,6 +663,9 @@ def run_ours(args):
     c3 = None
     if not args.no_c3:
         c3 = c3_leg(L, torch, dev, args.c3_nx, args.c3_cycles)
+    c1 = None
+    if not args.no_c1:
+        c1 = c1_leg(L, torch, dev, cpu=world == 1 and not args.no_cpu)
 
     adjoint = None
     if not args.no_adjoint:
@@ -645,7 +698,7 @@ def run_ours(args):
             "clocks": clock_record, "timed_regions": {"repeats": repeats, "cycles_each": cycles,
                                                       "ms_each": region_ms, "reported": "median"},
             "tuning": tuning, "geometry_split": GEOMETRY_SPLIT[tuning["geometry"]], "ensemble": ensemble, "adjoint": adjoint,
-            "c3_unbalanced_regions": c3, "blocks": blocks}
+            "c3_unbalanced_regions": c3, "c1_to_stoptime": c1, "blocks": blocks}
     print(json.dumps(line), flush=True)
     g.close()
     return 0
@@ -670,6 +723,7 @@ def main():
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint leg")
     ap.add_argument("--no-c3", action="store_true", help="skip the unbalanced-regions leg")
     ap.add_argument("--no-blocks", action="store_true", help="skip the multi-block (halo) leg")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 30^3 run-to-stoptime leg")
     ap.add_argument("--c3-nx", type=int, default=256)
     ap.add_argument("--c3-cycles", type=int, default=500)
     ap.add_argument("--adj-nx", type=int, default=48)
