@@ -114,7 +114,8 @@ class ClockSampler:
                 if v.lower() == "active":
                     reasons.add(n)
         if not sms:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"], "samples": 0}
+            why = "nvidia-smi unavailable" if self.proc is None else "no sample during the timed region"
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [why], "samples": 0}
         sms.sort()
         return {"sm_mhz": sms[len(sms) // 2], "sm_max_mhz": max(maxs), "reasons": sorted(reasons),
                 "samples": len(sms)}
